@@ -1,0 +1,240 @@
+// Runs the reference's own CPU propagators on a seeded instance and prints the
+// result as one JSON line. Test infrastructure: built by oracle/ref/Makefile
+// against the reference sources where they lie (src/Network.cpp, src/AC3.cpp,
+// src/AC3bit.cpp, src/SAC1.cpp, src/MAC.cpp, src/Solver.cpp, src/model/*.cpp)
+// plus the absl/glog shim in oracle/shim. Its outputs pin the oracle
+// restatement and become the golden fixtures under tests/golden/.
+//
+// Usage:
+//   ref_driver binary N D E P_LO P_HI REMOVE SEED  OP [ARG]
+//   ref_driver mixed  N D E P_LO P_HI K3 NTUP REMOVE SEED  OP [ARG]
+//   ref_driver mixedbin (same arguments as mixed; tables dropped)
+//   ref_driver uneven SEED N_LO N_HI D_CAP  OP [ARG]
+// OP: ac3bit | ac3 | sac1 | mac | time_ac REPS | time_branches K
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <sstream>
+#include <string>
+
+#include "Network.h"
+#include "Solver.h"
+#include "model/model_builder.h"
+#include "cp_gen.h"
+
+using namespace cpim;
+
+namespace {
+
+model::IntermediateModel build_model(const cpgen::Instance& I) {
+  model::ModelBuilder b("generated");
+  std::vector<model::DomainId> dom_ids;
+  std::vector<int> dom_size_of_id;
+  std::vector<model::VariableId> vars;
+  for (int x = 0; x < I.n; ++x) {
+    int found = -1;
+    for (size_t k = 0; k < dom_size_of_id.size(); ++k)
+      if (dom_size_of_id[k] == I.dom[x]) found = int(k);
+    if (found < 0) {
+      dom_ids.push_back(b.AddDomain("D" + std::to_string(I.dom[x])).WithRange(0, I.dom[x] - 1).Build());
+      dom_size_of_id.push_back(I.dom[x]);
+      found = int(dom_ids.size()) - 1;
+    }
+    vars.push_back(b.AddVariable("x" + std::to_string(x)).WithDomain(dom_ids[found]).Build());
+  }
+  for (int c = 0; c < I.n_bin(); ++c) {
+    std::vector<std::vector<int>> tuples;
+    const int x = I.bx[c], y = I.by[c];
+    for (int a = 0; a < I.dom[x]; ++a) {
+      const uint64_t* r = I.row(c, a);
+      for (int bv = 0; bv < I.dom[y]; ++bv)
+        if ((r[bv >> 6] >> (bv & 63)) & 1ull) tuples.push_back({a, bv});
+    }
+    b.AddConstraint().AsExtension(model::ExtensionConstraint::Semantics::kSupports,
+                                  {vars[x], vars[y]}, std::move(tuples)).Build();
+  }
+  for (int t = 0; t < I.n_tab(); ++t) {
+    const int r = I.tarity[t];
+    std::vector<model::VariableId> scope;
+    for (int i = 0; i < r; ++i) scope.push_back(vars[I.tscope[I.tscope_off[t] + i]]);
+    std::vector<std::vector<int>> tuples(I.tntup[t], std::vector<int>(r));
+    for (int k = 0; k < I.tntup[t]; ++k)
+      for (int i = 0; i < r; ++i) tuples[k][i] = I.ttup[I.ttup_off[t] + int64_t(k) * r + i];
+    b.AddConstraint().AsExtension(model::ExtensionConstraint::Semantics::kSupports, scope,
+                                  std::move(tuples)).Build();
+  }
+  auto m = std::move(b).Build();
+  if (!m.ok()) {
+    std::cerr << "model build failed: " << m.status().message() << std::endl;
+    std::exit(2);
+  }
+  return std::move(m).value();
+}
+
+void apply_initial_domains(Network& net, const cpgen::Instance& I) {
+  for (int x = 0; x < I.n; ++x)
+    for (int a = 0; a < I.dom[x]; ++a)
+      if (!I.bit(x, a)) net.vars[x]->RemoveValue(a, 0);
+}
+
+std::string domains_hex(Network& net, const cpgen::Instance& I, int level) {
+  std::string s;
+  char buf[17];
+  for (int x = 0; x < I.n; ++x) {
+    auto& bd = net.vars[x]->bitDom(level);
+    for (int w = 0; w < I.W; ++w) {
+      const uint64_t v = w < int(bd.size()) ? bd[w].to_ullong() : 0ull;
+      std::snprintf(buf, sizeof buf, "%016llx", static_cast<unsigned long long>(v));
+      s += buf;
+    }
+  }
+  return s;
+}
+
+struct Silence {
+  std::streambuf* old;
+  std::ofstream null;
+  Silence() : null("/dev/null") { old = std::cout.rdbuf(null.rdbuf()); }
+  ~Silence() { std::cout.rdbuf(old); }
+};
+
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  if (argc < 3) {
+    std::cerr << "usage: see header" << std::endl;
+    return 2;
+  }
+  std::string kind = argv[1];
+  int i = 2;
+  cpgen::Instance I;
+  if (kind == "binary" && argc >= 10) {
+    I = cpgen::random_binary(std::atoi(argv[2]), std::atoi(argv[3]), std::atoll(argv[4]), std::atof(argv[5]),
+                             std::atof(argv[6]), std::atof(argv[7]), std::strtoull(argv[8], nullptr, 10));
+    i = 9;
+  } else if (kind == "mixed" && argc >= 12) {
+    I = cpgen::random_mixed(std::atoi(argv[2]), std::atoi(argv[3]), std::atoll(argv[4]), std::atof(argv[5]),
+                            std::atof(argv[6]), std::atoi(argv[7]), std::atoi(argv[8]), std::atof(argv[9]),
+                            std::strtoull(argv[10], nullptr, 10));
+    i = 11;
+  } else if (kind == "mixedbin" && argc >= 12) {
+    // The binary sub-network of a mixed instance: same binary constraints and
+    // initial domains, tables dropped.
+    I = cpgen::random_mixed(std::atoi(argv[2]), std::atoi(argv[3]), std::atoll(argv[4]), std::atof(argv[5]),
+                            std::atof(argv[6]), std::atoi(argv[7]), std::atoi(argv[8]), std::atof(argv[9]),
+                            std::strtoull(argv[10], nullptr, 10));
+    I.tarity.clear();
+    I.tscope_off.clear();
+    I.tscope.clear();
+    I.tntup.clear();
+    I.ttup_off.clear();
+    I.ttup.clear();
+    i = 11;
+  } else if (kind == "uneven" && argc >= 7) {
+    I = cpgen::uneven_instance(std::strtoull(argv[2], nullptr, 10), std::atoi(argv[3]), std::atoi(argv[4]),
+                               std::atoi(argv[5]));
+    i = 6;
+  } else {
+    std::cerr << "bad arguments" << std::endl;
+    return 2;
+  }
+  const std::string op = argv[i];
+  const long arg = (i + 1 < argc) ? std::atol(argv[i + 1]) : 0;
+
+  model::IntermediateModel m = build_model(I);
+  Network net(m);
+  apply_initial_domains(net, I);
+
+  std::ostringstream out;
+  char fp[32];
+  std::snprintf(fp, sizeof fp, "%016llx", static_cast<unsigned long long>(cpgen::fingerprint(I)));
+  out << "{\"fingerprint\": \"" << fp << "\", \"n\": " << I.n << ", \"W\": " << I.W;
+
+  if (op == "ac3bit" || op == "ac3") {
+    AC* ac = (op == "ac3bit") ? static_cast<AC*>(new AC3bit(&net)) : static_cast<AC*>(new AC3(&net));
+    ConsistencyState cs;
+    {
+      Silence s;
+      cs = ac->enforce(net.vars, 0);
+    }
+    out << ", \"consistent\": " << (cs.state ? "true" : "false") << ", \"deletions\": " << cs.num_delete;
+    if (cs.state) out << ", \"domains\": \"" << domains_hex(net, I, 0) << "\"";
+    delete ac;
+  } else if (op == "sac1") {
+    SAC1 sac(&net, AC_3bit);
+    bool ok;
+    {
+      Silence s;
+      ok = sac.enforce(net.vars, 0);
+    }
+    out << ", \"consistent\": " << (ok ? "true" : "false") << ", \"deletions\": " << sac.del();
+    if (ok) out << ", \"domains\": \"" << domains_hex(net, I, 0) << "\"";
+  } else if (op == "mac") {
+    MAC mac(&net, AC_3bit, Heuristic::VRH_DOM_MIN, Heuristic::VLH_MIN);
+    SearchStatistics st;
+    {
+      Silence s;
+      st = mac.enforce(arg > 0 ? int(arg) : 600000);
+    }
+    out << ", \"num_positive\": " << st.num_positive << ", \"num_negative\": " << st.num_negative
+        << ", \"num_sol\": " << st.num_sol << ", \"time_out\": " << (st.time_out ? "true" : "false")
+        << ", \"solution\": [";
+    for (size_t k = 0; k < mac.solution.size(); ++k) out << (k ? ", " : "") << mac.solution[k];
+    out << "]";
+  } else if (op == "time_ac") {
+    const int reps = arg > 0 ? int(arg) : 3;
+    AC3bit ac(&net);
+    double best = 1e30;
+    int dels = 0;
+    bool ok = true;
+    for (int r = 0; r < reps; ++r) {
+      net.CopyLevel(0, 1);
+      const double t0 = now_s();
+      auto cs = ac.enforce(net.vars, 1);
+      const double t1 = now_s();
+      best = std::min(best, t1 - t0);
+      dels = cs.num_delete;
+      ok = cs.state;
+    }
+    out << ", \"consistent\": " << (ok ? "true" : "false") << ", \"deletions\": " << dels
+        << ", \"best_s\": " << best;
+  } else if (op == "time_branches") {
+    // The singleton test of SAC1::enforce (src/SAC1.cpp:70-79) on the first K
+    // live (x, a), timed; no deletion is committed.
+    const long K = arg > 0 ? arg : 100;
+    AC3bit ac(&net);
+    std::vector<IntVar*> evt;
+    long done = 0, failed = 0;
+    const double t0 = now_s();
+    for (auto* x : net.vars) {
+      for (int a : x->values()) {
+        if (done >= K) break;
+        if (!x->have(a, 0)) continue;
+        net.CopyLevel(0, net.tmp());
+        x->ReduceTo(a, net.tmp());
+        x->assign(true, net.tmp());
+        evt.push_back(x);
+        failed += ac.enforce(evt, net.tmp()).state ? 0 : 1;
+        evt.clear();
+        x->assign(false, 0);
+        net.ClearLevel(net.tmp());
+        ++done;
+      }
+      if (done >= K) break;
+    }
+    const double t1 = now_s();
+    out << ", \"branches\": " << done << ", \"failed\": " << failed << ", \"seconds\": " << (t1 - t0);
+  } else {
+    std::cerr << "unknown op " << op << std::endl;
+    return 2;
+  }
+  out << "}";
+  std::cout << out.str() << std::endl;
+  return 0;
+}
