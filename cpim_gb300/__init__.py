@@ -1,0 +1,322 @@
+"""GB300-native bitset-domain constraint propagation (AC_3bit, GAC, SAC1).
+
+Python view of the engine's C ABI (include/cpgpu.h). Every call goes to the
+CUDA library cpim_gb300/_build/libcpgpu.so; there is no CPU fallback: if the
+library is missing, importing the engine raises, and on a host without a GPU
+creating an Engine raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libcpgpu.so")
+
+__all__ = ["ACAlgorithm", "VarHeuristic", "ValHeuristic", "Engine", "Net", "Instance", "Stats",
+           "SearchResult", "CPError", "gen_binary", "gen_mixed", "gen_uneven", "lib"]
+
+
+class CPError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("cpgpu error %d: %s" % (code, msg))
+        self.code = code
+
+
+class ACAlgorithm(enum.IntEnum):
+    """include/Solver.h:13-31 (only AC_3bit and, for tables, GAC run here)."""
+    CA_AC1 = 0
+    CA_AC2 = 1
+    AC_3 = 2
+    AC_4 = 3
+    AC_6 = 4
+    AC_7 = 5
+    AC_2001 = 6
+    AC_3bit = 7
+    AC_3rm = 8
+
+
+class VarHeuristic(enum.IntEnum):
+    """Heuristic::Var, include/Solver.h:56-64."""
+    VRH_LEX = 0
+    VRH_DOM_MIN = 1
+
+
+class ValHeuristic(enum.IntEnum):
+    """Heuristic::Val, include/Solver.h:66."""
+    VLH_MIN = 0
+
+
+class Stats(C.Structure):
+    _fields_ = [("inconsistent", C.c_int32), ("rounds", C.c_int32), ("deletions", C.c_int64),
+                ("revisions", C.c_int64), ("rows", C.c_int64), ("fixpoints", C.c_int64),
+                ("branches", C.c_int64), ("sweeps", C.c_int32), ("launches", C.c_int32),
+                ("device_ms", C.c_double), ("alg_bytes", C.c_double), ("kernel_ms", C.c_double),
+                ("kernel_bytes", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class SearchResult(C.Structure):
+    _fields_ = [("status", C.c_int32), ("pad", C.c_int32), ("num_positive", C.c_int64),
+                ("num_negative", C.c_int64), ("propagations", C.c_int64), ("solve_ms", C.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    """Loads libcpgpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libcpgpu.so is not built (run: python -m cpim_gb300.build)")
+    L = C.CDLL(LIB_PATH)
+    vp, i, i64, d, u64 = C.c_void_p, C.c_int, C.c_int64, C.c_double, C.c_uint64
+    PI, P64, PU8 = C.POINTER(C.c_int), C.POINTER(C.c_uint64), C.POINTER(C.c_uint8)
+    PV = C.POINTER(C.c_void_p)
+    sig = {
+        "cp_last_error_string": ([], C.c_char_p),
+        "cp_engine_create": ([i, PV], i),
+        "cp_engine_destroy": ([vp], i),
+        "cp_engine_launches": ([vp], i64),
+        "cp_engine_set_tuning": ([vp, i, i, i], i),
+        "cp_net_upload": ([vp, i, PI, i, P64, i, PI, P64, i, PI, PI, PI, PI, i, PV], i),
+        "cp_net_destroy": ([vp], i),
+        "cp_net_device_bytes": ([vp], i64),
+        "cp_net_reload": ([vp, P64, P64], i),
+        "cp_level_copy": ([vp, i, i], i),
+        "cp_dom_get": ([vp, i, P64], i),
+        "cp_dom_set": ([vp, i, P64], i),
+        "cp_dom_sizes": ([vp, i, PI], i),
+        "cp_reduce_to": ([vp, i, i, i], i),
+        "cp_remove": ([vp, i, i, i], i),
+        "cp_enforce_ac": ([vp, i, i, PI, C.POINTER(Stats)], i),
+        "cp_enforce_sac1": ([vp, i, C.POINTER(Stats)], i),
+        "cp_singletons": ([vp, i, i, PI, PI, PU8, i, C.POINTER(Stats)], i),
+        "cp_mac_solve": ([vp, i, i, i64, C.POINTER(SearchResult), PI], i),
+        "cp_gsolver_solve": ([vp, i64, C.POINTER(SearchResult), PI], i),
+        "cp_gen_binary": ([i, i, i64, d, d, d, u64, PV], i),
+        "cp_gen_mixed": ([i, i, i64, d, d, i, i, d, u64, PV], i),
+        "cp_gen_uneven": ([u64, i, i, i, PV], i),
+        "cp_gen_free": ([vp], i),
+        "cp_gen_sizes": ([vp, C.POINTER(C.c_int64)], i),
+        "cp_gen_export": ([vp, PI, P64, PI, P64, PI, PI, PI, PI], i),
+        "cp_net_upload_instance": ([vp, vp, i, PV], i),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        raise CPError(rc, lib().cp_last_error_string().decode())
+
+
+def _p(a, ct):
+    return a.ctypes.data_as(C.POINTER(ct)) if a is not None else None
+
+
+@dataclass
+class Instance:
+    """A constraint network as the C ABI's upload arrays (numpy)."""
+    n: int
+    W: int
+    dom: np.ndarray
+    init: np.ndarray
+    bin_scope: np.ndarray
+    bin_rows: np.ndarray
+    tab_arity: np.ndarray
+    tab_scope: np.ndarray
+    tab_ntup: np.ndarray
+    tab_tuples: np.ndarray
+    fingerprint: str = ""
+
+    @property
+    def n_bin(self):
+        return int(self.bin_scope.shape[0] // 2)
+
+    @property
+    def n_tab(self):
+        return int(self.tab_arity.shape[0])
+
+
+def _export(h) -> Instance:
+    L = lib()
+    sz = (C.c_int64 * 8)()
+    _check(L.cp_gen_sizes(h, sz))
+    n, W, nb, nt, nrows, nsc, ntup, fp = list(sz)
+    inst = Instance(n=n, W=W, dom=np.zeros(n, np.int32), init=np.zeros(n * W, np.uint64),
+                    bin_scope=np.zeros(2 * nb, np.int32), bin_rows=np.zeros(nrows, np.uint64),
+                    tab_arity=np.zeros(nt, np.int32), tab_scope=np.zeros(nsc, np.int32),
+                    tab_ntup=np.zeros(nt, np.int32), tab_tuples=np.zeros(ntup, np.int32),
+                    fingerprint="%016x" % (fp & 0xFFFFFFFFFFFFFFFF))
+    _check(L.cp_gen_export(h, _p(inst.dom, C.c_int), _p(inst.init, C.c_uint64), _p(inst.bin_scope, C.c_int),
+                           _p(inst.bin_rows, C.c_uint64), _p(inst.tab_arity, C.c_int), _p(inst.tab_scope, C.c_int),
+                           _p(inst.tab_ntup, C.c_int), _p(inst.tab_tuples, C.c_int)))
+    L.cp_gen_free(h)
+    return inst
+
+
+def gen_binary(n, d, e, p_lo, p_hi=None, remove=0.0, seed=1) -> Instance:
+    """Model-B random binary network (cpim_gb300/csrc/cp_gen.h)."""
+    h = C.c_void_p()
+    _check(lib().cp_gen_binary(n, d, e, p_lo, p_lo if p_hi is None else p_hi, remove, seed, C.byref(h)))
+    return _export(h)
+
+
+def gen_mixed(n, d, e, p_lo, p_hi, k3, ntup, remove, seed) -> Instance:
+    """Binary network plus ternary positive tables."""
+    h = C.c_void_p()
+    _check(lib().cp_gen_mixed(n, d, e, p_lo, p_hi, k3, ntup, remove, seed, C.byref(h)))
+    return _export(h)
+
+
+def gen_uneven(seed, n_lo=20, n_hi=400, d_cap=256) -> Instance:
+    """One member of the uneven multi-instance batch."""
+    h = C.c_void_p()
+    _check(lib().cp_gen_uneven(seed, n_lo, n_hi, d_cap, C.byref(h)))
+    return _export(h)
+
+
+class Engine:
+    """One CUDA device and stream (replaces GModel's implicit device state)."""
+
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        _check(lib().cp_engine_create(device, C.byref(self._h)))
+
+    def close(self):
+        if self._h:
+            lib().cp_engine_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def launches(self) -> int:
+        return lib().cp_engine_launches(self._h)
+
+    def set_tuning(self, block=0, chunk=0, ctas_per_sm=0):
+        _check(lib().cp_engine_set_tuning(self._h, block, chunk, ctas_per_sm))
+
+    def upload(self, inst: Instance, max_levels: int = 0) -> "Net":
+        return Net(self, inst, max_levels)
+
+
+class Net:
+    """A device-resident network with its level stack."""
+
+    def __init__(self, engine: Engine, inst: Instance, max_levels: int = 0):
+        self.engine = engine
+        self.n, self.W = inst.n, inst.W
+        self.dom_sizes = inst.dom.copy()
+        self._h = C.c_void_p()
+        t = inst
+        _check(lib().cp_net_upload(engine._h, t.n, _p(t.dom, C.c_int), t.W, _p(t.init, C.c_uint64), t.n_bin,
+                                   _p(t.bin_scope, C.c_int), _p(t.bin_rows, C.c_uint64), t.n_tab,
+                                   _p(t.tab_arity, C.c_int), _p(t.tab_scope, C.c_int), _p(t.tab_ntup, C.c_int),
+                                   _p(t.tab_tuples, C.c_int), max_levels, C.byref(self._h)))
+
+    def close(self):
+        if self._h:
+            lib().cp_net_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def device_bytes(self) -> int:
+        return lib().cp_net_device_bytes(self._h)
+
+    def reload(self, inst: Instance):
+        _check(lib().cp_net_reload(self._h, _p(inst.init, C.c_uint64), _p(inst.bin_rows, C.c_uint64)))
+
+    # -- level stack --
+    def dom_get(self, level=0) -> np.ndarray:
+        out = np.zeros(self.n * self.W, np.uint64)
+        _check(lib().cp_dom_get(self._h, level, _p(out, C.c_uint64)))
+        return out
+
+    def dom_set(self, level, words):
+        w = np.ascontiguousarray(words, dtype=np.uint64)
+        _check(lib().cp_dom_set(self._h, level, _p(w, C.c_uint64)))
+
+    def sizes(self, level=0) -> np.ndarray:
+        out = np.zeros(self.n, np.int32)
+        _check(lib().cp_dom_sizes(self._h, level, _p(out, C.c_int)))
+        return out
+
+    def level_copy(self, src, dst):
+        _check(lib().cp_level_copy(self._h, src, dst))
+
+    def reduce_to(self, level, var, val):
+        _check(lib().cp_reduce_to(self._h, level, var, val))
+
+    def remove(self, level, var, val):
+        _check(lib().cp_remove(self._h, level, var, val))
+
+    # -- propagation --
+    def enforce_ac(self, level=0, evt=None) -> Stats:
+        st = Stats()
+        if evt is None:
+            _check(lib().cp_enforce_ac(self._h, level, 0, None, C.byref(st)))
+        else:
+            e = np.ascontiguousarray(evt, dtype=np.int32)
+            _check(lib().cp_enforce_ac(self._h, level, len(e), _p(e, C.c_int), C.byref(st)))
+        return st
+
+    def enforce_sac1(self, level=0) -> Stats:
+        st = Stats()
+        _check(lib().cp_enforce_sac1(self._h, level, C.byref(st)))
+        return st
+
+    def singletons(self, vars_, vals, level=0, mode=0):
+        v = np.ascontiguousarray(vars_, dtype=np.int32)
+        a = np.ascontiguousarray(vals, dtype=np.int32)
+        ok = np.zeros(len(v), np.uint8)
+        st = Stats()
+        _check(lib().cp_singletons(self._h, level, len(v), _p(v, C.c_int), _p(a, C.c_int), _p(ok, C.c_uint8), mode,
+                                   C.byref(st)))
+        return ok, st
+
+    # -- search --
+    def mac_solve(self, var_h=VarHeuristic.VRH_DOM_MIN, val_h=ValHeuristic.VLH_MIN, time_limit_ms=600000):
+        res = SearchResult()
+        sol = np.full(self.n, -1, np.int32)
+        _check(lib().cp_mac_solve(self._h, int(var_h), int(val_h), time_limit_ms, C.byref(res), _p(sol, C.c_int)))
+        return {"status": res.status, "num_positive": res.num_positive, "num_negative": res.num_negative,
+                "propagations": res.propagations, "solve_ms": res.solve_ms,
+                "solution": sol.tolist() if res.status == 1 else []}
+
+    def gsolver_solve(self, time_limit_ms=600000):
+        res = SearchResult()
+        sol = np.full(self.n, -1, np.int32)
+        _check(lib().cp_gsolver_solve(self._h, time_limit_ms, C.byref(res), _p(sol, C.c_int)))
+        return {"status": res.status, "num_positive": res.num_positive, "num_negative": res.num_negative,
+                "propagations": res.propagations, "solve_ms": res.solve_ms,
+                "solution": sol.tolist() if res.status == 1 else []}

@@ -1,0 +1,1179 @@
+// Host side of the propagation engine: the C ABI of include/cpgpu.h, network
+// upload, the device level stack, AC / SAC orchestration, and the MAC and
+// GModelSolver search loops that keep the reference's host control flow while
+// every domain operation and propagation runs on the device.
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/cpgpu.h"
+#include "cp_gen.h"
+#include "cp_internal.h"
+
+using namespace cpgpu;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define CP_CUDA(expr)                                                                          \
+  do {                                                                                         \
+    cudaError_t _e = (expr);                                                                   \
+    if (_e != cudaSuccess) {                                                                   \
+      const int _code = (_e == cudaErrorMemoryAllocation) ? CP_E_OOM : CP_E_CUDA;              \
+      return fail(_code, std::string(#expr) + ": " + cudaGetErrorString(_e));                  \
+    }                                                                                          \
+  } while (0)
+
+#define CP_TRY(expr)          \
+  do {                        \
+    int _r = (expr);          \
+    if (_r != CP_OK) return _r; \
+  } while (0)
+
+int internal_words(int W) {
+  if (W <= 2) return W;
+  if (W <= 4) return 4;
+  if (W <= 8) return 8;
+  return -1;
+}
+
+}  // namespace
+
+struct cp_engine {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
+  int sm_count = 0;
+  size_t smem_optin = 0;
+  int64_t launches = 0;
+  int live_nets = 0;
+  bool closed = false;
+  int block_node = 256;
+  int block_sac = 256;
+  int block_grid = 256;
+  int chunk = 0;
+  int ctas_per_sm = 0;
+};
+
+struct cp_net {
+  cp_engine* e = nullptr;
+  int n = 0, W_user = 1, W = 1, nb = 0, nt = 0, levels = 0;
+  std::vector<int> dom;
+  std::vector<int> bx, by;
+  DevNet dn;
+  std::vector<void*> allocs;
+  u64* d_levels = nullptr;
+  u64* d_rel = nullptr;
+  int* d_bx = nullptr;
+  int* d_by = nullptr;
+  int64_t* d_offA = nullptr;
+  int64_t* d_offB = nullptr;
+  int64_t relA_words = 0, relB_words = 0;
+  GridScratch G{};
+  SacScratch S{};
+  KStats* d_stats = nullptr;
+  KStats* h_stats = nullptr;  // pinned
+  int* d_evt = nullptr;       // n
+  int* d_sizes = nullptr;     // n
+  uint8_t* d_ok1 = nullptr;   // per-test results of the plain path
+  u64* h_dom = nullptr;       // pinned n*W
+  int* h_sizes = nullptr;     // pinned n
+  void* d_cta_scratch = nullptr;  // k_node state when shared memory is too small
+  void* d_sac_scratch = nullptr;
+  size_t sac_stride = 0;
+  int sac_grid = 0;
+  int grid_blocks = 0;
+  bool cta_in_smem = true;
+  bool prefer_grid = false;
+  int64_t device_bytes = 0;
+
+  ~cp_net() {
+    for (void* p : allocs) cudaFree(p);
+    if (h_stats) cudaFreeHost(h_stats);
+    if (h_dom) cudaFreeHost(h_dom);
+    if (h_sizes) cudaFreeHost(h_sizes);
+    if (e) --e->live_nets;
+  }
+
+  template <typename T>
+  int alloc(T** p, size_t count) {
+    void* raw = nullptr;
+    const size_t bytes = std::max<size_t>(count * sizeof(T), 16);
+    cudaError_t e = cudaMalloc(&raw, bytes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(e == cudaErrorMemoryAllocation ? CP_E_OOM : CP_E_CUDA,
+                  "cudaMalloc of " + std::to_string(bytes) + " bytes: " + cudaGetErrorString(e));
+    }
+    allocs.push_back(raw);
+    device_bytes += static_cast<int64_t>(bytes);
+    *p = static_cast<T*>(raw);
+    return CP_OK;
+  }
+  u64* level_ptr(int level) { return d_levels + static_cast<size_t>(level) * n * W; }
+};
+
+namespace {
+
+// ---- stats --------------------------------------------------------------
+int stats_begin(cp_net* net) {
+  KStats z{};
+  z.fail_var = -1;
+  *net->h_stats = z;
+  CP_CUDA(cudaMemcpyAsync(net->d_stats, net->h_stats, sizeof(KStats), cudaMemcpyHostToDevice, net->e->stream));
+  return CP_OK;
+}
+
+int stats_fetch(cp_net* net) {
+  CP_CUDA(cudaMemcpyAsync(net->h_stats, net->d_stats, sizeof(KStats), cudaMemcpyDeviceToHost, net->e->stream));
+  CP_CUDA(cudaStreamSynchronize(net->e->stream));
+  if (net->h_stats->grid_err) return fail(CP_E_TIMEOUT, "device grid barrier wait ran out");
+  if (net->h_stats->error) return fail(net->h_stats->error, "device-side check failed (round limit)");
+  return CP_OK;
+}
+
+struct Acc {
+  cp_stats s{};
+  void add(const KStats& k, int launches) {
+    s.revisions += static_cast<int64_t>(k.revisions);
+    s.rows += static_cast<int64_t>(k.rows + k.tuples);
+    s.fixpoints += static_cast<int64_t>(k.fixpoints);
+    s.branches += static_cast<int64_t>(k.branches);
+    s.rounds = std::max(s.rounds, k.rounds_max);
+    s.launches += launches;
+    tuples += static_cast<int64_t>(k.tuples);
+    bin_rows += static_cast<int64_t>(k.rows);
+    dels += static_cast<int64_t>(k.deletions);
+  }
+  int64_t tuples = 0, bin_rows = 0, dels = 0;
+};
+
+// Algorithmic bytes: support rows and tuples read, both domains of every
+// revision read, changed words written, plus each SAC branch's domain copy.
+double alg_bytes(const cp_net* net, const Acc& a, int64_t branches) {
+  const double wb = 8.0 * net->W_user;
+  return double(a.bin_rows) * wb + double(a.tuples) * 6.0 + double(a.s.revisions) * 2.0 * wb +
+         double(a.dels) * wb + double(branches) * 2.0 * net->n * wb;
+}
+
+// ---- one AC fixpoint at a level ----------------------------------------
+// evt_dev: device list of seeds (nullptr = all variables); nevt: its length.
+int run_ac(cp_net* net, int level, const int* evt_dev, int nevt, int& launches) {
+  cp_engine* e = net->e;
+  if (net->prefer_grid) {
+    cudaStream_t s = e->stream;
+    CP_CUDA(cudaMemsetAsync(net->G.qlen, 0, 3 * sizeof(int), s));
+    CP_CUDA(cudaMemsetAsync(net->G.failed, 0, 2 * sizeof(int), s));
+    CP_CUDA(cudaMemsetAsync(net->G.bar, 0, 2 * sizeof(unsigned), s));
+    const size_t nw = (static_cast<size_t>(net->n) + 31) / 32;
+    CP_CUDA(cudaMemsetAsync(net->G.fb[0], 0, nw * 4, s));
+    CP_CUDA(cudaMemsetAsync(net->G.fb[1], 0, nw * 4, s));
+    CP_CUDA(launch_ac_grid(net->dn, net->level_ptr(level), evt_dev, nullptr, evt_dev ? nevt : 0, net->G,
+                           net->d_stats, e->block_grid, net->grid_blocks, s));
+  } else {
+    const int op = evt_dev ? kOpEvents : kOpRoot;
+    CP_CUDA(launch_node(net->dn, net->d_levels, level, level, op, 0, 0, evt_dev, nevt, net->d_stats, nullptr,
+                        e->block_node, net->cta_in_smem ? nullptr : net->d_cta_scratch, e->stream));
+  }
+  ++launches;
+  ++e->launches;
+  return CP_OK;
+}
+
+// Copies level `level` (internal width) to the pinned host mirror and
+// converts to the user width into out (if given).
+int fetch_level(cp_net* net, int level, uint64_t* out) {
+  const size_t words = static_cast<size_t>(net->n) * net->W;
+  CP_CUDA(cudaMemcpyAsync(net->h_dom, net->level_ptr(level), words * 8, cudaMemcpyDeviceToHost, net->e->stream));
+  CP_CUDA(cudaStreamSynchronize(net->e->stream));
+  if (out) {
+    for (int x = 0; x < net->n; ++x)
+      for (int w = 0; w < net->W_user; ++w)
+        out[static_cast<size_t>(x) * net->W_user + w] = net->h_dom[static_cast<size_t>(x) * net->W + w];
+  }
+  return CP_OK;
+}
+
+int check_level(const cp_net* net, int level) {
+  if (level < 0 || level >= net->levels) return fail(CP_E_ARG, "level out of range: " + std::to_string(level));
+  return CP_OK;
+}
+
+int check_var_val(const cp_net* net, int var, int val) {
+  if (var < 0 || var >= net->n) return fail(CP_E_ARG, "variable out of range: " + std::to_string(var));
+  if (val < 0 || val >= net->dom[var]) return fail(CP_E_ARG, "value out of range: " + std::to_string(val));
+  return CP_OK;
+}
+
+double elapsed_ms(cp_engine* e) {
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e->ev0, e->ev1);
+  return ms;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char* cp_last_error_string(void) { return g_last_error.c_str(); }
+
+int cp_engine_create(int device, cp_engine** out) {
+  if (!out) return fail(CP_E_ARG, "null output pointer");
+  int count = 0;
+  CP_CUDA(cudaGetDeviceCount(&count));
+  if (device < 0 || device >= count) return fail(CP_E_ARG, "no CUDA device " + std::to_string(device));
+  CP_CUDA(cudaSetDevice(device));
+  auto e = std::make_unique<cp_engine>();
+  e->device = device;
+  cudaDeviceProp prop;
+  CP_CUDA(cudaGetDeviceProperties(&prop, device));
+  if (!prop.cooperativeLaunch) return fail(CP_E_UNSUPPORTED, "device lacks cooperative launch");
+  e->sm_count = prop.multiProcessorCount;
+  e->smem_optin = prop.sharedMemPerBlockOptin;
+  CP_CUDA(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+  CP_CUDA(cudaEventCreate(&e->ev0));
+  CP_CUDA(cudaEventCreate(&e->ev1));
+  CP_CUDA(cudaEventCreate(&e->evk0));
+  CP_CUDA(cudaEventCreate(&e->evk1));
+  *out = e.release();
+  return CP_OK;
+}
+
+// An engine outlives its networks: destroying it while networks are alive
+// only marks it closed, and the last network destroyed frees it.
+static void engine_free(cp_engine* e) {
+  cudaSetDevice(e->device);
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  if (e->ev0) cudaEventDestroy(e->ev0);
+  if (e->ev1) cudaEventDestroy(e->ev1);
+  if (e->evk0) cudaEventDestroy(e->evk0);
+  if (e->evk1) cudaEventDestroy(e->evk1);
+  if (e->stream) cudaStreamDestroy(e->stream);
+  delete e;
+}
+
+int cp_engine_destroy(cp_engine* e) {
+  if (!e) return CP_OK;
+  if (e->closed) return fail(CP_E_STATE, "engine destroyed twice");
+  e->closed = true;
+  if (e->live_nets == 0) engine_free(e);
+  return CP_OK;
+}
+
+int64_t cp_engine_launches(const cp_engine* e) { return e ? e->launches : 0; }
+
+int cp_engine_set_tuning(cp_engine* e, int block, int chunk, int ctas_per_sm) {
+  if (!e) return fail(CP_E_ARG, "null engine");
+  if (block < 0 || block > 1024 || (block % 32) != 0) return fail(CP_E_ARG, "block must be a multiple of 32 <= 1024");
+  if (block) {
+    e->block_node = block;
+    e->block_sac = std::min(block, 256);
+    e->block_grid = std::min(block, 512);
+  }
+  e->chunk = chunk;
+  e->ctas_per_sm = ctas_per_sm;
+  return CP_OK;
+}
+
+int cp_net_upload(cp_engine* e, int n, const int* dom, int W, const uint64_t* init, int n_bin, const int* bin_scope,
+                  const uint64_t* bin_rows, int n_tab, const int* tab_arity, const int* tab_scope,
+                  const int* tab_ntup, const int* tab_tuples, int max_levels, cp_net** out) {
+  if (!e || !out) return fail(CP_E_ARG, "null engine or output");
+  if (n < 1 || n >= kMaxVars) return fail(CP_E_ARG, "n out of range");
+  if (!dom || !init) return fail(CP_E_ARG, "null dom or init");
+  if (n_bin < 0 || n_tab < 0) return fail(CP_E_ARG, "negative constraint count");
+  if (n_bin > 0 && (!bin_scope || !bin_rows)) return fail(CP_E_ARG, "null binary arrays");
+  if (n_tab > 0 && (!tab_arity || !tab_scope || !tab_ntup || !tab_tuples)) return fail(CP_E_ARG, "null table arrays");
+  const int Wi = internal_words(W);
+  if (W < 1 || Wi < 0) return fail(CP_E_UNSUPPORTED, "domains wider than 512 values are not supported");
+  if (n_tab > 0 && Wi > 4) return fail(CP_E_UNSUPPORTED, "tables need domains of at most 256 values");
+  for (int x = 0; x < n; ++x)
+    if (dom[x] < 1 || dom[x] > 64 * W) return fail(CP_E_ARG, "domain size of variable " + std::to_string(x));
+  CP_CUDA(cudaSetDevice(e->device));
+  auto net = std::make_unique<cp_net>();
+  net->e = e;
+  ++e->live_nets;
+  net->n = n;
+  net->W_user = W;
+  net->W = Wi;
+  net->nb = n_bin;
+  net->nt = n_tab;
+  net->dom.assign(dom, dom + n);
+  net->levels = max_levels > 0 ? max_levels : n + 3;
+  if (net->levels < 2) net->levels = 2;
+
+  // Binary constraints: scopes, relation offsets, arcs by source variable.
+  net->bx.resize(n_bin);
+  net->by.resize(n_bin);
+  std::vector<int64_t> offA(n_bin), offB(n_bin);
+  int64_t ta = 0, tb = 0;
+  std::vector<int> arc_deg(n, 0), tab_deg(n, 0);
+  for (int c = 0; c < n_bin; ++c) {
+    const int x = bin_scope[2 * c], y = bin_scope[2 * c + 1];
+    if (x < 0 || x >= n || y < 0 || y >= n || x == y) return fail(CP_E_ARG, "bad binary scope " + std::to_string(c));
+    net->bx[c] = x;
+    net->by[c] = y;
+    offA[c] = ta;
+    ta += static_cast<int64_t>(dom[x]) * Wi;
+    ++arc_deg[x];
+    ++arc_deg[y];
+  }
+  for (int c = 0; c < n_bin; ++c) {
+    offB[c] = ta + tb;
+    tb += static_cast<int64_t>(net->dom[net->by[c]]) * Wi;
+  }
+  if (ta + tb >= (int64_t(1) << 32)) return fail(CP_E_UNSUPPORTED, "relations exceed 32 GiB");
+  net->relA_words = ta;
+  net->relB_words = tb;
+  std::vector<int> arc_start(n + 1, 0);
+  for (int x = 0; x < n; ++x) arc_start[x + 1] = arc_start[x] + arc_deg[x];
+  std::vector<Arc> arcs(static_cast<size_t>(2) * n_bin);
+  {
+    std::vector<int> fill(arc_start.begin(), arc_start.end() - 1);
+    for (int c = 0; c < n_bin; ++c) {
+      const int x = net->bx[c], y = net->by[c];
+      // Source y: revise x against y (x's rows are the A block).
+      arcs[fill[y]++] = Arc{x, static_cast<u32>(offA[c]), static_cast<u32>(offB[c]), 0};
+      // Source x: revise y against x (y's rows are the B block).
+      arcs[fill[x]++] = Arc{y, static_cast<u32>(offB[c]), static_cast<u32>(offA[c]), 0};
+    }
+  }
+  // Tables.
+  std::vector<int> t_arity(n_tab), t_scope(static_cast<size_t>(n_tab) * kMaxArity, 0), t_ntup(n_tab);
+  std::vector<int64_t> t_off(n_tab);
+  int64_t total_tup = 0;
+  {
+    int64_t so = 0;
+    for (int t = 0; t < n_tab; ++t) {
+      const int r = tab_arity[t];
+      if (r < 2 || r > kMaxArity) return fail(CP_E_UNSUPPORTED, "table arity must be 2..4");
+      if (tab_ntup[t] < 0) return fail(CP_E_ARG, "negative tuple count");
+      t_arity[t] = r;
+      for (int i = 0; i < r; ++i) {
+        const int v = tab_scope[so + i];
+        if (v < 0 || v >= n) return fail(CP_E_ARG, "bad table scope " + std::to_string(t));
+        for (int j = 0; j < i; ++j)
+          if (t_scope[static_cast<size_t>(t) * kMaxArity + j] == v) return fail(CP_E_ARG, "repeated variable in table");
+        t_scope[static_cast<size_t>(t) * kMaxArity + i] = v;
+        ++tab_deg[v];
+      }
+      so += r;
+      t_ntup[t] = tab_ntup[t];
+      t_off[t] = total_tup;
+      total_tup += static_cast<int64_t>(tab_ntup[t]) * r;
+    }
+  }
+  std::vector<uint16_t> t_tup(static_cast<size_t>(total_tup));
+  {
+    int64_t src = 0;
+    for (int t = 0; t < n_tab; ++t) {
+      const int r = t_arity[t], k = t_ntup[t];
+      for (int j = 0; j < k; ++j)
+        for (int i = 0; i < r; ++i) {
+          const int v = tab_tuples[src + static_cast<int64_t>(j) * r + i];
+          const int var = t_scope[static_cast<size_t>(t) * kMaxArity + i];
+          if (v < 0 || v >= dom[var]) return fail(CP_E_ARG, "tuple value out of range in table " + std::to_string(t));
+          t_tup[t_off[t] + static_cast<int64_t>(i) * k + j] = static_cast<uint16_t>(v);
+        }
+      src += static_cast<int64_t>(k) * r;
+    }
+  }
+  std::vector<int> tinc_start(n + 1, 0);
+  for (int x = 0; x < n; ++x) tinc_start[x + 1] = tinc_start[x] + tab_deg[x];
+  std::vector<int> vtab(tinc_start[n]);
+  {
+    std::vector<int> fill(tinc_start.begin(), tinc_start.end() - 1);
+    for (int t = 0; t < n_tab; ++t)
+      for (int i = 0; i < t_arity[t]; ++i) vtab[fill[t_scope[static_cast<size_t>(t) * kMaxArity + i]]++] = t;
+  }
+  // Work-item chunking.
+  int max_deg = 0;
+  for (int x = 0; x < n; ++x) max_deg = std::max(max_deg, arc_deg[x] + tab_deg[x]);
+  int chunk = e->chunk > 0 ? e->chunk : 8;
+  chunk = std::max(chunk, (max_deg + kMaxChunksPerVar - 1) / kMaxChunksPerVar);
+  int64_t max_items = 0;
+  for (int x = 0; x < n; ++x) max_items += std::max(1, (arc_deg[x] + tab_deg[x] + chunk - 1) / chunk);
+  if (max_items >= (int64_t(1) << 31)) return fail(CP_E_UNSUPPORTED, "too many work items");
+  int64_t total_values = 0;
+  for (int x = 0; x < n; ++x) total_values += dom[x];
+
+  // Device allocations and copies.
+  cudaStream_t s = e->stream;
+  DevNet& D = net->dn;
+  D.n = n;
+  D.W = Wi;
+  D.nb = n_bin;
+  D.nt = n_tab;
+  D.chunk = chunk;
+  D.max_items = static_cast<int>(max_items);
+  D.total_values = total_values;
+  int* d_dsize;
+  int* d_arc_start;
+  Arc* d_arcs;
+  int* d_tinc;
+  int* d_vtab;
+  int *d_tar, *d_tsc, *d_tnt;
+  int64_t* d_toff;
+  uint16_t* d_ttup;
+  CP_TRY(net->alloc(&d_dsize, n));
+  CP_TRY(net->alloc(&d_arc_start, n + 1));
+  CP_TRY(net->alloc(&d_arcs, arcs.size()));
+  CP_TRY(net->alloc(&d_tinc, n + 1));
+  CP_TRY(net->alloc(&d_vtab, vtab.size()));
+  CP_TRY(net->alloc(&d_tar, n_tab));
+  CP_TRY(net->alloc(&d_tsc, t_scope.size()));
+  CP_TRY(net->alloc(&d_tnt, n_tab));
+  CP_TRY(net->alloc(&d_toff, n_tab));
+  CP_TRY(net->alloc(&d_ttup, t_tup.size()));
+  CP_TRY(net->alloc(&net->d_rel, static_cast<size_t>(ta + tb)));
+  CP_TRY(net->alloc(&net->d_bx, n_bin));
+  CP_TRY(net->alloc(&net->d_by, n_bin));
+  CP_TRY(net->alloc(&net->d_offA, n_bin));
+  CP_TRY(net->alloc(&net->d_offB, n_bin));
+  CP_TRY(net->alloc(&net->d_levels, static_cast<size_t>(net->levels) * n * Wi));
+  CP_CUDA(cudaMemcpyAsync(d_dsize, dom, n * sizeof(int), cudaMemcpyHostToDevice, s));
+  CP_CUDA(cudaMemcpyAsync(d_arc_start, arc_start.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
+  if (!arcs.empty()) CP_CUDA(cudaMemcpyAsync(d_arcs, arcs.data(), arcs.size() * sizeof(Arc), cudaMemcpyHostToDevice, s));
+  CP_CUDA(cudaMemcpyAsync(d_tinc, tinc_start.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
+  if (!vtab.empty()) CP_CUDA(cudaMemcpyAsync(d_vtab, vtab.data(), vtab.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+  if (n_tab) {
+    CP_CUDA(cudaMemcpyAsync(d_tar, t_arity.data(), n_tab * sizeof(int), cudaMemcpyHostToDevice, s));
+    CP_CUDA(cudaMemcpyAsync(d_tsc, t_scope.data(), t_scope.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    CP_CUDA(cudaMemcpyAsync(d_tnt, t_ntup.data(), n_tab * sizeof(int), cudaMemcpyHostToDevice, s));
+    CP_CUDA(cudaMemcpyAsync(d_toff, t_off.data(), n_tab * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    if (!t_tup.empty())
+      CP_CUDA(cudaMemcpyAsync(d_ttup, t_tup.data(), t_tup.size() * sizeof(uint16_t), cudaMemcpyHostToDevice, s));
+  }
+  if (n_bin) {
+    CP_CUDA(cudaMemcpyAsync(net->d_bx, net->bx.data(), n_bin * sizeof(int), cudaMemcpyHostToDevice, s));
+    CP_CUDA(cudaMemcpyAsync(net->d_by, net->by.data(), n_bin * sizeof(int), cudaMemcpyHostToDevice, s));
+    CP_CUDA(cudaMemcpyAsync(net->d_offA, offA.data(), n_bin * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    CP_CUDA(cudaMemcpyAsync(net->d_offB, offB.data(), n_bin * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+  }
+  D.dsize = d_dsize;
+  D.arc_start = d_arc_start;
+  D.arcs = d_arcs;
+  D.tinc_start = d_tinc;
+  D.vtab = d_vtab;
+  D.rel = net->d_rel;
+  D.t_arity = d_tar;
+  D.t_scope = d_tsc;
+  D.t_ntup = d_tnt;
+  D.t_off = d_toff;
+  D.t_tup = d_ttup;
+
+  // Scratch.
+  const size_t nw = (static_cast<size_t>(n) + 31) / 32;
+  GridScratch& G = net->G;
+  CP_TRY(net->alloc(&G.q[0], max_items));
+  CP_TRY(net->alloc(&G.q[1], max_items));
+  CP_TRY(net->alloc(&G.fb[0], nw));
+  CP_TRY(net->alloc(&G.fb[1], nw));
+  CP_TRY(net->alloc(&G.qlen, 4));
+  CP_TRY(net->alloc(&G.tstamp, std::max(1, n_tab)));
+  CP_TRY(net->alloc(&G.epoch, 4));
+  CP_TRY(net->alloc(&G.failed, 4));
+  CP_TRY(net->alloc(&G.bar, 4));
+  CP_CUDA(cudaMemsetAsync(G.tstamp, 0, std::max(1, n_tab) * sizeof(int), s));
+  CP_CUDA(cudaMemsetAsync(G.epoch, 0, 4 * sizeof(int), s));
+  SacScratch& S = net->S;
+  CP_TRY(net->alloc(&S.work, total_values));
+  CP_TRY(net->alloc(&S.nwork, 4));
+  CP_TRY(net->alloc(&S.ok, total_values));
+  CP_TRY(net->alloc(&S.cursor, 4));
+  CP_TRY(net->alloc(&S.evt, n));
+  CP_TRY(net->alloc(&S.nevt, 4));
+  CP_TRY(net->alloc(&S.evt_fb, nw));
+  CP_TRY(net->alloc(&net->d_stats, 1));
+  CP_TRY(net->alloc(&net->d_evt, n));
+  CP_TRY(net->alloc(&net->d_sizes, n));
+  CP_TRY(net->alloc(&net->d_ok1, total_values));
+  CP_CUDA(cudaMallocHost(reinterpret_cast<void**>(&net->h_stats), sizeof(KStats)));
+  CP_CUDA(cudaMallocHost(reinterpret_cast<void**>(&net->h_dom), static_cast<size_t>(n) * Wi * 8));
+  CP_CUDA(cudaMallocHost(reinterpret_cast<void**>(&net->h_sizes), static_cast<size_t>(n) * sizeof(int)));
+
+  // CTA-local state: shared memory when it fits, else global scratch.
+  const size_t cta_bytes = cta_state_bytes(D);
+  net->cta_in_smem = cta_bytes + 1024 <= e->smem_optin;
+  if (!net->cta_in_smem) {
+    char* p;
+    CP_TRY(net->alloc(&p, cta_bytes));
+    net->d_cta_scratch = p;
+  }
+  // Persistent SAC grid.
+  int per_sm = sac_blocks_per_sm(D, e->block_sac, net->cta_in_smem);
+  if (per_sm < 1) return fail(CP_E_UNSUPPORTED, "SAC kernel does not fit on an SM");
+  if (e->ctas_per_sm > 0) per_sm = std::min(per_sm, e->ctas_per_sm);
+  net->sac_grid = per_sm * e->sm_count;
+  if (!net->cta_in_smem) {
+    net->sac_stride = (cta_bytes + 255) & ~size_t(255);
+    char* p;
+    CP_TRY(net->alloc(&p, net->sac_stride * net->sac_grid));
+    net->d_sac_scratch = p;
+  }
+  net->grid_blocks = ac_grid_max_blocks(D, e->block_grid, e->sm_count);
+  if (net->grid_blocks < 1) return fail(CP_E_UNSUPPORTED, "grid fixpoint kernel does not fit");
+  // Large networks run their single-instance fixpoints on the whole grid.
+  net->prefer_grid = (2 * static_cast<int64_t>(n_bin) + n_tab) > 8192 || !net->cta_in_smem;
+
+  // Relations: A blocks from the user's rows, B blocks transposed on device.
+  CP_TRY(cp_net_reload(net.get(), init, bin_rows));
+  *out = net.release();
+  return CP_OK;
+}
+
+int cp_net_reload(cp_net* net, const uint64_t* init, const uint64_t* bin_rows) {
+  if (!net) return fail(CP_E_ARG, "null net");
+  cp_engine* e = net->e;
+  cudaStream_t s = e->stream;
+  const int W = net->W_user, Wi = net->W, n = net->n;
+  if (net->nb > 0) {
+    if (!bin_rows) return fail(CP_E_ARG, "null rows");
+    if (W == Wi) {
+      CP_CUDA(cudaMemcpyAsync(net->d_rel, bin_rows, static_cast<size_t>(net->relA_words) * 8, cudaMemcpyHostToDevice, s));
+    } else {
+      std::vector<u64> pad(static_cast<size_t>(net->relA_words), 0);
+      int64_t src = 0, dst = 0;
+      for (int c = 0; c < net->nb; ++c)
+        for (int a = 0; a < net->dom[net->bx[c]]; ++a) {
+          for (int w = 0; w < W; ++w) pad[dst + w] = bin_rows[src + w];
+          src += W;
+          dst += Wi;
+        }
+      CP_CUDA(cudaMemcpyAsync(net->d_rel, pad.data(), pad.size() * 8, cudaMemcpyHostToDevice, s));
+      CP_CUDA(cudaStreamSynchronize(s));
+    }
+    CP_CUDA(cudaMemsetAsync(net->d_rel + net->relA_words, 0, static_cast<size_t>(net->relB_words) * 8, s));
+    CP_CUDA(launch_transpose(net->dn, net->d_rel, net->d_bx, net->d_by, net->d_offA, net->d_offB, s));
+    ++e->launches;
+  }
+  if (init) {
+    // Bits at or beyond a variable's size are cleared: the kernels index
+    // support rows by live values, so a stray bit would read past the block.
+    for (int x = 0; x < n; ++x)
+      for (int w = 0; w < Wi; ++w) {
+        u64 v = w < W ? init[static_cast<size_t>(x) * W + w] : 0ull;
+        const int lo = w * 64, d = net->dom[x];
+        if (d - lo < 64) v &= (d - lo <= 0) ? 0ull : ((1ull << (d - lo)) - 1ull);
+        net->h_dom[static_cast<size_t>(x) * Wi + w] = v;
+      }
+    CP_CUDA(cudaMemcpyAsync(net->d_levels, net->h_dom, static_cast<size_t>(n) * Wi * 8, cudaMemcpyHostToDevice, s));
+  }
+  CP_CUDA(cudaStreamSynchronize(s));
+  return CP_OK;
+}
+
+int cp_net_destroy(cp_net* net) {
+  if (!net) return CP_OK;
+  cp_engine* e = net->e;
+  cudaSetDevice(e->device);
+  cudaStreamSynchronize(e->stream);
+  delete net;  // ~cp_net releases its hold on the engine
+  if (e->closed && e->live_nets == 0) engine_free(e);
+  return CP_OK;
+}
+
+int64_t cp_net_device_bytes(const cp_net* net) { return net ? net->device_bytes : 0; }
+
+int cp_level_copy(cp_net* net, int src, int dst) {
+  if (!net) return fail(CP_E_ARG, "null net");
+  CP_TRY(check_level(net, src));
+  CP_TRY(check_level(net, dst));
+  if (src == dst) return CP_OK;
+  const size_t bytes = static_cast<size_t>(net->n) * net->W * 8;
+  CP_CUDA(cudaMemcpyAsync(net->level_ptr(dst), net->level_ptr(src), bytes, cudaMemcpyDeviceToDevice, net->e->stream));
+  CP_CUDA(cudaStreamSynchronize(net->e->stream));
+  return CP_OK;
+}
+
+int cp_dom_get(cp_net* net, int level, uint64_t* out) {
+  if (!net || !out) return fail(CP_E_ARG, "null argument");
+  CP_TRY(check_level(net, level));
+  return fetch_level(net, level, out);
+}
+
+int cp_dom_set(cp_net* net, int level, const uint64_t* in) {
+  if (!net || !in) return fail(CP_E_ARG, "null argument");
+  CP_TRY(check_level(net, level));
+  const int W = net->W_user, Wi = net->W;
+  for (int x = 0; x < net->n; ++x)
+    for (int w = 0; w < Wi; ++w) {
+      u64 v = w < W ? in[static_cast<size_t>(x) * W + w] : 0ull;
+      const int lo = w * 64, d = net->dom[x];
+      if (d - lo < 64) v &= (d - lo <= 0) ? 0ull : ((1ull << (d - lo)) - 1ull);
+      net->h_dom[static_cast<size_t>(x) * Wi + w] = v;
+    }
+  CP_CUDA(cudaMemcpyAsync(net->level_ptr(level), net->h_dom, static_cast<size_t>(net->n) * Wi * 8,
+                          cudaMemcpyHostToDevice, net->e->stream));
+  CP_CUDA(cudaStreamSynchronize(net->e->stream));
+  return CP_OK;
+}
+
+int cp_dom_sizes(cp_net* net, int level, int* out) {
+  if (!net || !out) return fail(CP_E_ARG, "null argument");
+  CP_TRY(check_level(net, level));
+  CP_CUDA(launch_popcount(net->dn, net->level_ptr(level), net->d_sizes, net->e->stream));
+  ++net->e->launches;
+  CP_CUDA(cudaMemcpyAsync(out, net->d_sizes, net->n * sizeof(int), cudaMemcpyDeviceToHost, net->e->stream));
+  CP_CUDA(cudaStreamSynchronize(net->e->stream));
+  return CP_OK;
+}
+
+int cp_reduce_to(cp_net* net, int level, int var, int value) {
+  if (!net) return fail(CP_E_ARG, "null net");
+  CP_TRY(check_level(net, level));
+  CP_TRY(check_var_val(net, var, value));
+  CP_CUDA(launch_level_edit(net->dn, net->level_ptr(level), var, value, kOpAssign, net->e->stream));
+  ++net->e->launches;
+  CP_CUDA(cudaStreamSynchronize(net->e->stream));
+  return CP_OK;
+}
+
+int cp_remove(cp_net* net, int level, int var, int value) {
+  if (!net) return fail(CP_E_ARG, "null net");
+  CP_TRY(check_level(net, level));
+  CP_TRY(check_var_val(net, var, value));
+  CP_CUDA(launch_level_edit(net->dn, net->level_ptr(level), var, value, kOpRefute, net->e->stream));
+  ++net->e->launches;
+  CP_CUDA(cudaStreamSynchronize(net->e->stream));
+  return CP_OK;
+}
+
+int cp_enforce_ac(cp_net* net, int level, int n_evt, const int* evt, cp_stats* st) {
+  if (!net) return fail(CP_E_ARG, "null net");
+  CP_TRY(check_level(net, level));
+  cp_engine* e = net->e;
+  const int* evt_dev = nullptr;
+  if (evt && n_evt > 0) {
+    if (n_evt > net->n) return fail(CP_E_ARG, "too many event variables");
+    for (int i = 0; i < n_evt; ++i)
+      if (evt[i] < 0 || evt[i] >= net->n) return fail(CP_E_ARG, "event variable out of range");
+    std::memcpy(net->h_sizes, evt, n_evt * sizeof(int));
+    CP_CUDA(cudaMemcpyAsync(net->d_evt, net->h_sizes, n_evt * sizeof(int), cudaMemcpyHostToDevice, e->stream));
+    evt_dev = net->d_evt;
+  }
+  CP_TRY(stats_begin(net));
+  CP_CUDA(cudaEventRecord(e->ev0, e->stream));
+  int launches = 0;
+  CP_TRY(run_ac(net, level, evt_dev, evt_dev ? n_evt : 0, launches));
+  CP_CUDA(cudaEventRecord(e->ev1, e->stream));
+  CP_TRY(stats_fetch(net));
+  if (st) {
+    Acc a;
+    a.add(*net->h_stats, launches);
+    a.s.inconsistent = net->h_stats->inconsistent;
+    a.s.deletions = a.dels;
+    a.s.device_ms = elapsed_ms(e);
+    a.s.alg_bytes = alg_bytes(net, a, 0);
+    *st = a.s;
+  }
+  return CP_OK;
+}
+
+int cp_enforce_sac1(cp_net* net, int level, cp_stats* st) {
+  if (!net) return fail(CP_E_ARG, "null net");
+  CP_TRY(check_level(net, level));
+  cp_engine* e = net->e;
+  cudaStream_t s = e->stream;
+  Acc acc;
+  int launches = 0;
+  CP_CUDA(cudaEventRecord(e->ev0, s));
+  // Root AC (SAC1::enforce first runs AC on every variable, src/SAC1.cpp:58).
+  CP_TRY(stats_begin(net));
+  CP_TRY(run_ac(net, level, nullptr, 0, launches));
+  CP_TRY(stats_fetch(net));
+  acc.add(*net->h_stats, 0);
+  bool inconsistent = net->h_stats->inconsistent != 0;
+  int sweeps = 0;
+  double kernel_ms = 0, kernel_bytes = 0;
+  const size_t nw = (static_cast<size_t>(net->n) + 31) / 32;
+  while (!inconsistent) {
+    ++sweeps;
+    CP_TRY(stats_begin(net));
+    CP_CUDA(cudaMemsetAsync(net->S.nwork, 0, sizeof(int), s));
+    CP_CUDA(cudaMemsetAsync(net->S.cursor, 0, sizeof(int), s));
+    CP_CUDA(cudaMemsetAsync(net->S.nevt, 0, sizeof(int), s));
+    CP_CUDA(cudaMemsetAsync(net->S.evt_fb, 0, nw * 4, s));
+    CP_CUDA(launch_build_work(net->dn, net->level_ptr(level), net->S, s));
+    CP_CUDA(cudaEventRecord(e->evk0, s));
+    CP_CUDA(launch_sac_branches(net->dn, net->level_ptr(level), net->S.work, net->S.nwork, net->S.cursor, net->S.ok,
+                                net->d_stats, e->block_sac, net->sac_grid, net->d_sac_scratch, net->sac_stride, s));
+    CP_CUDA(cudaEventRecord(e->evk1, s));
+    CP_CUDA(launch_commit(net->dn, net->level_ptr(level), net->S, net->d_stats, s));
+    launches += 3;
+    e->launches += 3;
+    CP_TRY(stats_fetch(net));
+    const KStats k = *net->h_stats;
+    {
+      // Values removed at the level are the failed tests; removals inside the
+      // branches' private domain copies are not deletions of this call.
+      KStats kl = k;
+      kl.deletions = k.removed;
+      acc.add(kl, 0);
+    }
+    {
+      float kms = 0;
+      cudaEventElapsedTime(&kms, e->evk0, e->evk1);
+      kernel_ms += kms;
+      Acc ka;
+      KStats kk = k;
+      kk.deletions -= kk.removed;  // commit-kernel removals are not the branch kernel's
+      ka.add(kk, 0);
+      kernel_bytes += alg_bytes(net, ka, static_cast<int64_t>(k.branches));
+    }
+    if (k.removed == 0) break;
+    // Propagate the removals at the level (SAC1.cpp:85-92, batched).
+    int nevt = 0;
+    CP_CUDA(cudaMemcpyAsync(&net->h_sizes[0], net->S.nevt, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CP_CUDA(cudaStreamSynchronize(s));
+    nevt = net->h_sizes[0];
+    CP_TRY(stats_begin(net));
+    CP_TRY(run_ac(net, level, net->S.evt, nevt, launches));
+    CP_TRY(stats_fetch(net));
+    acc.add(*net->h_stats, 0);
+    inconsistent = net->h_stats->inconsistent != 0;
+  }
+  CP_CUDA(cudaEventRecord(e->ev1, s));
+  CP_CUDA(cudaEventSynchronize(e->ev1));
+  if (st) {
+    acc.s.inconsistent = inconsistent ? 1 : 0;
+    acc.s.deletions = acc.dels;
+    acc.s.sweeps = sweeps;
+    acc.s.launches = launches;
+    acc.s.device_ms = elapsed_ms(e);
+    acc.s.alg_bytes = alg_bytes(net, acc, acc.s.branches);
+    acc.s.kernel_ms = kernel_ms;
+    acc.s.kernel_bytes = kernel_bytes;
+    *st = acc.s;
+  }
+  return CP_OK;
+}
+
+int cp_singletons(cp_net* net, int level, int count, const int* vars, const int* vals, uint8_t* ok, int mode,
+                  cp_stats* st) {
+  if (!net || (count > 0 && (!vars || !vals || !ok))) return fail(CP_E_ARG, "null argument");
+  CP_TRY(check_level(net, level));
+  if (count < 0 || count > net->dn.total_values) return fail(CP_E_ARG, "count out of range");
+  for (int i = 0; i < count; ++i) CP_TRY(check_var_val(net, vars[i], vals[i]));
+  cp_engine* e = net->e;
+  cudaStream_t s = e->stream;
+  std::vector<int2> pairs(count);
+  for (int i = 0; i < count; ++i) pairs[i] = make_int2(vars[i], vals[i]);
+  if (count) CP_CUDA(cudaMemcpyAsync(net->S.work, pairs.data(), count * sizeof(int2), cudaMemcpyHostToDevice, s));
+  net->h_sizes[0] = count;
+  CP_CUDA(cudaMemcpyAsync(net->S.nwork, net->h_sizes, sizeof(int), cudaMemcpyHostToDevice, s));
+  CP_CUDA(cudaMemsetAsync(net->S.cursor, 0, sizeof(int), s));
+  CP_CUDA(cudaStreamSynchronize(s));
+  CP_TRY(stats_begin(net));
+  int launches = 0;
+  CP_CUDA(cudaEventRecord(e->ev0, s));
+  uint8_t* d_ok = nullptr;
+  if (mode == 0) {
+    CP_CUDA(launch_sac_branches(net->dn, net->level_ptr(level), net->S.work, net->S.nwork, net->S.cursor, net->S.ok,
+                                net->d_stats, e->block_sac, net->sac_grid, net->d_sac_scratch, net->sac_stride, s));
+    ++launches;
+    d_ok = net->S.ok;
+  } else if (mode == 1) {
+    for (int i = 0; i < count; ++i) {
+      CP_CUDA(launch_node(net->dn, net->d_levels, level, level, kOpSingleton, vars[i], vals[i], nullptr, 0,
+                          net->d_stats, net->d_ok1 + i, e->block_node,
+                          net->cta_in_smem ? nullptr : net->d_cta_scratch, s));
+      ++launches;
+    }
+    d_ok = net->d_ok1;
+  } else {
+    return fail(CP_E_ARG, "mode must be 0 (batched) or 1 (one launch per test)");
+  }
+  e->launches += launches;
+  CP_CUDA(cudaEventRecord(e->ev1, s));
+  if (count) CP_CUDA(cudaMemcpyAsync(ok, d_ok, count, cudaMemcpyDeviceToHost, s));
+  CP_TRY(stats_fetch(net));
+  if (st) {
+    Acc a;
+    a.add(*net->h_stats, launches);
+    if (mode == 1) {
+      a.s.branches = count;
+      a.s.fixpoints = count;
+    }
+    a.s.deletions = 0;
+    a.s.device_ms = elapsed_ms(e);
+    a.s.alg_bytes = alg_bytes(net, a, a.s.branches);
+    a.s.kernel_ms = a.s.device_ms;
+    a.s.kernel_bytes = a.s.alg_bytes;
+    *st = a.s;
+  }
+  return CP_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Search
+// ===========================================================================
+namespace {
+
+// Device-resident node operations for the search loops: each returns the
+// consistency verdict and leaves the resulting level mirrored in h_dom.
+struct NodeRunner {
+  cp_net* net;
+  int64_t propagations = 0;
+
+  int node(int op, int src, int dst, int var, int val, bool& consistent) {
+    cp_engine* e = net->e;
+    cudaStream_t s = e->stream;
+    CP_TRY(stats_begin(net));
+    if (!net->prefer_grid) {
+      CP_CUDA(launch_node(net->dn, net->d_levels, src, dst, op, var, val, nullptr, 0, net->d_stats, nullptr,
+                          e->block_node, net->cta_in_smem ? nullptr : net->d_cta_scratch, s));
+      ++e->launches;
+    } else {
+      int launches = 0;
+      if (op == kOpRoot) {
+        CP_TRY(run_ac(net, src, nullptr, 0, launches));
+      } else {
+        if (src != dst)
+          CP_CUDA(cudaMemcpyAsync(net->level_ptr(dst), net->level_ptr(src), static_cast<size_t>(net->n) * net->W * 8,
+                                  cudaMemcpyDeviceToDevice, s));
+        CP_CUDA(launch_level_edit(net->dn, net->level_ptr(dst), var, val, op == kOpRefute ? kOpRefute : kOpAssign, s));
+        ++e->launches;
+        net->h_sizes[0] = var;
+        CP_CUDA(cudaMemcpyAsync(net->d_evt, net->h_sizes, sizeof(int), cudaMemcpyHostToDevice, s));
+        CP_TRY(run_ac(net, dst, net->d_evt, 1, launches));
+      }
+    }
+    ++propagations;
+    CP_CUDA(cudaMemcpyAsync(net->h_dom, net->level_ptr(dst), static_cast<size_t>(net->n) * net->W * 8,
+                            cudaMemcpyDeviceToHost, s));
+    CP_TRY(stats_fetch(net));
+    consistent = net->h_stats->inconsistent == 0;
+    return CP_OK;
+  }
+  int size(int x) const {
+    int sz = 0;
+    for (int w = 0; w < net->W; ++w) sz += __builtin_popcountll(net->h_dom[static_cast<size_t>(x) * net->W + w]);
+    return sz;
+  }
+  int head(int x) const {
+    for (int w = 0; w < net->W; ++w) {
+      const u64 v = net->h_dom[static_cast<size_t>(x) * net->W + w];
+      if (v) return w * 64 + __builtin_ctzll(v);
+    }
+    return -1;
+  }
+  int next(int x, int a) const {
+    for (int b = a + 1; b < net->dom[x]; ++b)
+      if ((net->h_dom[static_cast<size_t>(x) * net->W + (b >> 6)] >> (b & 63)) & 1ull) return b;
+    return -1;
+  }
+};
+
+// MAC::enforce (src/MAC.cpp:100-165) with the per-level "assigned" flags of
+// IntVar (include/Network.h:183, src/Network.cpp:112-118, 235-256) and
+// AssignedStack (src/Solver.cpp:36-56, 114-116), which decide the variable
+// order; only domains live on the device.
+class DeviceMAC {
+ public:
+  DeviceMAC(cp_net* net, int varh, int valh) : R{net}, n_(net->n), L_(net->levels), varh_(varh), valh_(valh) {
+    assigned_.assign(static_cast<size_t>(L_) * n_, 0);
+    top_.assign(n_, 0);
+  }
+
+  int solve(int64_t time_limit_ms, cp_search_result* res, int* solution) {
+    const auto t0 = std::chrono::steady_clock::now();
+    auto elapsed = [&]() {
+      return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    };
+    *res = cp_search_result{};
+    bool consistent = false;
+    CP_TRY(R.node(kOpRoot, 0, 0, 0, 0, consistent));
+    if (!consistent) return finish(res, 0, elapsed());
+    for (;;) {
+      if (elapsed() > double(time_limit_ms)) return finish(res, 2, elapsed());
+      const int p = static_cast<int>(I_.size());
+      if (p + 1 >= L_) return fail(CP_E_ARG, "level stack too shallow for the search");
+      const int var = select_var(p);
+      if (var < 0) return fail(CP_E_STATE, "no variable to branch on");
+      const int val = R.head(var);
+      new_level(p);
+      push(var, val);
+      ++res->num_positive;
+      const int lv = static_cast<int>(I_.size());
+      A(lv)[var] = 1;  // IntVar::ReduceTo marks the variable assigned
+      CP_TRY(R.node(kOpAssign, p, lv, var, val, consistent));
+      if (consistent && lv == n_) {
+        for (int x = 0; x < n_; ++x) solution[x] = R.head(x);
+        return finish(res, 1, elapsed());
+      }
+      while (!consistent && !I_.empty()) {
+        const auto va = pop();
+        const int q = static_cast<int>(I_.size());
+        back_to(q);
+        ++res->num_negative;
+        CP_TRY(R.node(kOpRefute, q, q, va.first, va.second, consistent));
+        update_model_assigned();
+      }
+      if (!consistent) return finish(res, 0, elapsed());
+    }
+  }
+
+ private:
+  NodeRunner R;
+  int n_, L_, varh_, valh_;
+  std::vector<char> assigned_;
+  std::vector<int> top_;
+  std::vector<std::pair<int, int>> I_;
+
+  char* A(int p) { return &assigned_[static_cast<size_t>(p) * n_]; }
+  int finish(cp_search_result* res, int status, double ms) {
+    res->status = status;
+    res->propagations = R.propagations;
+    res->solve_ms = ms;
+    return CP_OK;
+  }
+  // VRH_DOM_MIN (src/MAC.cpp:357-365): first unassigned variable of strictly
+  // smaller size; VRH_LEX (:366-368).
+  int select_var(int p) {
+    if (varh_ == 0) return static_cast<int>(I_.size()) + 1 < n_ ? static_cast<int>(I_.size()) + 1 : -1;
+    int var = -1;
+    double min_size = 1e300;
+    for (int v = 0; v < n_; ++v)
+      if (!A(p)[v] && R.size(v) < min_size) {
+        min_size = R.size(v);
+        var = v;
+      }
+    return var;
+  }
+  void new_level(int src) {
+    std::copy(A(src), A(src) + n_, A(src + 1));
+    std::fill(top_.begin(), top_.end(), src);
+  }
+  void back_to(int dest) {
+    for (int v = 0; v < n_; ++v) {
+      for (int i = dest; i <= top_[v]; ++i) A(i)[v] = 0;
+      top_[v] = dest;
+    }
+  }
+  void push(int v, int a) {
+    I_.emplace_back(v, a);
+    A(static_cast<int>(I_.size()))[v] = 1;
+  }
+  std::pair<int, int> pop() {
+    const auto va = I_.back();
+    I_.pop_back();
+    A(static_cast<int>(I_.size()))[va.first] = 0;
+    return va;
+  }
+  void update_model_assigned() {
+    for (const auto& va : I_) A(static_cast<int>(I_.size()))[va.first] = 1;
+  }
+};
+
+// GModelSolver::Solve / Search (src/GModelSolver.cu:31-189): d-way search,
+// smallest domain among variables with more than one value
+// (GModel::GetMinDomainVar, src/GModel.cu:1553-1572), values in increasing
+// order, one GAC per node.
+class DeviceGSolver {
+ public:
+  explicit DeviceGSolver(cp_net* net) : R{net}, n_(net->n) {}
+  int solve(int64_t time_limit_ms, cp_search_result* res, int* solution) {
+    t0_ = std::chrono::steady_clock::now();
+    limit_ = time_limit_ms;
+    *res = cp_search_result{};
+    res_ = res;
+    sol_ = solution;
+    bool consistent = false;
+    CP_TRY(R.node(kOpRoot, 0, 0, 0, 0, consistent));
+    if (!consistent) return finish(0);
+    if (fully_assigned()) {
+      extract();
+      return finish(1);
+    }
+    bool stop = false;
+    CP_TRY(search(0, stop));
+    return finish(found_ ? 1 : (timed_out_ ? 2 : 0));
+  }
+
+ private:
+  NodeRunner R;
+  int n_;
+  std::chrono::steady_clock::time_point t0_;
+  int64_t limit_ = 0;
+  cp_search_result* res_ = nullptr;
+  int* sol_ = nullptr;
+  bool found_ = false, timed_out_ = false;
+
+  double elapsed() const {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0_).count();
+  }
+  int finish(int status) {
+    res_->status = status;
+    res_->propagations = R.propagations;
+    res_->solve_ms = elapsed();
+    return CP_OK;
+  }
+  bool fully_assigned() const {
+    for (int x = 0; x < n_; ++x)
+      if (R.size(x) != 1) return false;
+    return true;
+  }
+  void extract() {
+    for (int x = 0; x < n_; ++x) sol_[x] = R.head(x);
+    found_ = true;
+  }
+  int search(int level, bool& stop) {
+    if (limit_ > 0 && elapsed() >= double(limit_)) {
+      timed_out_ = true;
+      stop = true;
+      return CP_OK;
+    }
+    if (level + 1 >= R.net->levels) return fail(CP_E_ARG, "level stack too shallow for the search");
+    // R.h_dom mirrors `level` here.
+    std::vector<u64> here(R.net->h_dom, R.net->h_dom + static_cast<size_t>(n_) * R.net->W);
+    int var = -1, min_size = 1 << 30;
+    for (int x = 0; x < n_; ++x) {
+      const int sz = R.size(x);
+      if (sz > 1 && sz < min_size) {
+        min_size = sz;
+        var = x;
+      }
+    }
+    if (var < 0) {
+      if (fully_assigned()) {
+        extract();
+        stop = true;
+      }
+      return CP_OK;
+    }
+    for (int val = R.head(var); val != -1;) {
+      ++res_->num_positive;
+      bool consistent = false;
+      CP_TRY(R.node(kOpAssign, level, level + 1, var, val, consistent));
+      if (!consistent) {
+        ++res_->num_negative;
+      } else {
+        CP_TRY(search(level + 1, stop));
+        if (stop) return CP_OK;
+      }
+      std::copy(here.begin(), here.end(), R.net->h_dom);
+      val = R.next(var, val);
+    }
+    return CP_OK;
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+int cp_mac_solve(cp_net* net, int var_heuristic, int val_heuristic, int64_t time_limit_ms, cp_search_result* res,
+                 int* solution) {
+  if (!net || !res || !solution) return fail(CP_E_ARG, "null argument");
+  if (var_heuristic != 0 && var_heuristic != 1)
+    return fail(CP_E_UNSUPPORTED, "variable heuristic: 0 (VRH_LEX) or 1 (VRH_DOM_MIN)");
+  if (val_heuristic != 0) return fail(CP_E_UNSUPPORTED, "value heuristic: 0 (VLH_MIN)");
+  DeviceMAC mac(net, var_heuristic, val_heuristic);
+  return mac.solve(time_limit_ms, res, solution);
+}
+
+int cp_gsolver_solve(cp_net* net, int64_t time_limit_ms, cp_search_result* res, int* solution) {
+  if (!net || !res || !solution) return fail(CP_E_ARG, "null argument");
+  DeviceGSolver g(net);
+  return g.solve(time_limit_ms, res, solution);
+}
+
+// ---- generator --------------------------------------------------------
+struct cp_instance {
+  cpgen::Instance I;
+};
+
+int cp_gen_binary(int n, int d, int64_t e, double p_lo, double p_hi, double remove, uint64_t seed, cp_instance** out) {
+  if (!out || n < 2 || d < 1 || e < 0) return fail(CP_E_ARG, "bad generator arguments");
+  try {
+    *out = new cp_instance{cpgen::random_binary(n, d, e, p_lo, p_hi, remove, seed)};
+  } catch (const std::exception& ex) {
+    return fail(CP_E_ARG, ex.what());
+  }
+  return CP_OK;
+}
+
+int cp_gen_mixed(int n, int d, int64_t e, double p_lo, double p_hi, int k3, int ntup, double remove, uint64_t seed,
+                 cp_instance** out) {
+  if (!out || n < 3 || d < 1 || e < 0 || k3 < 0 || ntup < 0) return fail(CP_E_ARG, "bad generator arguments");
+  try {
+    *out = new cp_instance{cpgen::random_mixed(n, d, e, p_lo, p_hi, k3, ntup, remove, seed)};
+  } catch (const std::exception& ex) {
+    return fail(CP_E_ARG, ex.what());
+  }
+  return CP_OK;
+}
+
+int cp_gen_uneven(uint64_t seed, int n_lo, int n_hi, int d_cap, cp_instance** out) {
+  if (!out || n_lo < 2 || n_hi < n_lo || d_cap < 8) return fail(CP_E_ARG, "bad generator arguments");
+  *out = new cp_instance{cpgen::uneven_instance(seed, n_lo, n_hi, d_cap)};
+  return CP_OK;
+}
+
+int cp_gen_free(cp_instance* inst) {
+  delete inst;
+  return CP_OK;
+}
+
+int cp_gen_sizes(const cp_instance* inst, int64_t* sizes) {
+  if (!inst || !sizes) return fail(CP_E_ARG, "null argument");
+  const auto& I = inst->I;
+  sizes[0] = I.n;
+  sizes[1] = I.W;
+  sizes[2] = I.n_bin();
+  sizes[3] = I.n_tab();
+  sizes[4] = static_cast<int64_t>(I.brows.size());
+  sizes[5] = static_cast<int64_t>(I.tscope.size());
+  sizes[6] = static_cast<int64_t>(I.ttup.size());
+  sizes[7] = static_cast<int64_t>(cpgen::fingerprint(I));
+  return CP_OK;
+}
+
+int cp_gen_export(const cp_instance* inst, int* dom, uint64_t* init, int* bin_scope, uint64_t* bin_rows, int* tab_arity,
+                  int* tab_scope, int* tab_ntup, int* tab_tuples) {
+  if (!inst) return fail(CP_E_ARG, "null instance");
+  const auto& I = inst->I;
+  if (dom) std::copy(I.dom.begin(), I.dom.end(), dom);
+  if (init) std::copy(I.init.begin(), I.init.end(), init);
+  if (bin_scope)
+    for (int c = 0; c < I.n_bin(); ++c) {
+      bin_scope[2 * c] = I.bx[c];
+      bin_scope[2 * c + 1] = I.by[c];
+    }
+  if (bin_rows) std::copy(I.brows.begin(), I.brows.end(), bin_rows);
+  if (tab_arity) std::copy(I.tarity.begin(), I.tarity.end(), tab_arity);
+  if (tab_scope) std::copy(I.tscope.begin(), I.tscope.end(), tab_scope);
+  if (tab_ntup) std::copy(I.tntup.begin(), I.tntup.end(), tab_ntup);
+  if (tab_tuples) std::copy(I.ttup.begin(), I.ttup.end(), tab_tuples);
+  return CP_OK;
+}
+
+int cp_net_upload_instance(cp_engine* e, const cp_instance* inst, int max_levels, cp_net** out) {
+  if (!inst) return fail(CP_E_ARG, "null instance");
+  const auto& I = inst->I;
+  std::vector<int> scope(2 * static_cast<size_t>(I.n_bin()));
+  for (int c = 0; c < I.n_bin(); ++c) {
+    scope[2 * c] = I.bx[c];
+    scope[2 * c + 1] = I.by[c];
+  }
+  return cp_net_upload(e, I.n, I.dom.data(), I.W, I.init.data(), I.n_bin(), scope.data(), I.brows.data(), I.n_tab(),
+                       I.tarity.data(), I.tscope.data(), I.tntup.data(), I.ttup.data(), max_levels, out);
+}
+
+}  // extern "C"

@@ -1,0 +1,129 @@
+// Internal layout shared by the host engine (cp_engine.cu) and the kernels
+// (cp_kernels.cu). Plain structs of device pointers, passed by value to
+// kernels.
+//
+// HBM layout of one network (all u64 words, W = internal words per domain,
+// 1, 2, 4 or 8; a user W of 3 is padded to 4 and 5..8 to 8):
+//   levels   [L][n][W]          domain stack, level 0 = root
+//   rel      [A blocks][B blocks]
+//            A block of binary constraint c = (x, y): dom[x] rows of W words,
+//            row a = supports of x=a among y's values (the user's rows);
+//            B block: dom[y] rows, row b = supports of y=b among x's values
+//            (the transpose, built on the device at upload).
+//   arcs     grouped by source variable y: revising z against y for every
+//            constraint linking y and z; zy = word offset of z's rows (bits
+//            over y), yz = offset of y's rows (bits over z).
+//   tables   u16 tuples, column-major per table (coordinate i of all tuples
+//            contiguous) for coalesced loads; incidence var -> tables.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace cpgpu {
+
+using u64 = unsigned long long;
+using u32 = unsigned int;
+
+constexpr int kMaxArity = 4;
+constexpr int kItemVarShift = 12;             // work item = (var << 12) | chunk
+constexpr int kMaxChunksPerVar = 1 << kItemVarShift;
+constexpr int kMaxVars = 1 << (32 - kItemVarShift);
+
+struct Arc {
+  int z;        // variable revised
+  u32 zy;       // word offset of z's rows (value-wise revise)
+  u32 yz;       // word offset of y's rows (union-of-supports revise)
+  int pad;
+};
+
+struct DevNet {
+  int n = 0, W = 1, nb = 0, nt = 0;
+  int chunk = 8;          // incidences per work item
+  int max_items = 0;      // capacity of one work queue
+  int64_t total_values = 0;
+  const int* dsize = nullptr;       // [n]
+  const int* arc_start = nullptr;   // [n+1]
+  const Arc* arcs = nullptr;        // [2*nb]
+  const int* tinc_start = nullptr;  // [n+1]
+  const int* vtab = nullptr;        // table ids per variable
+  const u64* rel = nullptr;
+  const int* t_arity = nullptr;
+  const int* t_scope = nullptr;     // [nt * kMaxArity]
+  const int* t_ntup = nullptr;
+  const int64_t* t_off = nullptr;   // offset of table t's tuples in t_tup
+  const uint16_t* t_tup = nullptr;
+};
+
+// Counters of one propagation call, accumulated on the device.
+struct KStats {
+  u64 revisions;
+  u64 rows;           // binary support rows read
+  u64 tuples;         // table tuples scanned
+  u64 deletions;
+  u64 fixpoints;
+  u64 branches;
+  u64 removed;        // SAC: values removed by failed singleton tests
+  int rounds_max;
+  int inconsistent;
+  int fail_var;
+  int error;          // 0, or a CP_E_* code set by a device-side check
+  int grid_err;       // bounded grid barrier timeout
+  int pad[3];
+};
+
+// Global-memory state of the grid-wide fixpoint (one per network).
+struct GridScratch {
+  u32* q[2];          // work queues, max_items each
+  u32* fb[2];         // dedupe bitmaps, ceil(n/32) words each
+  int* qlen;          // [3] rotating queue lengths
+  int* tstamp;        // [nt] round stamp of the last table revision
+  int* epoch;         // [1] stamp base carried across calls
+  int* failed;        // [1]
+  unsigned* bar;      // [2] grid barrier: count, generation
+};
+
+// SAC sweep buffers (one per network).
+struct SacScratch {
+  int2* work;         // live (x, a) pairs, up to total_values
+  int* nwork;         // [1]
+  uint8_t* ok;        // per pair: singleton test result
+  int* cursor;        // [1] next branch for the persistent CTAs
+  int* evt;           // variables changed by a commit, up to n
+  int* nevt;          // [1]
+  u32* evt_fb;        // dedupe bitmap for evt
+};
+
+enum NodeOp { kOpRoot = 0, kOpAssign = 1, kOpRefute = 2, kOpSingleton = 3, kOpEvents = 4 };
+
+// Shared-memory (or per-CTA scratch) bytes of the CTA-local fixpoint.
+size_t cta_state_bytes(const DevNet& N);
+
+// ---- launch wrappers (cp_kernels.cu) ----
+// One CTA: domains of level src loaded to the CTA's state, the operation
+// applied, fixpoint computed, result written to level dst (unless singleton).
+cudaError_t launch_node(const DevNet& N, u64* levels, int src, int dst, int op, int var, int val,
+                        const int* evt, int nevt, KStats* st, uint8_t* ok_out, int block, void* gscratch,
+                        cudaStream_t s);
+// Grid-wide persistent fixpoint at level `level`, seeded with evt (or all
+// variables when evt == nullptr).
+cudaError_t launch_ac_grid(const DevNet& N, u64* level_dom, const int* evt, const int* nevt_dev, int nevt,
+                           GridScratch G, KStats* st, int block, int grid, cudaStream_t s);
+int ac_grid_max_blocks(const DevNet& N, int block, int sm_count);
+// Persistent batched singleton tests: pairs work[0..*nwork), results in ok.
+cudaError_t launch_sac_branches(const DevNet& N, const u64* root, const int2* work, const int* nwork, int* cursor,
+                                uint8_t* ok, KStats* st, int block, int grid, void* gscratch, size_t gstride,
+                                cudaStream_t s);
+int sac_blocks_per_sm(const DevNet& N, int block, bool smem_state);
+// Builds the list of live (x, a) pairs of a level (warp ballot + prefix).
+cudaError_t launch_build_work(const DevNet& N, const u64* dom, SacScratch S, cudaStream_t s);
+// Removes failed pairs from the level, collecting changed variables.
+cudaError_t launch_commit(const DevNet& N, u64* dom, SacScratch S, KStats* st, cudaStream_t s);
+// Builds the B blocks (transposes) of the binary relations.
+cudaError_t launch_transpose(const DevNet& N, u64* rel, const int* bx, const int* by, const int64_t* offA,
+                             const int64_t* offB, cudaStream_t s);
+// Level helpers.
+cudaError_t launch_popcount(const DevNet& N, const u64* dom, int* sizes, cudaStream_t s);
+cudaError_t launch_level_edit(const DevNet& N, u64* dom, int var, int val, int op, cudaStream_t s);
+
+}  // namespace cpgpu

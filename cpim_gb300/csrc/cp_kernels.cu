@@ -1,0 +1,880 @@
+// Bitset-domain propagation kernels for sm_103a.
+//
+// One fixpoint body serves three launch shapes:
+//   - k_node:  one CTA owns one network state (domains copied from a level
+//              into shared memory); MAC nodes, small root ACs, and the plain
+//              one-test-per-launch singleton baseline;
+//   - k_sac:   persistent CTAs pull SAC singleton branches (x, a) from a
+//              device work list; each branch gets its own domain copy in the
+//              CTA's shared memory, only a 1-byte verdict leaves the SM;
+//   - k_ac_grid: the whole grid runs one fixpoint on global-memory domains
+//              under a bounded grid barrier (cooperative launch).
+//
+// Frontier: a queue of work items (variable y, chunk of y's incidences) plus a
+// bitmap that admits each changed variable once per round. Round r processes
+// queue r&1 and appends to the other; a variable's bit in the current bitmap
+// is cleared by the warp that takes its first chunk, so both bitmaps are clean
+// at every round boundary without a clearing pass.
+//
+// Revise of arc (z <- y) by one warp (the AND-then-any of AC3bit::seek_support,
+// src/AC3bit.cpp:29-38, over all values of z at once): the warp either tests
+// every live z value's support row against D(y) (32 values per ballot), or
+// ORs the support rows of the live y values and intersects; it picks the side
+// with fewer live values, so an assigned (singleton) y costs one row.
+#include <algorithm>
+#include <cstdio>
+#include <type_traits>
+
+#include "cp_internal.h"
+
+namespace cpgpu {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr long long kBarrierTimeoutNs = 2000000000ll;  // 2 s
+
+__device__ __forceinline__ u64 vload(const u64* p) { return *reinterpret_cast<const volatile u64*>(p); }
+__device__ __forceinline__ int vloadi(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
+
+template <int WT>
+__device__ __forceinline__ u64 sel(const u64 (&a)[WT], int i) {
+  u64 v = 0;
+#pragma unroll
+  for (int w = 0; w < WT; ++w)
+    if (w == i) v = a[w];
+  return v;
+}
+
+template <int WT>
+__device__ __forceinline__ void or_at(u64 (&a)[WT], int i, u64 m) {
+#pragma unroll
+  for (int w = 0; w < WT; ++w)
+    if (w == i) a[w] |= m;
+}
+
+__device__ __forceinline__ u64 warp_or64(u64 x) {
+  const u32 lo = __reduce_or_sync(kFull, static_cast<u32>(x));
+  const u32 hi = __reduce_or_sync(kFull, static_cast<u32>(x >> 32));
+  return (static_cast<u64>(hi) << 32) | lo;
+}
+
+// Support rows are read-only during a launch: non-coherent 128-bit loads.
+template <int WT>
+__device__ __forceinline__ void load_row(const u64* rel, size_t off, u64 (&r)[WT]) {
+  if constexpr (WT == 1) {
+    r[0] = __ldg(rel + off);
+  } else {
+    const ulonglong2* p = reinterpret_cast<const ulonglong2*>(rel + off);
+#pragma unroll
+    for (int h = 0; h < WT / 2; ++h) {
+      const ulonglong2 v = __ldg(p + h);
+      r[2 * h] = v.x;
+      r[2 * h + 1] = v.y;
+    }
+  }
+}
+
+__device__ __forceinline__ long long globaltimer_ns() {
+  long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// State of one fixpoint; pointers are shared or global memory.
+struct Fix {
+  u64* D;
+  u32* q0;
+  u32* q1;
+  u32* fb0;
+  u32* fb1;
+  int* qlen;     // [3]
+  int* tstamp;   // [nt] or null
+  int* failed;   // [2] per round parity
+  int* fail_var;
+  int stamp_base;
+};
+
+struct Cnt {
+  u64 rev = 0, rows = 0, tuples = 0, dels = 0;
+};
+
+// Domains and flags are shrunk concurrently by other warps, so lanes of one
+// warp reading them separately may see different snapshots. Every value that
+// steers warp-collective code (ballot, reduce, shuffle) is therefore read once
+// and made warp-uniform: a domain is loaded one word per lane and broadcast;
+// flags go through __any_sync. Call only from warp-converged code.
+template <int WT>
+__device__ __forceinline__ void load_dom_uniform(const u64* p, u64 (&d)[WT]) {
+  const int lane = threadIdx.x & 31;
+  const u64 mine = (lane < WT) ? vload(p + lane) : 0ull;
+#pragma unroll
+  for (int w = 0; w < WT; ++w) d[w] = __shfl_sync(kFull, mine, w);
+}
+
+__device__ __forceinline__ bool any_failed(const Fix& F) {
+  return __any_sync(kFull, (vloadi(F.failed) | vloadi(F.failed + 1)) != 0);
+}
+
+__device__ __forceinline__ void set_failed(const Fix& F, int slot, int var) {
+  atomicExch(F.failed + slot, 1);
+  if (F.fail_var) atomicExch(F.fail_var, var);
+}
+
+__device__ __forceinline__ int incidences(const DevNet& N, int z) {
+  return (N.arc_start[z + 1] - N.arc_start[z]) + (N.tinc_start[z + 1] - N.tinc_start[z]);
+}
+
+// Admits z to the next round once (bitmap), appending all its work items.
+__device__ __forceinline__ void append_var(const DevNet& N, u32* q, u32* fb, int* qlen, int z) {
+  const u32 bit = 1u << (z & 31);
+  const u32 old = atomicOr(fb + (z >> 5), bit);
+  if (old & bit) return;
+  int nch = (incidences(N, z) + N.chunk - 1) / N.chunk;
+  if (nch < 1) nch = 1;
+  const int base = atomicAdd(qlen, nch);
+  for (int c = 0; c < nch; ++c) q[base + c] = (static_cast<u32>(z) << kItemVarShift) | static_cast<u32>(c);
+}
+
+// Seeds variable z (single thread): a seeded variable with an empty domain is
+// a wipe-out.
+template <int WT>
+__device__ __forceinline__ void seed_var(const DevNet& N, const Fix& F, int z) {
+  u64 any = 0;
+#pragma unroll
+  for (int w = 0; w < WT; ++w) any |= vload(F.D + static_cast<size_t>(z) * WT + w);
+  if (!any) {
+    set_failed(F, 0, z);
+    return;
+  }
+  append_var(N, F.q0, F.fb0, F.qlen, z);
+}
+
+// Removes rm (warp-uniform) from D(z); on a change, checks for wipe-out and
+// admits z to the next round.
+template <int WT, bool kGlobal>
+__device__ __forceinline__ void commit(const DevNet& N, const Fix& F, u32* qn, u32* fbn, int* qlenn, int slot, int z,
+                                       const u64 (&rm)[WT], Cnt& cn) {
+  const int lane = threadIdx.x & 31;
+  bool any = false;
+#pragma unroll
+  for (int w = 0; w < WT; ++w) any |= rm[w] != 0;
+  if (!any) return;
+  u64 newly = 0;
+  if (lane < WT) {
+    const u64 r = sel<WT>(rm, lane);
+    if (r) {
+      const u64 old = atomicAnd(F.D + static_cast<size_t>(z) * WT + lane, ~r);
+      newly = old & r;
+    }
+  }
+  if (__ballot_sync(kFull, newly != 0) == 0) return;
+  cn.dels += __popcll(newly);
+  if (kGlobal)
+    __threadfence();
+  else
+    __threadfence_block();
+  const u64 cur = (lane < WT) ? vload(F.D + static_cast<size_t>(z) * WT + lane) : 0ull;
+  const bool nonempty = __ballot_sync(kFull, cur != 0) != 0;
+  if (lane == 0) {
+    if (!nonempty)
+      set_failed(F, slot, z);
+    else
+      append_var(N, qn, fbn, qlenn, z);
+  }
+}
+
+template <int WT, bool kGlobal>
+__device__ __forceinline__ void revise_arc(const DevNet& N, const Fix& F, u32* qn, u32* fbn, int* qlenn, int slot,
+                                           int y, const Arc A, Cnt& cn) {
+  const int lane = threadIdx.x & 31;
+  const int z = A.z;
+  u64 dy[WT], dz[WT];
+  load_dom_uniform<WT>(F.D + static_cast<size_t>(y) * WT, dy);
+  load_dom_uniform<WT>(F.D + static_cast<size_t>(z) * WT, dz);
+  int cy = 0, cz = 0;
+#pragma unroll
+  for (int w = 0; w < WT; ++w) {
+    cy += __popcll(dy[w]);
+    cz += __popcll(dz[w]);
+  }
+  if (lane == 0) ++cn.rev;
+  if (cy == 0 || cz == 0) {
+    if (lane == 0) set_failed(F, slot, cy == 0 ? y : z);
+    return;
+  }
+  u64 rm[WT];
+#pragma unroll
+  for (int w = 0; w < WT; ++w) rm[w] = 0;
+  if (cy < cz) {
+    // Union of the supports (in z) of the live values of y.
+    u64 acc[WT];
+#pragma unroll
+    for (int w = 0; w < WT; ++w) acc[w] = 0;
+#pragma unroll
+    for (int base = 0; base < 64 * WT; base += 32) {
+      const u32 bits = static_cast<u32>(dy[base >> 6] >> (base & 32));
+      if (bits == 0) continue;
+      if ((bits >> lane) & 1u) {
+        u64 r[WT];
+        load_row<WT>(N.rel, A.yz + static_cast<size_t>(base + lane) * WT, r);
+#pragma unroll
+        for (int w = 0; w < WT; ++w) acc[w] |= r[w];
+      }
+    }
+#pragma unroll
+    for (int w = 0; w < WT; ++w) rm[w] = dz[w] & ~warp_or64(acc[w]);
+    if (lane == 0) cn.rows += cy;
+  } else {
+    // Every live value of z tests its support row against D(y).
+#pragma unroll
+    for (int base = 0; base < 64 * WT; base += 32) {
+      const u32 bits = static_cast<u32>(dz[base >> 6] >> (base & 32));
+      if (bits == 0) continue;
+      bool unsup = false;
+      if ((bits >> lane) & 1u) {
+        u64 r[WT];
+        load_row<WT>(N.rel, A.zy + static_cast<size_t>(base + lane) * WT, r);
+        u64 hit = 0;
+#pragma unroll
+        for (int w = 0; w < WT; ++w) hit |= r[w] & dy[w];
+        unsup = hit == 0;
+      }
+      const u32 m = __ballot_sync(kFull, unsup);
+      rm[base >> 6] |= static_cast<u64>(m) << (base & 32);
+    }
+    if (lane == 0) cn.rows += cz;
+  }
+  commit<WT, kGlobal>(N, F, qn, fbn, qlenn, slot, z, rm, cn);
+}
+
+// Table revision (GAC on a positive table, the definition of
+// samples/verify_gac.cpp:121-164): a tuple is valid iff every coordinate is
+// in its variable's domain; each scope variable keeps exactly the values that
+// appear in a valid tuple. Lanes stride over tuples, projections are OR-reduced
+// across the warp.
+template <int WT, bool kGlobal>
+__device__ __forceinline__ void revise_table(const DevNet& N, const Fix& F, u32* qn, u32* fbn, int* qlenn, int slot,
+                                             int t, Cnt& cn) {
+  if constexpr (WT > 4) {
+    return;  // tables are rejected at upload for domains wider than 256 values
+  } else {
+    const int lane = threadIdx.x & 31;
+    const int r = N.t_arity[t];
+    int s[kMaxArity];
+    u64 snap[kMaxArity][WT], proj[kMaxArity][WT];
+    int empty_var = -1;
+#pragma unroll
+    for (int i = 0; i < kMaxArity; ++i) {
+      s[i] = i < r ? N.t_scope[t * kMaxArity + i] : 0;
+      u64 any = 0;
+      if (i < r) {
+        load_dom_uniform<WT>(F.D + static_cast<size_t>(s[i]) * WT, snap[i]);
+      } else {
+#pragma unroll
+        for (int w = 0; w < WT; ++w) snap[i][w] = 0;
+      }
+#pragma unroll
+      for (int w = 0; w < WT; ++w) {
+        proj[i][w] = 0;
+        any |= snap[i][w];
+      }
+      if (i < r && any == 0) empty_var = s[i];
+    }
+    if (lane == 0) ++cn.rev;
+    if (empty_var >= 0) {
+      if (lane == 0) set_failed(F, slot, empty_var);
+      return;
+    }
+    const int nt = N.t_ntup[t];
+    const uint16_t* tp = N.t_tup + N.t_off[t];
+    for (int k = lane; k < nt; k += 32) {
+      int v[kMaxArity];
+      bool valid = true;
+#pragma unroll
+      for (int i = 0; i < kMaxArity; ++i) {
+        v[i] = 0;
+        if (i < r) {
+          v[i] = tp[static_cast<size_t>(i) * nt + k];
+          valid = valid && ((sel<WT>(snap[i], v[i] >> 6) >> (v[i] & 63)) & 1ull);
+        }
+      }
+      if (valid) {
+#pragma unroll
+        for (int i = 0; i < kMaxArity; ++i)
+          if (i < r) or_at<WT>(proj[i], v[i] >> 6, 1ull << (v[i] & 63));
+      }
+    }
+    if (lane == 0) cn.tuples += nt;
+#pragma unroll
+    for (int i = 0; i < kMaxArity; ++i) {
+      if (i < r) {
+        u64 rm[WT];
+#pragma unroll
+        for (int w = 0; w < WT; ++w) rm[w] = snap[i][w] & ~warp_or64(proj[i][w]);
+        commit<WT, kGlobal>(N, F, qn, fbn, qlenn, slot, s[i], rm, cn);
+      }
+    }
+  }
+}
+
+template <int WT, bool kTab, bool kGlobal>
+__device__ __forceinline__ void process_item(const DevNet& N, const Fix& F, u32 item, u32* fbc, u32* qn, u32* fbn,
+                                             int* qlenn, int slot, int stamp, Cnt& cn) {
+  const int lane = threadIdx.x & 31;
+  const int y = static_cast<int>(item >> kItemVarShift);
+  const int c = static_cast<int>(item & (kMaxChunksPerVar - 1));
+  if (c == 0 && lane == 0) atomicAnd(fbc + (y >> 5), ~(1u << (y & 31)));
+  const int a0 = N.arc_start[y], da = N.arc_start[y + 1] - a0;
+  const int t0 = N.tinc_start[y], dt = N.tinc_start[y + 1] - t0;
+  const int lo = c * N.chunk;
+  const int hi = min(lo + N.chunk, da + dt);
+  for (int i = lo; i < hi; ++i) {
+    if (any_failed(F)) return;
+    if (i < da) {
+      const Arc A = N.arcs[a0 + i];
+      revise_arc<WT, kGlobal>(N, F, qn, fbn, qlenn, slot, y, A, cn);
+    } else if constexpr (kTab) {
+      const int t = N.vtab[t0 + i - da];
+      int prev = 0;
+      if (lane == 0) prev = atomicMax(F.tstamp + t, stamp);
+      prev = __shfl_sync(kFull, prev, 0);
+      if (prev >= stamp) continue;
+      revise_table<WT, kGlobal>(N, F, qn, fbn, qlenn, slot, t, cn);
+    }
+  }
+}
+
+// CTA-local fixpoint; the caller has seeded queue 0 and synchronised.
+// Returns the number of rounds; sets *err on a round-count overrun.
+template <int WT, bool kTab>
+__device__ int cta_fixpoint(const DevNet& N, const Fix& F, Cnt& cn, int* err) {
+  const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const long long max_rounds = N.total_values + 2;
+  int r = 0;
+  for (;; ++r) {
+    const int cur = r & 1;
+    const int len = vloadi(F.qlen + r % 3);
+    const int fl = vloadi(F.failed + cur);
+    if (len == 0 || fl) break;
+    if (r > max_rounds) {
+      if (threadIdx.x == 0) atomicExch(err, -4);
+      break;
+    }
+    if (threadIdx.x == 0) F.qlen[(r + 2) % 3] = 0;
+    const u32* qc = cur ? F.q1 : F.q0;
+    u32* qn = cur ? F.q0 : F.q1;
+    u32* fbc = cur ? F.fb1 : F.fb0;
+    u32* fbn = cur ? F.fb0 : F.fb1;
+    int* qlenn = F.qlen + (r + 1) % 3;
+    for (int j = warp; j < len; j += nwarps)
+      process_item<WT, kTab, false>(N, F, qc[j], fbc, qn, fbn, qlenn, cur ^ 1, F.stamp_base + r + 1, cn);
+    __syncthreads();
+  }
+  return r;
+}
+
+// Layout of the CTA-local state inside a byte buffer.
+struct CtaLayout {
+  size_t d, q0, q1, fb0, fb1, ts, total;
+};
+
+__host__ __device__ inline CtaLayout cta_layout(const DevNet& N) {
+  CtaLayout L;
+  auto up = [](size_t x) { return (x + 15) & ~size_t(15); };
+  const size_t nw = (static_cast<size_t>(N.n) + 31) / 32;
+  L.d = 0;
+  L.q0 = up(L.d + static_cast<size_t>(N.n) * N.W * 8);
+  L.q1 = up(L.q0 + static_cast<size_t>(N.max_items) * 4);
+  L.fb0 = up(L.q1 + static_cast<size_t>(N.max_items) * 4);
+  L.fb1 = up(L.fb0 + nw * 4);
+  L.ts = up(L.fb1 + nw * 4);
+  L.total = up(L.ts + static_cast<size_t>(N.nt) * 4);
+  return L;
+}
+
+__device__ __forceinline__ Fix make_cta_fix(const DevNet& N, char* base, int* qlen, int* failed, int* fail_var) {
+  const CtaLayout L = cta_layout(N);
+  Fix F;
+  F.D = reinterpret_cast<u64*>(base + L.d);
+  F.q0 = reinterpret_cast<u32*>(base + L.q0);
+  F.q1 = reinterpret_cast<u32*>(base + L.q1);
+  F.fb0 = reinterpret_cast<u32*>(base + L.fb0);
+  F.fb1 = reinterpret_cast<u32*>(base + L.fb1);
+  F.tstamp = N.nt ? reinterpret_cast<int*>(base + L.ts) : nullptr;
+  F.qlen = qlen;
+  F.failed = failed;
+  F.fail_var = fail_var;
+  F.stamp_base = 0;
+  return F;
+}
+
+// Copies n*WT words with 16-byte vector accesses where possible.
+__device__ __forceinline__ void block_copy(u64* dst, const u64* src, size_t words) {
+  if (((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15) == 0) {
+    const size_t h = words / 2;
+    const ulonglong2* s = reinterpret_cast<const ulonglong2*>(src);
+    ulonglong2* d = reinterpret_cast<ulonglong2*>(dst);
+    for (size_t i = threadIdx.x; i < h; i += blockDim.x) d[i] = s[i];
+    if ((words & 1) && threadIdx.x == 0) dst[words - 1] = src[words - 1];
+  } else {
+    for (size_t i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+  }
+}
+
+__device__ __forceinline__ void block_zero(u32* p, size_t n) {
+  for (size_t i = threadIdx.x; i < n; i += blockDim.x) p[i] = 0;
+}
+
+__device__ __forceinline__ void flush_counts(KStats* st, const Cnt& cn) {
+  // Warp-reduce then one atomic per warp.
+  u64 rev = cn.rev, rows = cn.rows, tuples = cn.tuples, dels = cn.dels;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    rev += __shfl_xor_sync(kFull, rev, o);
+    rows += __shfl_xor_sync(kFull, rows, o);
+    tuples += __shfl_xor_sync(kFull, tuples, o);
+    dels += __shfl_xor_sync(kFull, dels, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (rev) atomicAdd(&st->revisions, rev);
+    if (rows) atomicAdd(&st->rows, rows);
+    if (tuples) atomicAdd(&st->tuples, tuples);
+    if (dels) atomicAdd(&st->deletions, dels);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_node: one CTA, one network state.
+// ---------------------------------------------------------------------------
+template <int WT, bool kTab>
+__global__ void __launch_bounds__(512) k_node(DevNet N, u64* levels, int src, int dst, int op, int var, int val,
+                                               const int* evt, int nevt, KStats* st, uint8_t* ok_out,
+                                               char* gscratch) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_qlen[3], s_failed[2], s_failvar, s_err;
+  char* base = gscratch ? gscratch : reinterpret_cast<char*>(smem_raw);
+  Fix F = make_cta_fix(N, base, s_qlen, s_failed, &s_failvar);
+  const size_t words = static_cast<size_t>(N.n) * WT;
+  const CtaLayout L = cta_layout(N);
+  block_copy(F.D, levels + static_cast<size_t>(src) * words, words);
+  block_zero(reinterpret_cast<u32*>(base + L.fb0), (L.ts - L.fb0) / 4);
+  if (N.nt) block_zero(reinterpret_cast<u32*>(F.tstamp), N.nt);
+  if (threadIdx.x == 0) {
+    s_qlen[0] = s_qlen[1] = s_qlen[2] = 0;
+    s_failed[0] = s_failed[1] = 0;
+    s_failvar = -1;
+    s_err = 0;
+  }
+  __syncthreads();
+  if (op == kOpRoot) {
+    for (int z = threadIdx.x; z < N.n; z += blockDim.x) seed_var<WT>(N, F, z);
+  } else if (op == kOpEvents) {
+    for (int i = threadIdx.x; i < nevt; i += blockDim.x) seed_var<WT>(N, F, evt[i]);
+  } else if (threadIdx.x == 0) {
+    u64* dv = F.D + static_cast<size_t>(var) * WT;
+    if (op == kOpAssign || op == kOpSingleton) {
+      for (int w = 0; w < WT; ++w) dv[w] = (w == (val >> 6)) ? (1ull << (val & 63)) : 0ull;
+    } else {  // refute
+      dv[val >> 6] &= ~(1ull << (val & 63));
+    }
+    seed_var<WT>(N, F, var);
+  }
+  __syncthreads();
+  Cnt cn;
+  const int rounds = cta_fixpoint<WT, kTab>(N, F, cn, &s_err);
+  const bool failed = (s_failed[0] | s_failed[1]) != 0;
+  if (op != kOpSingleton) block_copy(levels + static_cast<size_t>(dst) * words, F.D, words);
+  flush_counts(st, cn);
+  if (threadIdx.x == 0) {
+    st->inconsistent = failed ? 1 : 0;
+    st->fail_var = s_failvar;
+    atomicMax(&st->rounds_max, rounds);
+    atomicAdd(&st->fixpoints, 1ull);
+    if (s_err) st->error = s_err;
+    if (ok_out) *ok_out = failed ? 0 : 1;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_sac: persistent CTAs over the SAC branch work list.
+// ---------------------------------------------------------------------------
+template <int WT, bool kTab>
+__global__ void __launch_bounds__(256) k_sac(DevNet N, const u64* root, const int2* work, const int* nwork,
+                                             int* cursor, uint8_t* ok, KStats* st, char* gscratch, size_t gstride) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_qlen[3], s_failed[2], s_failvar, s_err, s_b;
+  char* base = gscratch ? gscratch + blockIdx.x * gstride : reinterpret_cast<char*>(smem_raw);
+  Fix F = make_cta_fix(N, base, s_qlen, s_failed, &s_failvar);
+  const CtaLayout L = cta_layout(N);
+  const size_t words = static_cast<size_t>(N.n) * WT;
+  const int total = *nwork;
+  if (threadIdx.x == 0) s_err = 0;
+  Cnt cn;
+  int rounds_max = 0;
+  u64 done = 0;
+  for (;;) {
+    if (threadIdx.x == 0) s_b = atomicAdd(cursor, 1);
+    __syncthreads();
+    const int b = s_b;
+    if (b >= total) break;
+    const int2 xa = work[b];
+    block_copy(F.D, root, words);
+    block_zero(reinterpret_cast<u32*>(base + L.fb0), (L.ts - L.fb0) / 4);
+    if (N.nt) block_zero(reinterpret_cast<u32*>(F.tstamp), N.nt);
+    if (threadIdx.x == 0) {
+      s_qlen[0] = s_qlen[1] = s_qlen[2] = 0;
+      s_failed[0] = s_failed[1] = 0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      u64* dv = F.D + static_cast<size_t>(xa.x) * WT;
+      for (int w = 0; w < WT; ++w) dv[w] = (w == (xa.y >> 6)) ? (1ull << (xa.y & 63)) : 0ull;
+      append_var(N, F.q0, F.fb0, F.qlen, xa.x);
+    }
+    __syncthreads();
+    const int rounds = cta_fixpoint<WT, kTab>(N, F, cn, &s_err);
+    rounds_max = max(rounds_max, rounds);
+    if (threadIdx.x == 0) ok[b] = (s_failed[0] | s_failed[1]) ? 0 : 1;
+    ++done;
+    __syncthreads();
+  }
+  flush_counts(st, cn);
+  if (threadIdx.x == 0) {
+    atomicMax(&st->rounds_max, rounds_max);
+    if (done) {
+      atomicAdd(&st->fixpoints, done);
+      atomicAdd(&st->branches, done);
+    }
+    if (s_err) st->error = s_err;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_ac_grid: whole-grid fixpoint with a bounded grid barrier.
+// ---------------------------------------------------------------------------
+// Sense-free generation barrier; every block waits at most
+// kBarrierTimeoutNs, then reports CP_E_TIMEOUT through *err and returns false.
+__device__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* err) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    volatile unsigned* vgen = bar + 1;
+    const unsigned gen = *vgen;
+    __threadfence();
+    const unsigned arrived = atomicAdd(bar, 1u);
+    if (arrived == nblocks - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      const long long t0 = globaltimer_ns();
+      unsigned sleep = 32;
+      while (*vgen == gen) {
+        if (vloadi(err) != 0 || globaltimer_ns() - t0 > kBarrierTimeoutNs) {
+          atomicExch(err, -4);
+          ok = 0;
+          break;
+        }
+        __nanosleep(sleep);
+        if (sleep < 1024) sleep <<= 1;
+      }
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+template <int WT, bool kTab>
+__global__ void __launch_bounds__(512) k_ac_grid(DevNet N, u64* D, const int* evt, const int* nevt_dev, int nevt,
+                                                 GridScratch G, KStats* st) {
+  Fix F;
+  F.D = D;
+  F.q0 = G.q[0];
+  F.q1 = G.q[1];
+  F.fb0 = G.fb[0];
+  F.fb1 = G.fb[1];
+  F.qlen = G.qlen;
+  F.tstamp = G.tstamp;
+  F.failed = G.failed;
+  F.fail_var = &st->fail_var;
+  F.stamp_base = vloadi(G.epoch);
+  const unsigned nblocks = gridDim.x;
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gthreads = gridDim.x * blockDim.x;
+  const int ne = evt ? (nevt_dev ? vloadi(nevt_dev) : nevt) : N.n;
+  for (int i = gtid; i < ne; i += gthreads) seed_var<WT>(N, F, evt ? evt[i] : i);
+  int* err = &st->grid_err;
+  Cnt cn;
+  const long long max_rounds = N.total_values + 2;
+  int r = 0;
+  bool ok = grid_barrier(G.bar, nblocks, err);
+  const int gwarp = gtid >> 5, nwarps = gthreads >> 5;
+  for (; ok; ++r) {
+    const int cur = r & 1;
+    const int len = vloadi(F.qlen + r % 3);
+    const int fl = vloadi(F.failed + cur);
+    if (len == 0 || fl) break;
+    if (r > max_rounds) {
+      if (gtid == 0) st->error = -4;
+      break;
+    }
+    if (gtid == 0) F.qlen[(r + 2) % 3] = 0;
+    const u32* qc = cur ? F.q1 : F.q0;
+    u32* qn = cur ? F.q0 : F.q1;
+    u32* fbc = cur ? F.fb1 : F.fb0;
+    u32* fbn = cur ? F.fb0 : F.fb1;
+    int* qlenn = F.qlen + (r + 1) % 3;
+    for (int j = gwarp; j < len; j += nwarps)
+      process_item<WT, kTab, true>(N, F, qc[j], fbc, qn, fbn, qlenn, cur ^ 1, F.stamp_base + r + 1, cn);
+    ok = grid_barrier(G.bar, nblocks, err);
+  }
+  flush_counts(st, cn);
+  if (gtid == 0) {
+    st->inconsistent = (vloadi(F.failed) | vloadi(F.failed + 1)) ? 1 : 0;
+    atomicMax(&st->rounds_max, r);
+    atomicAdd(&st->fixpoints, 1ull);
+    *G.epoch = F.stamp_base + r + 2;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Small kernels.
+// ---------------------------------------------------------------------------
+// Live (x, a) pairs of a level, one warp per variable: ballot of the live
+// flags, lane offsets by prefix popcount, one atomic per 32 values.
+template <int WT>
+__global__ void k_build_work(DevNet N, const u64* dom, int2* work, int* nwork) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int x = gw; x < N.n; x += nw) {
+    const int ds = N.dsize[x];
+    for (int base = 0; base < ds; base += 32) {
+      const u64 word = dom[static_cast<size_t>(x) * WT + (base >> 6)];
+      const u32 bits = static_cast<u32>(word >> (base & 32));
+      if (bits == 0) continue;
+      int b0 = 0;
+      if (lane == 0) b0 = atomicAdd(nwork, __popc(bits));
+      b0 = __shfl_sync(kFull, b0, 0);
+      if ((bits >> lane) & 1u) work[b0 + __popc(bits & ((1u << lane) - 1u))] = make_int2(x, base + lane);
+    }
+  }
+}
+
+__global__ void k_commit(int W, const int2* work, const int* nwork, const uint8_t* ok, u64* dom, int* evt, int* nevt,
+                         u32* evt_fb, KStats* st) {
+  const int total = *nwork;
+  u64 removed = 0;
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < total; b += gridDim.x * blockDim.x) {
+    if (ok[b]) continue;
+    const int2 xa = work[b];
+    atomicAnd(dom + static_cast<size_t>(xa.x) * W + (xa.y >> 6), ~(1ull << (xa.y & 63)));
+    ++removed;
+    const u32 bit = 1u << (xa.x & 31);
+    if (!(atomicOr(evt_fb + (xa.x >> 5), bit) & bit)) evt[atomicAdd(nevt, 1)] = xa.x;
+  }
+  if (removed) {
+    atomicAdd(&st->removed, removed);
+    atomicAdd(&st->deletions, removed);
+  }
+}
+
+// B block of constraint c (rows of y values over x values) from its A block,
+// one warp per (c, group of 32 x values): each lane holds one x row; the
+// ballot over lanes of bit b is the 32-bit slice of y=b's row.
+template <int WT>
+__global__ void k_transpose(DevNet N, u64* rel, const int* bx, const int* by, const int64_t* offA,
+                            const int64_t* offB, int groups) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int item = gw; item < N.nb * groups; item += nw) {
+    const int c = item / groups, g = item % groups;
+    const int dx = N.dsize[bx[c]], dy = N.dsize[by[c]];
+    if (g * 32 >= dx) continue;
+    const int a = g * 32 + lane;
+    u64 row[WT];
+#pragma unroll
+    for (int w = 0; w < WT; ++w) row[w] = (a < dx) ? rel[offA[c] + static_cast<int64_t>(a) * WT + w] : 0ull;
+    u32* out = reinterpret_cast<u32*>(rel + offB[c]);
+    for (int bb = 0; bb < dy; bb += 32) {
+      u32 mine = 0;
+#pragma unroll 4
+      for (int j = 0; j < 32; ++j) {
+        const int b = bb + j;
+        const bool bit = b < dy && ((sel<WT>(row, b >> 6) >> (b & 63)) & 1ull);
+        const u32 m = __ballot_sync(kFull, bit);
+        if (lane == j) mine = m;
+      }
+      const int b = bb + lane;
+      if (b < dy) out[(static_cast<int64_t>(b) * WT) * 2 + g] = mine;
+    }
+  }
+}
+
+template <int WT>
+__global__ void k_popcount(int n, const u64* dom, int* sizes) {
+  for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x) {
+    int s = 0;
+#pragma unroll
+    for (int w = 0; w < WT; ++w) s += __popcll(dom[static_cast<size_t>(x) * WT + w]);
+    sizes[x] = s;
+  }
+}
+
+__global__ void k_level_edit(int W, u64* dom, int var, int val, int op) {
+  u64* dv = dom + static_cast<size_t>(var) * W;
+  if (op == kOpAssign) {
+    for (int w = 0; w < W; ++w) dv[w] = (w == (val >> 6)) ? (1ull << (val & 63)) : 0ull;
+  } else {
+    dv[val >> 6] &= ~(1ull << (val & 63));
+  }
+}
+
+template <typename F>
+cudaError_t dispatch_w(int W, F&& f) {
+  switch (W) {
+    case 1: return f(std::integral_constant<int, 1>{});
+    case 2: return f(std::integral_constant<int, 2>{});
+    case 4: return f(std::integral_constant<int, 4>{});
+    case 8: return f(std::integral_constant<int, 8>{});
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// Dispatch on the domain width and on whether the network has tables
+// (binary-only networks use kernels without the table path, which keeps
+// their register count low).
+template <typename F>
+cudaError_t dispatch_wt(const DevNet& N, F&& f) {
+  if (N.nt > 0) {
+    switch (N.W) {
+      case 1: return f(std::integral_constant<int, 1>{}, std::true_type{});
+      case 2: return f(std::integral_constant<int, 2>{}, std::true_type{});
+      case 4: return f(std::integral_constant<int, 4>{}, std::true_type{});
+      default: return cudaErrorInvalidValue;
+    }
+  }
+  return dispatch_w(N.W, [&](auto wt) { return f(wt, std::false_type{}); });
+}
+
+template <typename K>
+cudaError_t allow_smem(K kernel, size_t bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+}
+
+}  // namespace
+
+size_t cta_state_bytes(const DevNet& N) { return cta_layout(N).total; }
+
+cudaError_t launch_node(const DevNet& N, u64* levels, int src, int dst, int op, int var, int val, const int* evt,
+                        int nevt, KStats* st, uint8_t* ok_out, int block, void* gscratch, cudaStream_t s) {
+  const size_t smem = gscratch ? 0 : cta_state_bytes(N);
+  return dispatch_wt(N, [&](auto wt, auto tab) -> cudaError_t {
+    constexpr int WT = decltype(wt)::value;
+    constexpr bool TB = decltype(tab)::value;
+    cudaError_t e = allow_smem(k_node<WT, TB>, smem);
+    if (e != cudaSuccess) return e;
+    k_node<WT, TB><<<1, block, smem, s>>>(N, levels, src, dst, op, var, val, evt, nevt, st, ok_out,
+                                      static_cast<char*>(gscratch));
+    return cudaGetLastError();
+  });
+}
+
+int ac_grid_max_blocks(const DevNet& N, int block, int sm_count) {
+  int per_sm = 0;
+  cudaError_t e = dispatch_wt(N, [&](auto wt, auto tab) -> cudaError_t {
+    constexpr int WT = decltype(wt)::value;
+    constexpr bool TB = decltype(tab)::value;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ac_grid<WT, TB>, block, 0);
+  });
+  if (e != cudaSuccess || per_sm < 1) return 0;
+  return per_sm * sm_count;
+}
+
+cudaError_t launch_ac_grid(const DevNet& N, u64* level_dom, const int* evt, const int* nevt_dev, int nevt,
+                           GridScratch G, KStats* st, int block, int grid, cudaStream_t s) {
+  return dispatch_wt(N, [&](auto wt, auto tab) -> cudaError_t {
+    constexpr int WT = decltype(wt)::value;
+    constexpr bool TB = decltype(tab)::value;
+    DevNet n2 = N;
+    void* args[] = {&n2, &level_dom, &evt, &nevt_dev, &nevt, &G, &st};
+    return cudaLaunchCooperativeKernel(reinterpret_cast<void*>(k_ac_grid<WT, TB>), dim3(grid), dim3(block), args, 0,
+                                       s);
+  });
+}
+
+int sac_blocks_per_sm(const DevNet& N, int block, bool smem_state) {
+  const size_t smem = smem_state ? cta_state_bytes(N) : 0;
+  int per_sm = 0;
+  cudaError_t e = dispatch_wt(N, [&](auto wt, auto tab) -> cudaError_t {
+    constexpr int WT = decltype(wt)::value;
+    constexpr bool TB = decltype(tab)::value;
+    cudaError_t e2 = allow_smem(k_sac<WT, TB>, smem);
+    if (e2 != cudaSuccess) return e2;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sac<WT, TB>, block, smem);
+  });
+  return e == cudaSuccess ? per_sm : 0;
+}
+
+cudaError_t launch_sac_branches(const DevNet& N, const u64* root, const int2* work, const int* nwork, int* cursor,
+                                uint8_t* ok, KStats* st, int block, int grid, void* gscratch, size_t gstride,
+                                cudaStream_t s) {
+  const size_t smem = gscratch ? 0 : cta_state_bytes(N);
+  return dispatch_wt(N, [&](auto wt, auto tab) -> cudaError_t {
+    constexpr int WT = decltype(wt)::value;
+    constexpr bool TB = decltype(tab)::value;
+    cudaError_t e = allow_smem(k_sac<WT, TB>, smem);
+    if (e != cudaSuccess) return e;
+    k_sac<WT, TB><<<grid, block, smem, s>>>(N, root, work, nwork, cursor, ok, st, static_cast<char*>(gscratch), gstride);
+    return cudaGetLastError();
+  });
+}
+
+cudaError_t launch_build_work(const DevNet& N, const u64* dom, SacScratch S, cudaStream_t s) {
+  return dispatch_w(N.W, [&](auto wt) -> cudaError_t {
+    constexpr int WT = decltype(wt)::value;
+    const int blocks = std::max(1, std::min(4096, (N.n * 32 + 255) / 256));
+    k_build_work<WT><<<blocks, 256, 0, s>>>(N, dom, S.work, S.nwork);
+    return cudaGetLastError();
+  });
+}
+
+cudaError_t launch_commit(const DevNet& N, u64* dom, SacScratch S, KStats* st, cudaStream_t s) {
+  const int blocks = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(4096, (N.total_values + 255) / 256)));
+  k_commit<<<blocks, 256, 0, s>>>(N.W, S.work, S.nwork, S.ok, dom, S.evt, S.nevt, S.evt_fb, st);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_transpose(const DevNet& N, u64* rel, const int* bx, const int* by, const int64_t* offA,
+                             const int64_t* offB, cudaStream_t s) {
+  if (N.nb == 0) return cudaSuccess;
+  const int groups = 2 * N.W;
+  return dispatch_w(N.W, [&](auto wt) -> cudaError_t {
+    constexpr int WT = decltype(wt)::value;
+    const int64_t warps = static_cast<int64_t>(N.nb) * groups;
+    const int blocks = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(8192, (warps * 32 + 255) / 256)));
+    k_transpose<WT><<<blocks, 256, 0, s>>>(N, rel, bx, by, offA, offB, groups);
+    return cudaGetLastError();
+  });
+}
+
+cudaError_t launch_popcount(const DevNet& N, const u64* dom, int* sizes, cudaStream_t s) {
+  return dispatch_w(N.W, [&](auto wt) -> cudaError_t {
+    constexpr int WT = decltype(wt)::value;
+    const int blocks = std::max(1, std::min(1024, (N.n + 255) / 256));
+    k_popcount<WT><<<blocks, 256, 0, s>>>(N.n, dom, sizes);
+    return cudaGetLastError();
+  });
+}
+
+cudaError_t launch_level_edit(const DevNet& N, u64* dom, int var, int val, int op, cudaStream_t s) {
+  k_level_edit<<<1, 1, 0, s>>>(N.W, dom, var, val, op);
+  return cudaGetLastError();
+}
+
+}  // namespace cpgpu

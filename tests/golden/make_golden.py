@@ -54,9 +54,9 @@ def cases():
     # GAC oracle), and the reference's generic AC3 on the mixed instance
     # itself, recorded to document its mixed-arity defect.
     for s in range(1, 4):
-        args = [60, 16, 200, 0.3, 0.5, 40, 60, 0.2, s]
-        out.append(("mixedbin", ["mixedbin"] + args, "ac3bit"))
-        out.append(("mixed_ref_ac3", ["mixed"] + args, "ac3"))
+        for args in ([60, 8, 150, 0.2, 0.4, 20, 300, 0.1, s], [60, 16, 200, 0.2, 0.4, 30, 2000, 0.1, s]):
+            out.append(("mixedbin", ["mixedbin"] + args, "ac3bit"))
+            out.append(("mixed_ref_ac3", ["mixed"] + args, "ac3"))
     return out
 
 

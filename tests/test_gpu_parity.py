@@ -1,0 +1,203 @@
+"""GPU parity: the engine's results through the C ABI against the reference's
+own outputs (golden fixtures) and the CPU oracle. Bit-exact: final domain
+words, verdicts, deletion counts, MAC node counts and first solutions."""
+import numpy as np
+import pytest
+
+import cpim_gb300 as cp
+from oracle import pyoracle as O
+from tests.golden_cases import dom_hex, make_engine_instance, oracle_view_of
+
+pytestmark = pytest.mark.gpu
+
+
+def _cases(golden, op, names=None):
+    return [c for c in golden if c["op"] == op and (names is None or c["name"] in names)]
+
+
+def test_ac_matches_reference(engine, golden):
+    cases = _cases(golden, "ac3bit")
+    assert cases
+    for c in cases:
+        inst = make_engine_instance(c["args"])
+        net = engine.upload(inst)
+        st = net.enforce_ac(0)
+        r = c["result"]
+        assert bool(st.inconsistent) == (not r["consistent"]), c["args"]
+        if r["consistent"]:
+            assert st.deletions == r["deletions"], c["args"]
+            assert dom_hex(net.dom_get(0)) == r["domains"], c["args"]
+        net.close()
+
+
+def test_sac1_matches_reference(engine, golden):
+    cases = _cases(golden, "sac1")
+    assert cases
+    for c in cases:
+        inst = make_engine_instance(c["args"])
+        net = engine.upload(inst)
+        st = net.enforce_sac1(0)
+        r = c["result"]
+        assert bool(st.inconsistent) == (not r["consistent"]), c["args"]
+        if r["consistent"]:
+            assert st.deletions == r["deletions"], c["args"]
+            assert dom_hex(net.dom_get(0)) == r["domains"], c["args"]
+        net.close()
+
+
+def test_mac_matches_reference(engine, golden):
+    cases = _cases(golden, "mac")
+    assert cases
+    for c in cases:
+        inst = make_engine_instance(c["args"])
+        net = engine.upload(inst)
+        m = net.mac_solve(time_limit_ms=60000)
+        r = c["result"]
+        assert m["num_positive"] == r["num_positive"], c["args"]
+        assert m["num_negative"] == r["num_negative"], c["args"]
+        assert (m["status"] == 1) == (r["num_sol"] == 1), c["args"]
+        if m["status"] == 1:
+            assert m["solution"] == r["solution"], c["args"]
+        net.close()
+
+
+@pytest.mark.parametrize("args", [(60, 8, 150, 0.2, 0.4, 20, 300, 0.1), (60, 16, 200, 0.2, 0.4, 30, 2000, 0.1),
+                                  (40, 8, 100, 0.3, 0.5, 30, 150, 0.1), (30, 8, 60, 0.3, 0.5, 40, 60, 0.2)])
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_gac_mixed_matches_oracle(engine, args, seed):
+    inst = cp.gen_mixed(*args, seed)
+    ok, d, dels = O.gac(oracle_view_of(inst))
+    net = engine.upload(inst)
+    st = net.enforce_ac(0)
+    assert bool(st.inconsistent) == (not ok)
+    if ok:
+        assert st.deletions == dels
+        assert np.array_equal(net.dom_get(0), d)
+    net.close()
+
+
+@pytest.mark.parametrize("args", [(40, 8, 100, 0.2, 0.3, 15, 350, 0.0), (30, 8, 60, 0.25, 0.45, 20, 120, 0.1)])
+def test_sac_mixed_matches_oracle(engine, args):
+    for seed in (1, 2):
+        inst = cp.gen_mixed(*args, seed)
+        ok, d, dels = O.sac1(oracle_view_of(inst))
+        net = engine.upload(inst)
+        st = net.enforce_sac1(0)
+        assert bool(st.inconsistent) == (not ok)
+        if ok:
+            assert np.array_equal(net.dom_get(0), d)
+            assert st.deletions == dels
+        net.close()
+
+
+def test_singletons_batched_plain_oracle(engine):
+    inst = cp.gen_binary(100, 128, 1000, 0.4, 0.4, 0.0, 7)
+    ov = oracle_view_of(inst)
+    net = engine.upload(inst)
+    rng = np.random.default_rng(5)
+    xs = rng.integers(0, inst.n, 300).astype(np.int32)
+    avals = rng.integers(0, 128, 300).astype(np.int32)
+    ok_b, st_b = net.singletons(xs, avals, mode=0)
+    ok_p, st_p = net.singletons(xs, avals, mode=1)
+    assert np.array_equal(ok_b, ok_p)
+    d0 = inst.init.copy()
+    for i in range(0, 300, 10):
+        assert bool(ok_b[i]) == O.singleton(ov, d0, int(xs[i]), int(avals[i]))
+    assert st_b.branches == 300 and st_p.launches == 300
+    net.close()
+
+
+def test_singletons_tight_failures(engine):
+    # Tight network where many singleton tests fail: batched == plain == oracle.
+    # Singleton tests run on an AC-closed level, as in SAC1 (the closure of
+    # the level with x reduced to a is then unique).
+    for seed in (2, 3):
+        inst = cp.gen_binary(30, 8, 120, 0.45, 0.45, 0.1, seed)
+        ov = oracle_view_of(inst)
+        net = engine.upload(inst)
+        st = net.enforce_ac(0)
+        assert not st.inconsistent
+        dom = net.dom_get(0)
+        okc, d_or, _ = O.ac3bit(ov)
+        assert okc and np.array_equal(dom, d_or)
+        xs, vs = [], []
+        for x in range(inst.n):
+            for a in range(8):
+                if (int(dom[x]) >> a) & 1:
+                    xs.append(x)
+                    vs.append(a)
+        ok_b, _ = net.singletons(xs, vs, mode=0)
+        ok_p, _ = net.singletons(xs, vs, mode=1)
+        assert np.array_equal(ok_b, ok_p)
+        ref = [O.singleton(ov, dom, x, a) for x, a in zip(xs, vs)]
+        assert ok_b.astype(bool).tolist() == ref
+        assert 0 < sum(ref) < len(ref)
+        net.close()
+
+
+@pytest.mark.parametrize("args", [(800, 64, 6000, 0.2, 0.5, 1500, 1000, 0.2, 11),
+                                  (800, 64, 6000, 0.2, 0.5, 1500, 500, 0.2, 11),
+                                  (2000, 64, 30000, 0.2, 0.5, 5000, 1200, 0.2, 1),
+                                  (2000, 64, 30000, 0.2, 0.5, 5000, 500, 0.2, 1)])
+def test_grid_kernel_large_mixed_matches_oracle(engine, args):
+    # More than 8192 arc+table incidences: the single-instance fixpoint runs on
+    # the whole grid (cooperative persistent kernel). The last case is the
+    # full mixed-arity workload (n=2000, d=64, 30000 binary + 5000 ternary
+    # tables of 500 tuples, 20% of values removed), whose GAC closure is empty.
+    inst = cp.gen_mixed(*args)
+    ok, d, dels = O.gac(oracle_view_of(inst))
+    net = engine.upload(inst)
+    st = net.enforce_ac(0)
+    assert bool(st.inconsistent) == (not ok)
+    if ok:
+        assert st.deletions == dels
+        assert np.array_equal(net.dom_get(0), d)
+        # Idempotent: a second pass removes nothing.
+        st2 = net.enforce_ac(0)
+        assert st2.deletions == 0 and not st2.inconsistent
+    net.close()
+
+
+def test_grid_kernel_binary_matches_oracle(engine):
+    inst = cp.gen_binary(2000, 64, 30000, 0.2, 0.5, 0.2, 3)
+    ok, d, dels = O.ac3bit(oracle_view_of(inst))
+    net = engine.upload(inst)
+    st = net.enforce_ac(0)
+    assert bool(st.inconsistent) == (not ok)
+    if ok:
+        assert st.deletions == dels
+        assert np.array_equal(net.dom_get(0), d)
+    net.close()
+
+
+def test_gsolver_solution_valid(engine):
+    for seed in range(1, 6):
+        inst = cp.gen_binary(50, 16, 250, 0.3, 0.3, 0.0, seed)
+        net = engine.upload(inst)
+        g = net.gsolver_solve(time_limit_ms=60000)
+        m = O.mac(oracle_view_of(inst))
+        assert (g["status"] == 1) == (m["status"] == 1)
+        if g["status"] == 1:
+            assert O.check_solution(oracle_view_of(inst), g["solution"])
+        net.close()
+
+
+def test_level_ops_round_trip(engine):
+    inst = cp.gen_binary(20, 100, 40, 0.5, 0.5, 0.0, 4)
+    net = engine.upload(inst, max_levels=4)
+    d0 = net.dom_get(0)
+    assert np.array_equal(d0, inst.init)
+    net.level_copy(0, 1)
+    net.reduce_to(1, 3, 77)
+    d1 = net.dom_get(1)
+    assert net.sizes(1)[3] == 1 and (int(d1[3 * 2 + 1]) >> (77 - 64)) & 1
+    net.remove(1, 4, 5)
+    assert net.sizes(1)[4] == 99
+    assert np.array_equal(net.dom_get(0), d0)
+    with pytest.raises(cp.CPError):
+        net.reduce_to(1, 3, 100)
+    with pytest.raises(cp.CPError):
+        net.level_copy(0, 4)
+    net.dom_set(2, d0)
+    assert np.array_equal(net.dom_get(2), d0)
+    net.close()
