@@ -72,7 +72,7 @@ class ClockSampler:
              "clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -149,8 +149,11 @@ def run_reference(args):
     inst = cp.gen_binary(N, D, E, P, P, 0.0, SEED)
     threads = os.cpu_count() or 1
     vals = []
+    # Each step is a bounded sample sized so the whole run stays near 90 s of
+    # wall time on the host's cores.
+    per_step_wall = max(0.25, 90.0 / max(1, args.warmup + args.steps))
     for i in range(args.warmup + args.steps):
-        r = cpu_baseline_port(inst, threads, budget_s=4.0 * threads)
+        r = cpu_baseline_port(inst, threads, budget_s=per_step_wall * threads)
         if i >= args.warmup:
             vals.append(r["value"])
     v = statistics.median(vals)
@@ -202,6 +205,16 @@ def run_ours(args):
     torch.cuda.synchronize()
     launches0 = eng.launches
     sts = []
+    if args.quick:
+        # Profiling mode: the timed steps only, no baselines and no e2e leg.
+        for _ in range(args.steps):
+            sts.append(step())
+        torch.cuda.synchronize()
+        if rank == 0:
+            print(json.dumps({"quick": True, "steps": len(sts), "ms_per_step": sum(s.device_ms for s in sts) / len(sts),
+                              "kernel_ms": sum(s.kernel_ms for s in sts) / len(sts),
+                              "branches": int(sts[-1].branches)}))
+        return 0
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
             sts.append(step())
@@ -307,9 +320,10 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--quick", action="store_true", help="timed steps only (for profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
