@@ -49,6 +49,8 @@ int internal_words(int W) {
 
 }  // namespace
 
+void cpgpu::set_last_error(const std::string& msg) { g_last_error = msg; }
+
 struct cp_engine {
   int device = 0;
   cudaStream_t stream = nullptr;

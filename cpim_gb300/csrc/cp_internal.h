@@ -18,6 +18,8 @@
 #pragma once
 
 #include <cstdint>
+#include <string>
+
 #include <cuda_runtime.h>
 
 namespace cpgpu {
@@ -122,6 +124,8 @@ cudaError_t launch_commit(const DevNet& N, u64* dom, SacScratch S, KStats* st, c
 // Builds the B blocks (transposes) of the binary relations.
 cudaError_t launch_transpose(const DevNet& N, u64* rel, const int* bx, const int* by, const int64_t* offA,
                              const int64_t* offB, cudaStream_t s);
+// Sets the message returned by cp_last_error_string on this thread.
+void set_last_error(const std::string& msg);
 // Level helpers.
 cudaError_t launch_popcount(const DevNet& N, const u64* dom, int* sizes, cudaStream_t s);
 cudaError_t launch_level_edit(const DevNet& N, u64* dom, int var, int val, int op, cudaStream_t s);

@@ -158,6 +158,27 @@ int cp_gen_export(const cp_instance* inst, int* dom, uint64_t* init, int* bin_sc
 /* Uploads an instance directly (no host export). */
 int cp_net_upload_instance(cp_engine* e, const cp_instance* inst, int max_levels, cp_net** out);
 
+/* ---- allocation-free AC fixpoint ------------------------------------------
+ * No counterpart in the reference. For callers that must not allocate device
+ * memory while they run: cudaMalloc/cudaFree synchronise the whole device
+ * (a stall for a latency-bound search or serving loop), and a host framework
+ * that already owns the device memory budget may not let a plugin allocate.
+ * The caller keeps a binary network in its own device buffers, in the upload
+ * format above: d_dom_size[n], d_bin_scope[2*n_bin], d_bin_rows (dom[x]*W
+ * words per constraint), and the domains d_dom[n*W] (level image, updated in
+ * place to the AC fixpoint; bits beyond each size are cleared). On the given
+ * stream (NULL = default stream) the call writes d_status[0..3] =
+ * {inconsistent, deletions, rounds, error code}. It calls no cudaMalloc,
+ * cudaFree or allocating library routine: all scratch is one static device
+ * array of 9 MiB in the library, held on every GPU that loads it until exit.
+ * Limits: n <= 2048, W <= 2 (128 values), n_bin <= 2048; larger sizes return
+ * CP_E_ARG. All calls on a device share that array (each clears what must
+ * start at zero); calls that overlap on the GPU race. The first call on a
+ * device sets up the array's device address, so make it before any stream
+ * capture. */
+int cp_enforce_ac_static(int n, int W, const int* d_dom_size, uint64_t* d_dom, int n_bin, const int* d_bin_scope,
+                         const uint64_t* d_bin_rows, int64_t* d_status, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
