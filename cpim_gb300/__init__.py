@@ -87,6 +87,7 @@ def lib():
         "cp_engine_destroy": ([vp], i),
         "cp_engine_launches": ([vp], i64),
         "cp_engine_set_tuning": ([vp, i, i, i], i),
+        "cp_engine_set_sac_mode": ([vp, i], i),
         "cp_net_upload": ([vp, i, PI, i, P64, i, PI, P64, i, PI, PI, PI, PI, i, PV], i),
         "cp_net_destroy": ([vp], i),
         "cp_net_device_bytes": ([vp], i64),
@@ -219,6 +220,10 @@ class Engine:
 
     def set_tuning(self, block=0, chunk=0, ctas_per_sm=0):
         _check(lib().cp_engine_set_tuning(self._h, block, chunk, ctas_per_sm))
+
+    def set_sac_mode(self, mode: int):
+        """0: tiled SAC sweep where eligible; 1: general per-branch kernel only."""
+        _check(lib().cp_engine_set_sac_mode(self._h, mode))
 
     def upload(self, inst: Instance, max_levels: int = 0) -> "Net":
         return Net(self, inst, max_levels)

@@ -65,6 +65,7 @@ struct cp_engine {
   int block_grid = 256;
   int chunk = 0;
   int ctas_per_sm = 0;
+  int sac_mode = 0;  // 0: tiled sweep where eligible, 1: general kernel only
 };
 
 struct cp_net {
@@ -94,6 +95,8 @@ struct cp_net {
   void* d_sac_scratch = nullptr;
   size_t sac_stride = 0;
   int sac_grid = 0;
+  int tile_grid = 0;   // persistent CTAs of the tiled sweep (0: not eligible)
+  int slot_cap = 0;    // neighbours per tile held in shared memory
   int grid_blocks = 0;
   bool cta_in_smem = true;
   bool prefer_grid = false;
@@ -287,6 +290,13 @@ int cp_engine_set_tuning(cp_engine* e, int block, int chunk, int ctas_per_sm) {
   }
   e->chunk = chunk;
   e->ctas_per_sm = ctas_per_sm;
+  return CP_OK;
+}
+
+int cp_engine_set_sac_mode(cp_engine* e, int mode) {
+  if (!e) return fail(CP_E_ARG, "null engine");
+  if (mode != 0 && mode != 1) return fail(CP_E_ARG, "SAC mode must be 0 (tiled where eligible) or 1 (general)");
+  e->sac_mode = mode;
   return CP_OK;
 }
 
@@ -499,6 +509,11 @@ int cp_net_upload(cp_engine* e, int n, const int* dom, int W, const uint64_t* in
   CP_TRY(net->alloc(&S.evt, n));
   CP_TRY(net->alloc(&S.nevt, 4));
   CP_TRY(net->alloc(&S.evt_fb, nw));
+  CP_TRY(net->alloc(&S.tiles, static_cast<size_t>(n) * 2 * Wi));
+  CP_TRY(net->alloc(&S.ntiles, 4));
+  CP_TRY(net->alloc(&S.tcursor, 4));
+  CP_TRY(net->alloc(&S.deep, total_values));
+  CP_TRY(net->alloc(&S.ndeep, 4));
   CP_TRY(net->alloc(&net->d_stats, 1));
   CP_TRY(net->alloc(&net->d_evt, n));
   CP_TRY(net->alloc(&net->d_sizes, n));
@@ -528,6 +543,21 @@ int cp_net_upload(cp_engine* e, int n, const int* dom, int W, const uint64_t* in
   }
   net->grid_blocks = ac_grid_max_blocks(D, e->block_grid, e->sm_count);
   if (net->grid_blocks < 1) return fail(CP_E_UNSUPPORTED, "grid fixpoint kernel does not fit");
+  // Tiled SAC sweep (binary networks): shared memory holds the round-one
+  // domains of up to slot_cap neighbours for 32 branches, plus a slot map.
+  if (n_tab == 0) {
+    const size_t budget = std::min<size_t>(e->smem_optin > 4096 ? e->smem_optin - 4096 : 0, 100 * 1024);
+    const size_t per_slot = static_cast<size_t>(32) * Wi * 8;
+    int cap = 0;
+    for (int x = 0; x < n; ++x) cap = std::max(cap, arc_deg[x]);
+    cap = std::max(cap, 1);
+    if (static_cast<size_t>(n) * 4 + per_slot * 8 <= budget) {
+      const size_t fit = (budget - static_cast<size_t>(n) * 4) / per_slot;
+      net->slot_cap = static_cast<int>(std::min<size_t>(static_cast<size_t>(cap), fit));
+      const int per_sm_t = sac_tile_blocks_per_sm(D, net->slot_cap, 256);
+      net->tile_grid = per_sm_t > 0 ? per_sm_t * e->sm_count : 0;
+    }
+  }
   // Large networks run their single-instance fixpoints on the whole grid.
   net->prefer_grid = (2 * static_cast<int64_t>(n_bin) + n_tab) > 8192 || !net->cta_in_smem;
 
@@ -709,12 +739,32 @@ int cp_enforce_sac1(cp_net* net, int level, cp_stats* st) {
     CP_CUDA(cudaMemsetAsync(net->S.cursor, 0, sizeof(int), s));
     CP_CUDA(cudaMemsetAsync(net->S.nevt, 0, sizeof(int), s));
     CP_CUDA(cudaMemsetAsync(net->S.evt_fb, 0, nw * 4, s));
-    CP_CUDA(launch_build_work(net->dn, net->level_ptr(level), net->S, s));
+    const bool tiled = net->tile_grid > 0 && e->sac_mode == 0;
+    SacScratch S = net->S;
+    if (!tiled) S.tiles = nullptr;
+    if (tiled) {
+      CP_CUDA(cudaMemsetAsync(S.ntiles, 0, sizeof(int), s));
+      CP_CUDA(cudaMemsetAsync(S.tcursor, 0, sizeof(int), s));
+      CP_CUDA(cudaMemsetAsync(S.ndeep, 0, sizeof(int), s));
+    }
+    CP_CUDA(launch_build_work(net->dn, net->level_ptr(level), S, s));
     CP_CUDA(cudaEventRecord(e->evk0, s));
-    CP_CUDA(launch_sac_branches(net->dn, net->level_ptr(level), net->S.work, net->S.nwork, net->S.cursor, net->S.ok,
-                                net->d_stats, e->block_sac, net->sac_grid, net->d_sac_scratch, net->sac_stride, s));
+    if (tiled) {
+      // Two-round branches resolved by the tiled kernel, the rest (the deep
+      // list) by the general kernel.
+      CP_CUDA(launch_sac_tile(net->dn, net->level_ptr(level), S, S.ok, net->slot_cap, net->d_stats, 256,
+                              net->tile_grid, s));
+      CP_CUDA(launch_sac_branches(net->dn, net->level_ptr(level), S.work, S.nwork, S.cursor, S.ok, net->d_stats,
+                                  e->block_sac, net->sac_grid, net->d_sac_scratch, net->sac_stride, s, S.deep,
+                                  S.ndeep));
+      launches += 1;
+      e->launches += 1;
+    } else {
+      CP_CUDA(launch_sac_branches(net->dn, net->level_ptr(level), S.work, S.nwork, S.cursor, S.ok, net->d_stats,
+                                  e->block_sac, net->sac_grid, net->d_sac_scratch, net->sac_stride, s));
+    }
     CP_CUDA(cudaEventRecord(e->evk1, s));
-    CP_CUDA(launch_commit(net->dn, net->level_ptr(level), net->S, net->d_stats, s));
+    CP_CUDA(launch_commit(net->dn, net->level_ptr(level), S, net->d_stats, s));
     launches += 3;
     e->launches += 3;
     CP_TRY(stats_fetch(net));

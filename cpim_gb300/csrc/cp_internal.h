@@ -94,6 +94,11 @@ struct SacScratch {
   int* evt;           // variables changed by a commit, up to n
   int* nevt;          // [1]
   u32* evt_fb;        // dedupe bitmap for evt
+  int4* tiles;        // (x, first value, first work index, live mask) per 32 values
+  int* ntiles;        // [1]
+  int* tcursor;       // [1]
+  int* deep;          // work indices the tiled kernel hands to the general one
+  int* ndeep;         // [1]
 };
 
 enum NodeOp { kOpRoot = 0, kOpAssign = 1, kOpRefute = 2, kOpSingleton = 3, kOpEvents = 4 };
@@ -113,11 +118,20 @@ cudaError_t launch_ac_grid(const DevNet& N, u64* level_dom, const int* evt, cons
                            GridScratch G, KStats* st, int block, int grid, cudaStream_t s);
 int ac_grid_max_blocks(const DevNet& N, int block, int sm_count);
 // Persistent batched singleton tests: pairs work[0..*nwork), results in ok.
+// With idx != nullptr the tests are work[idx[i]] for i < *nidx.
 cudaError_t launch_sac_branches(const DevNet& N, const u64* root, const int2* work, const int* nwork, int* cursor,
                                 uint8_t* ok, KStats* st, int block, int grid, void* gscratch, size_t gstride,
-                                cudaStream_t s);
+                                cudaStream_t s, const int* idx = nullptr, const int* nidx = nullptr);
 int sac_blocks_per_sm(const DevNet& N, int block, bool smem_state);
-// Builds the list of live (x, a) pairs of a level (warp ballot + prefix).
+// Tiled singleton tests (binary networks): 32 branches of one variable per
+// tile; branches that need more than two propagation rounds are appended to
+// S.deep for the general kernel. slot_cap: neighbours held in shared memory.
+cudaError_t launch_sac_tile(const DevNet& N, const u64* root, SacScratch S, uint8_t* ok, int slot_cap, KStats* st,
+                            int block, int grid, cudaStream_t s);
+size_t sac_tile_smem(const DevNet& N, int slot_cap);
+int sac_tile_blocks_per_sm(const DevNet& N, int slot_cap, int block);
+// Builds the list of live (x, a) pairs of a level (warp ballot + prefix);
+// when S.tiles is set, also one tile per 32-value slice with live values.
 cudaError_t launch_build_work(const DevNet& N, const u64* dom, SacScratch S, cudaStream_t s);
 // Removes failed pairs from the level, collecting changed variables.
 cudaError_t launch_commit(const DevNet& N, u64* dom, SacScratch S, KStats* st, cudaStream_t s);

@@ -500,7 +500,8 @@ __global__ void __launch_bounds__(512) k_node(DevNet N, u64* levels, int src, in
 // ---------------------------------------------------------------------------
 template <int WT, bool kTab>
 __global__ void __launch_bounds__(256) k_sac(DevNet N, const u64* root, const int2* work, const int* nwork,
-                                             int* cursor, uint8_t* ok, KStats* st, char* gscratch, size_t gstride) {
+                                             int* cursor, uint8_t* ok, KStats* st, char* gscratch, size_t gstride,
+                                             const int* idx) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_qlen[3], s_failed[2], s_failvar, s_err, s_b;
   char* base = gscratch ? gscratch + blockIdx.x * gstride : reinterpret_cast<char*>(smem_raw);
@@ -515,8 +516,9 @@ __global__ void __launch_bounds__(256) k_sac(DevNet N, const u64* root, const in
   for (;;) {
     if (threadIdx.x == 0) s_b = atomicAdd(cursor, 1);
     __syncthreads();
-    const int b = s_b;
-    if (b >= total) break;
+    const int i = s_b;
+    if (i >= total) break;
+    const int b = idx ? idx[i] : i;
     const int2 xa = work[b];
     block_copy(F.D, root, words);
     block_zero(reinterpret_cast<u32*>(base + L.fb0), (L.ts - L.fb0) / 4);
@@ -646,7 +648,7 @@ __global__ void __launch_bounds__(512) k_ac_grid(DevNet N, u64* D, const int* ev
 // Live (x, a) pairs of a level, one warp per variable: ballot of the live
 // flags, lane offsets by prefix popcount, one atomic per 32 values.
 template <int WT>
-__global__ void k_build_work(DevNet N, const u64* dom, int2* work, int* nwork) {
+__global__ void k_build_work(DevNet N, const u64* dom, int2* work, int* nwork, int4* tiles, int* ntiles) {
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -657,10 +659,206 @@ __global__ void k_build_work(DevNet N, const u64* dom, int2* work, int* nwork) {
       const u32 bits = static_cast<u32>(word >> (base & 32));
       if (bits == 0) continue;
       int b0 = 0;
-      if (lane == 0) b0 = atomicAdd(nwork, __popc(bits));
+      if (lane == 0) {
+        b0 = atomicAdd(nwork, __popc(bits));
+        if (tiles) tiles[atomicAdd(ntiles, 1)] = make_int4(x, base, b0, static_cast<int>(bits));
+      }
       b0 = __shfl_sync(kFull, b0, 0);
       if ((bits >> lane) & 1u) work[b0 + __popc(bits & ((1u << lane) - 1u))] = make_int2(x, base + lane);
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_sac_tile: the singleton tests of 32 values of one variable x at once,
+// lane l of every warp standing for branch (x, base + l).
+//
+// On an AC-closed level, the fixpoint of branch (x, a) is reached after two
+// rounds unless round two removes something: round one only shrinks the
+// neighbours y of x to D0(y) & R[x=a -> y]; round two revises every arc
+// (z <- y) out of those neighbours. This kernel computes round one for all 32
+// branches into shared memory, then only tests round two: for each arc it
+// ORs the support rows R[y=c -> z] over c in each lane's D_a(y) (one
+// broadcast load per row serves all 32 branches) and stops as soon as every
+// lane's D(z) is covered. A branch whose round two would remove nothing is
+// consistent; one whose round two empties a domain is not; any other branch
+// (round two removes values) is handed to the general kernel, which computes
+// its fixpoint in full. Arcs back into x need no test: x's single value keeps
+// a support in every non-empty D_a(y) by construction.
+// ---------------------------------------------------------------------------
+template <int WT>
+__device__ __forceinline__ int pop_low(u64& m, int word) {
+  if (!m) return -1;
+  const int b = __ffsll(static_cast<long long>(m)) - 1;
+  m &= m - 1;
+  return word * 64 + b;
+}
+
+template <int WT>
+__global__ void __launch_bounds__(256) k_sac_tile(DevNet N, const u64* root, const int4* tiles, const int* ntiles,
+                                                  int* tcursor, uint8_t* ok, int* deep, int* ndeep, int slot_cap,
+                                                  KStats* st) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  u64* T = reinterpret_cast<u64*>(smem_raw);  // [slot_cap][32][WT]
+  int* slot_of = reinterpret_cast<int*>(smem_raw + static_cast<size_t>(slot_cap) * 32 * WT * 8);  // [n]
+  __shared__ int s_t;
+  __shared__ u32 s_fail, s_deep;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int total = *ntiles;
+  for (int i = threadIdx.x; i < N.n; i += blockDim.x) slot_of[i] = -1;
+  u64 c_rev = 0, c_rows = 0, c_done = 0;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_t = atomicAdd(tcursor, 1);
+      s_fail = 0;
+      s_deep = 0;
+    }
+    __syncthreads();
+    const int t = s_t;
+    if (t >= total) break;
+    const int4 tl = tiles[t];
+    const int x = tl.x, base = tl.y, b0 = tl.z;
+    const u32 live = static_cast<u32>(tl.w);
+    const int a0 = N.arc_start[x], deg = N.arc_start[x + 1] - a0;
+    const bool fits = deg <= slot_cap;
+    if (fits) {
+      // Round one: slots for the distinct neighbours, D_a(y) = D0(y) & rows.
+      for (int i = threadIdx.x; i < deg; i += blockDim.x) atomicCAS(&slot_of[N.arcs[a0 + i].z], -1, i);
+      __syncthreads();
+      for (int k = threadIdx.x; k < deg * 32; k += blockDim.x) {
+        const int i = k >> 5, l = k & 31;
+        const int z = N.arcs[a0 + i].z;
+        if (slot_of[z] == i) {
+#pragma unroll
+          for (int w = 0; w < WT; ++w) T[(static_cast<size_t>(i) * 32 + l) * WT + w] = root[static_cast<size_t>(z) * WT + w];
+        }
+      }
+      __syncthreads();
+      for (int i = warp; i < deg; i += nwarps) {
+        const Arc A = N.arcs[a0 + i];
+        const int s = slot_of[A.z];
+        if ((live >> lane) & 1u) {
+          u64 r[WT];
+          load_row<WT>(N.rel, A.yz + static_cast<size_t>(base + lane) * WT, r);
+#pragma unroll
+          for (int w = 0; w < WT; ++w) atomicAnd(&T[(static_cast<size_t>(s) * 32 + lane) * WT + w], r[w]);
+        }
+      }
+      __syncthreads();
+      for (int k = threadIdx.x; k < deg * 32; k += blockDim.x) {
+        const int i = k >> 5, l = k & 31;
+        if (slot_of[N.arcs[a0 + i].z] != i || !((live >> l) & 1u)) continue;
+        u64 any = 0;
+#pragma unroll
+        for (int w = 0; w < WT; ++w) any |= T[(static_cast<size_t>(i) * 32 + l) * WT + w];
+        if (!any) atomicOr(&s_fail, 1u << l);
+      }
+      __syncthreads();
+      // Round two, tested only.
+      for (int s = warp; s < deg; s += nwarps) {
+        const int y = N.arcs[a0 + s].z;
+        if (slot_of[y] != s) continue;
+        u64 dy[WT];
+#pragma unroll
+        for (int w = 0; w < WT; ++w) dy[w] = T[(static_cast<size_t>(s) * 32 + lane) * WT + w];
+        const int y0 = N.arc_start[y], y1 = N.arc_start[y + 1];
+        for (int j = y0; j < y1; ++j) {
+          // Lanes still open (live, not failed, not handed over), warp-uniform.
+          const u32 done_m = __shfl_sync(kFull, *reinterpret_cast<volatile u32*>(&s_fail) |
+                                                    *reinterpret_cast<volatile u32*>(&s_deep), 0);
+          const u32 open = live & ~done_m;
+          if (!open) break;
+          const Arc A = N.arcs[j];
+          const int z = A.z;
+          if (z == x) continue;
+          const int sz = slot_of[z];
+          u64 cur[WT];
+          if (sz >= 0) {
+#pragma unroll
+            for (int w = 0; w < WT; ++w) cur[w] = T[(static_cast<size_t>(sz) * 32 + lane) * WT + w];
+          } else {
+#pragma unroll
+            for (int w = 0; w < WT; ++w) cur[w] = __ldg(root + static_cast<size_t>(z) * WT + w);
+          }
+          const bool mine = (open >> lane) & 1u;
+          u64 uc[WT], acc[WT];
+#pragma unroll
+          for (int w = 0; w < WT; ++w) {
+            uc[w] = warp_or64(mine ? dy[w] : 0ull);
+            acc[w] = 0;
+          }
+          bool still = mine;
+          bool go = true;
+          int loaded = 0;
+#pragma unroll
+          for (int w = 0; w < WT; ++w) {
+            u64 m = go ? uc[w] : 0ull;
+            while (m) {
+              const int c0 = pop_low<WT>(m, w), c1 = pop_low<WT>(m, w), c2 = pop_low<WT>(m, w), c3 = pop_low<WT>(m, w);
+              u64 r0[WT], r1[WT], r2[WT], r3[WT];
+              load_row<WT>(N.rel, A.yz + static_cast<size_t>(c0) * WT, r0);
+              if (c1 >= 0) load_row<WT>(N.rel, A.yz + static_cast<size_t>(c1) * WT, r1);
+              if (c2 >= 0) load_row<WT>(N.rel, A.yz + static_cast<size_t>(c2) * WT, r2);
+              if (c3 >= 0) load_row<WT>(N.rel, A.yz + static_cast<size_t>(c3) * WT, r3);
+              loaded += 1 + (c1 >= 0) + (c2 >= 0) + (c3 >= 0);
+              const bool h0 = (sel<WT>(dy, c0 >> 6) >> (c0 & 63)) & 1ull;
+              const bool h1 = c1 >= 0 && ((sel<WT>(dy, c1 >> 6) >> (c1 & 63)) & 1ull);
+              const bool h2 = c2 >= 0 && ((sel<WT>(dy, c2 >> 6) >> (c2 & 63)) & 1ull);
+              const bool h3 = c3 >= 0 && ((sel<WT>(dy, c3 >> 6) >> (c3 & 63)) & 1ull);
+              u64 gap = 0;
+#pragma unroll
+              for (int q = 0; q < WT; ++q) {
+                acc[q] |= (h0 ? r0[q] : 0ull) | (h1 ? r1[q] : 0ull) | (h2 ? r2[q] : 0ull) | (h3 ? r3[q] : 0ull);
+                gap |= cur[q] & ~acc[q];
+              }
+              still = still && gap != 0;
+              if (__ballot_sync(kFull, still) == 0) {
+                m = 0;
+                go = false;  // every open lane is covered: no change in round two
+              }
+            }
+          }
+          if (lane == 0) {
+            ++c_rev;
+            c_rows += loaded;
+          }
+          if (still) {
+            u64 left = 0;
+#pragma unroll
+            for (int q = 0; q < WT; ++q) left |= cur[q] & acc[q];
+            atomicOr(left ? &s_deep : &s_fail, 1u << lane);
+          }
+        }
+      }
+      __syncthreads();
+      for (int i = threadIdx.x; i < deg; i += blockDim.x) slot_of[N.arcs[a0 + i].z] = -1;
+    }
+    // Verdicts: warp 0 writes them; handed-over branches go to the deep list.
+    if (warp == 0) {
+      const bool is_live = (live >> lane) & 1u;
+      const u32 failm = *reinterpret_cast<volatile u32*>(&s_fail);
+      const u32 deepm = fits ? *reinterpret_cast<volatile u32*>(&s_deep) : live;
+      const bool f = is_live && ((failm >> lane) & 1u);
+      const bool d = is_live && !f && ((deepm >> lane) & 1u);
+      const int b = b0 + __popc(live & ((1u << lane) - 1u));
+      const u32 dm = __ballot_sync(kFull, d);
+      int db = 0;
+      if (lane == 0 && dm) db = atomicAdd(ndeep, __popc(dm));
+      db = __shfl_sync(kFull, db, 0);
+      if (d) deep[db + __popc(dm & ((1u << lane) - 1u))] = b;
+      if (is_live && !d) ok[b] = f ? 0 : 1;
+      if (lane == 0) c_done += __popc(live & ~dm);
+    }
+    __syncthreads();
+  }
+  Cnt cn;
+  cn.rev = c_rev;
+  cn.rows = c_rows;
+  flush_counts(st, cn);
+  if (threadIdx.x == 0 && c_done) {
+    atomicAdd(&st->fixpoints, c_done);
+    atomicAdd(&st->branches, c_done);
+    atomicMax(&st->rounds_max, 2);
   }
 }
 
@@ -823,14 +1021,45 @@ int sac_blocks_per_sm(const DevNet& N, int block, bool smem_state) {
 
 cudaError_t launch_sac_branches(const DevNet& N, const u64* root, const int2* work, const int* nwork, int* cursor,
                                 uint8_t* ok, KStats* st, int block, int grid, void* gscratch, size_t gstride,
-                                cudaStream_t s) {
+                                cudaStream_t s, const int* idx, const int* nidx) {
   const size_t smem = gscratch ? 0 : cta_state_bytes(N);
+  const int* count = idx ? nidx : nwork;
   return dispatch_wt(N, [&](auto wt, auto tab) -> cudaError_t {
     constexpr int WT = decltype(wt)::value;
     constexpr bool TB = decltype(tab)::value;
     cudaError_t e = allow_smem(k_sac<WT, TB>, smem);
     if (e != cudaSuccess) return e;
-    k_sac<WT, TB><<<grid, block, smem, s>>>(N, root, work, nwork, cursor, ok, st, static_cast<char*>(gscratch), gstride);
+    k_sac<WT, TB><<<grid, block, smem, s>>>(N, root, work, count, cursor, ok, st, static_cast<char*>(gscratch),
+                                            gstride, idx);
+    return cudaGetLastError();
+  });
+}
+
+size_t sac_tile_smem(const DevNet& N, int slot_cap) {
+  return static_cast<size_t>(slot_cap) * 32 * N.W * 8 + static_cast<size_t>(N.n) * 4;
+}
+
+int sac_tile_blocks_per_sm(const DevNet& N, int slot_cap, int block) {
+  const size_t smem = sac_tile_smem(N, slot_cap);
+  int per_sm = 0;
+  cudaError_t e = dispatch_w(N.W, [&](auto wt) -> cudaError_t {
+    constexpr int WT = decltype(wt)::value;
+    cudaError_t e2 = allow_smem(k_sac_tile<WT>, smem);
+    if (e2 != cudaSuccess) return e2;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sac_tile<WT>, block, smem);
+  });
+  return e == cudaSuccess ? per_sm : 0;
+}
+
+cudaError_t launch_sac_tile(const DevNet& N, const u64* root, SacScratch S, uint8_t* ok, int slot_cap, KStats* st,
+                            int block, int grid, cudaStream_t s) {
+  const size_t smem = sac_tile_smem(N, slot_cap);
+  return dispatch_w(N.W, [&](auto wt) -> cudaError_t {
+    constexpr int WT = decltype(wt)::value;
+    cudaError_t e = allow_smem(k_sac_tile<WT>, smem);
+    if (e != cudaSuccess) return e;
+    k_sac_tile<WT><<<grid, block, smem, s>>>(N, root, S.tiles, S.ntiles, S.tcursor, ok, S.deep, S.ndeep, slot_cap,
+                                             st);
     return cudaGetLastError();
   });
 }
@@ -839,7 +1068,7 @@ cudaError_t launch_build_work(const DevNet& N, const u64* dom, SacScratch S, cud
   return dispatch_w(N.W, [&](auto wt) -> cudaError_t {
     constexpr int WT = decltype(wt)::value;
     const int blocks = std::max(1, std::min(4096, (N.n * 32 + 255) / 256));
-    k_build_work<WT><<<blocks, 256, 0, s>>>(N, dom, S.work, S.nwork);
+    k_build_work<WT><<<blocks, 256, 0, s>>>(N, dom, S.work, S.nwork, S.tiles, S.ntiles);
     return cudaGetLastError();
   });
 }

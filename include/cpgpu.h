@@ -74,6 +74,10 @@ int64_t cp_engine_launches(const cp_engine* e);
  * block: threads per CTA; chunk: incidences per work item; ctas_per_sm:
  * resident CTAs per SM for the batched kernels. */
 int cp_engine_set_tuning(cp_engine* e, int block, int chunk, int ctas_per_sm);
+/* SAC sweep kernel: 0 = tiled (32 branches of one variable per tile, two-round
+ * test, deeper branches re-run by the general kernel) wherever the network is
+ * binary and fits, 1 = general per-branch kernel only. Results are identical. */
+int cp_engine_set_sac_mode(cp_engine* e, int mode);
 
 /* ---- networks ------------------------------------------------------------ */
 /* Uploads a network; replaces GModelAdapter::Build

@@ -90,6 +90,31 @@ def test_sac_mixed_matches_oracle(engine, args):
         net.close()
 
 
+@pytest.mark.parametrize("args", [(30, 8, 120, 0.35, 0.35, 0.1, 1), (30, 8, 120, 0.35, 0.35, 0.1, 4),
+                                  (30, 8, 120, 0.45, 0.45, 0.1, 3), (40, 100, 160, 0.8, 0.8, 0.2, 3),
+                                  (24, 256, 60, 0.9, 0.9, 0.3, 3), (60, 64, 600, 0.55, 0.55, 0.1, 5),
+                                  (100, 128, 1000, 0.4, 0.4, 0.0, 7), (150, 16, 3000, 0.3, 0.3, 0.05, 2)])
+def test_sac_tiled_equals_general(args):
+    # The tiled sweep (two-round test, deeper branches handed to the general
+    # kernel) and the general per-branch kernel give the same SAC closure,
+    # which is the oracle's.
+    inst = cp.gen_binary(*args)
+    ok_o, d_o, dels_o = O.sac1(oracle_view_of(inst))
+    out = []
+    for mode in (0, 1):
+        with cp.Engine(0) as eng:
+            eng.set_sac_mode(mode)
+            net = eng.upload(inst)
+            st = net.enforce_sac1(0)
+            out.append((bool(st.inconsistent), net.dom_get(0), st.deletions, st.branches))
+            net.close()
+    for inc, d, dels, _ in out:
+        assert inc == (not ok_o)
+        if ok_o:
+            assert np.array_equal(d, d_o)
+            assert dels == dels_o
+
+
 def test_singletons_batched_plain_oracle(engine):
     inst = cp.gen_binary(100, 128, 1000, 0.4, 0.4, 0.0, 7)
     ov = oracle_view_of(inst)
