@@ -17,7 +17,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libcpgpu.so")
 
-__all__ = ["ACAlgorithm", "VarHeuristic", "ValHeuristic", "Engine", "Net", "Instance", "Stats",
+__all__ = ["ACAlgorithm", "VarHeuristic", "ValHeuristic", "Engine", "Net", "Batch", "Instance", "Stats",
            "SearchResult", "CPError", "gen_binary", "gen_mixed", "gen_uneven", "lib"]
 
 
@@ -110,6 +110,13 @@ def lib():
         "cp_gen_sizes": ([vp, C.POINTER(C.c_int64)], i),
         "cp_gen_export": ([vp, PI, P64, PI, P64, PI, PI, PI, PI], i),
         "cp_net_upload_instance": ([vp, vp, i, PV], i),
+        "cp_batch_create": ([vp, i, PV, i, PV], i),
+        "cp_batch_destroy": ([vp], i),
+        "cp_batch_ac": ([vp, C.POINTER(Stats), PU8], i),
+        "cp_batch_sac1": ([vp, C.POINTER(Stats), PU8], i),
+        "cp_batch_set_graphs": ([vp, i], i),
+        "cp_batch_tune": ([vp], i),
+        "cp_batch_info": ([vp, i, PI], i),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -325,3 +332,49 @@ class Net:
         return {"status": res.status, "num_positive": res.num_positive, "num_negative": res.num_negative,
                 "propagations": res.propagations, "solve_ms": res.solve_ms,
                 "solution": sol.tolist() if res.status == 1 else []}
+
+
+class Batch:
+    """Many independent networks propagated together (cp_batch_*)."""
+
+    def __init__(self, engine: Engine, nets, level: int = 0):
+        self.engine = engine
+        self.nets = list(nets)
+        arr = (C.c_void_p * len(self.nets))(*[n._h.value for n in self.nets])
+        self._h = C.c_void_p()
+        _check(lib().cp_batch_create(engine._h, len(self.nets), arr, level, C.byref(self._h)))
+
+    def close(self):
+        if self._h:
+            lib().cp_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def ac(self):
+        st = Stats()
+        inc = np.zeros(len(self.nets), np.uint8)
+        _check(lib().cp_batch_ac(self._h, C.byref(st), _p(inc, C.c_uint8)))
+        return st, inc
+
+    def sac1(self):
+        st = Stats()
+        inc = np.zeros(len(self.nets), np.uint8)
+        _check(lib().cp_batch_sac1(self._h, C.byref(st), _p(inc, C.c_uint8)))
+        return st, inc
+
+    def set_graphs(self, on: bool):
+        _check(lib().cp_batch_set_graphs(self._h, 1 if on else 0))
+
+    def tune(self):
+        _check(lib().cp_batch_tune(self._h))
+
+    def info(self, group: int = 0):
+        out = np.zeros(8, np.int32)
+        _check(lib().cp_batch_info(self._h, group, _p(out, C.c_int)))
+        keys = ["groups", "W", "tables", "members", "tiled", "cta_threads", "slot_cap", "cta_in_smem"]
+        return dict(zip(keys, out.tolist()))

@@ -2,9 +2,12 @@
 // upload, the device level stack, AC / SAC orchestration, and the MAC and
 // GModelSolver search loops that keep the reference's host control flow while
 // every domain operation and propagation runs on the device.
+#include <sys/stat.h>
+
 #include <algorithm>
 #include <chrono>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -1226,6 +1229,499 @@ int cp_net_upload_instance(cp_engine* e, const cp_instance* inst, int max_levels
   }
   return cp_net_upload(e, I.n, I.dom.data(), I.W, I.init.data(), I.n_bin(), scope.data(), I.brows.data(), I.n_tab(),
                        I.tarity.data(), I.tscope.data(), I.tntup.data(), I.ttup.data(), max_levels, out);
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Multi-instance batches
+// ===========================================================================
+namespace {
+
+struct BatchGroup {
+  int W = 1;
+  bool tables = false;
+  std::vector<int> members;  // indices into cp_batch::nets
+  BatchDev B;
+  int max_n = 0;
+  int slot_cap = 0;
+  bool tiled = false;
+  int tile_grid = 0;
+  size_t cta_bytes = 0;
+  bool cta_smem = true;
+  void* gscratch = nullptr;
+  size_t gstride = 0;
+  int node_grid = 0;
+  int sac_grid = 0;
+  int sac_block = 256;
+  int64_t total_values = 0;
+  cudaGraphExec_t exec = nullptr;
+  std::string key;  // autotuner cache key
+};
+
+std::string tune_cache_path() {
+  const char* p = std::getenv("CPGPU_TUNE_CACHE");
+  if (p && *p) return p;
+  const char* h = std::getenv("HOME");
+  return std::string(h && *h ? h : "/tmp") + "/.cache/cpgpu_tune.txt";
+}
+
+// Cache lines: "<key> <tiled> <sac_block>".
+bool tune_lookup(const std::string& key, bool& tiled, int& block) {
+  FILE* f = std::fopen(tune_cache_path().c_str(), "r");
+  if (!f) return false;
+  char k[256];
+  int t = 0, b = 0;
+  bool found = false;
+  while (std::fscanf(f, "%255s %d %d", k, &t, &b) == 3)
+    if (key == k) {
+      tiled = t != 0;
+      block = b;
+      found = true;
+    }
+  std::fclose(f);
+  return found;
+}
+
+void tune_store(const std::string& key, bool tiled, int block) {
+  const std::string path = tune_cache_path();
+  const size_t slash = path.rfind('/');
+  if (slash != std::string::npos) {
+    const std::string dir = path.substr(0, slash);
+    for (size_t i = 1; i <= dir.size(); ++i)
+      if (i == dir.size() || dir[i] == '/') {
+        const std::string sub = dir.substr(0, i);
+        if (!sub.empty()) mkdir(sub.c_str(), 0755);
+      }
+  }
+  FILE* f = std::fopen(path.c_str(), "a");
+  if (!f) return;
+  std::fprintf(f, "%s %d %d\n", key.c_str(), tiled ? 1 : 0, block);
+  std::fclose(f);
+}
+
+}  // namespace
+
+struct cp_batch {
+  cp_engine* e = nullptr;
+  int k = 0;
+  int level = 0;
+  std::vector<cp_net*> nets;
+  std::vector<BatchGroup> groups;
+  std::vector<void*> allocs;
+  KStats* d_stats = nullptr;
+  KStats* h_stats = nullptr;
+  int* h_int = nullptr;
+  bool use_graph = true;
+  ~cp_batch() {
+    for (auto& g : groups)
+      if (g.exec) cudaGraphExecDestroy(g.exec);
+    for (void* p : allocs) cudaFree(p);
+    if (h_stats) cudaFreeHost(h_stats);
+    if (h_int) cudaFreeHost(h_int);
+  }
+  template <typename T>
+  int alloc(T** p, size_t count) {
+    void* raw = nullptr;
+    cudaError_t err = cudaMalloc(&raw, std::max<size_t>(count * sizeof(T), 16));
+    if (err != cudaSuccess) {
+      cudaGetLastError();
+      return fail(err == cudaErrorMemoryAllocation ? CP_E_OOM : CP_E_CUDA,
+                  std::string("batch cudaMalloc: ") + cudaGetErrorString(err));
+    }
+    allocs.push_back(raw);
+    *p = static_cast<T*>(raw);
+    return CP_OK;
+  }
+};
+
+namespace {
+
+int batch_group_setup(cp_batch* b, BatchGroup& g) {
+  cp_engine* e = b->e;
+  cudaStream_t s = e->stream;
+  const int kg = static_cast<int>(g.members.size());
+  std::vector<DevNet> nets(kg);
+  std::vector<u64*> roots(kg);
+  std::vector<int> var_base(kg + 1, 0);
+  int max_deg = 1;
+  g.cta_bytes = 0;
+  g.total_values = 0;
+  for (int i = 0; i < kg; ++i) {
+    cp_net* n = b->nets[g.members[i]];
+    nets[i] = n->dn;
+    roots[i] = n->level_ptr(b->level);
+    var_base[i + 1] = var_base[i] + n->n;
+    g.max_n = std::max(g.max_n, n->n);
+    g.cta_bytes = std::max(g.cta_bytes, cta_state_bytes(n->dn));
+    g.total_values += n->dn.total_values;
+    std::vector<int> deg(n->n + 1);
+    CP_CUDA(cudaMemcpy(deg.data(), n->dn.arc_start, (n->n + 1) * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int x = 0; x < n->n; ++x) max_deg = std::max(max_deg, deg[x + 1] - deg[x]);
+  }
+  const int tv = var_base[kg];
+  std::vector<int> var_inst(tv);
+  for (int i = 0; i < kg; ++i)
+    for (int x = var_base[i]; x < var_base[i + 1]; ++x) var_inst[x] = i;
+  BatchDev& B = g.B;
+  B.k = kg;
+  B.total_vars = tv;
+  DevNet* d_nets;
+  u64** d_roots;
+  int *d_vb, *d_vi;
+  CP_TRY(b->alloc(&d_nets, kg));
+  CP_TRY(b->alloc(&d_roots, kg));
+  CP_TRY(b->alloc(&d_vb, kg + 1));
+  CP_TRY(b->alloc(&d_vi, tv));
+  CP_CUDA(cudaMemcpyAsync(d_nets, nets.data(), kg * sizeof(DevNet), cudaMemcpyHostToDevice, s));
+  CP_CUDA(cudaMemcpyAsync(d_roots, roots.data(), kg * sizeof(u64*), cudaMemcpyHostToDevice, s));
+  CP_CUDA(cudaMemcpyAsync(d_vb, var_base.data(), (kg + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
+  CP_CUDA(cudaMemcpyAsync(d_vi, var_inst.data(), tv * sizeof(int), cudaMemcpyHostToDevice, s));
+  B.nets = d_nets;
+  B.roots = d_roots;
+  B.var_base = d_vb;
+  B.var_inst = d_vi;
+  CP_TRY(b->alloc(&B.inc, kg));
+  CP_TRY(b->alloc(&B.act, kg));
+  CP_TRY(b->alloc(&B.removed, kg));
+  CP_TRY(b->alloc(&B.evt, tv));
+  CP_TRY(b->alloc(&B.nevt, kg));
+  CP_TRY(b->alloc(&B.evt_fb, (tv + 31) / 32));
+  CP_TRY(b->alloc(&B.act_list, kg));
+  CP_TRY(b->alloc(&B.nact, 4));
+  CP_TRY(b->alloc(&B.work, g.total_values));
+  CP_TRY(b->alloc(&B.nwork, 4));
+  CP_TRY(b->alloc(&B.ok, g.total_values));
+  CP_TRY(b->alloc(&B.cursor, 4));
+  CP_TRY(b->alloc(&B.tiles, static_cast<size_t>(tv) * 2 * g.W));
+  CP_TRY(b->alloc(&B.ntiles, 4));
+  CP_TRY(b->alloc(&B.tcursor, 4));
+  CP_TRY(b->alloc(&B.deep, g.total_values));
+  CP_TRY(b->alloc(&B.ndeep, 4));
+  // CTA-local state: shared memory when it fits.
+  g.cta_smem = g.cta_bytes + 2048 <= e->smem_optin;
+  const size_t smem = g.cta_smem ? g.cta_bytes : 0;
+  int per_sm_node = batch_node_blocks_per_sm(g.W, g.tables, e->block_node, smem);
+  int per_sm_sac = batch_sac_blocks_per_sm(g.W, g.tables, g.sac_block, smem);
+  if (per_sm_node < 1 || per_sm_sac < 1) return fail(CP_E_UNSUPPORTED, "batch kernels do not fit on an SM");
+  if (e->ctas_per_sm > 0) per_sm_sac = std::min(per_sm_sac, e->ctas_per_sm);
+  g.node_grid = std::min(per_sm_node * e->sm_count, std::max(1, kg));
+  g.sac_grid = per_sm_sac * e->sm_count;
+  if (!g.cta_smem) {
+    g.gstride = (g.cta_bytes + 255) & ~size_t(255);
+    char* p;
+    CP_TRY(b->alloc(&p, g.gstride * static_cast<size_t>(std::max(g.node_grid, g.sac_grid))));
+    g.gscratch = p;
+  }
+  // Tiled sweep where the network kind allows it.
+  g.tiled = false;
+  g.tile_grid = 0;
+  if (!g.tables && g.max_n < 65536) {
+    const size_t budget = std::min<size_t>(e->smem_optin > 4096 ? e->smem_optin - 4096 : 0, 100 * 1024);
+    const size_t per_slot = static_cast<size_t>(32) * g.W * 8;
+    if (static_cast<size_t>(g.max_n) * 4 + per_slot * 8 <= budget) {
+      g.slot_cap = static_cast<int>(std::min<size_t>(max_deg, (budget - static_cast<size_t>(g.max_n) * 4) / per_slot));
+      const int per_sm_t = batch_tile_blocks_per_sm(g.W, g.slot_cap, g.max_n);
+      if (per_sm_t > 0) {
+        g.tile_grid = per_sm_t * e->sm_count;
+        g.tiled = true;
+      }
+    }
+  }
+  // Autotuner cache: shape bucket of the group.
+  int maxd = 0;
+  for (int m : g.members)
+    for (int d : b->nets[m]->dom) maxd = std::max(maxd, d);
+  char key[160];
+  std::snprintf(key, sizeof key, "W%d_tab%d_n%d_deg%d_d%d_k%d", g.W, g.tables ? 1 : 0, 1 << (32 - __builtin_clz(std::max(1, g.max_n))),
+                1 << (32 - __builtin_clz(std::max(1, max_deg))), maxd, 1 << (32 - __builtin_clz(std::max(1, kg))));
+  g.key = key;
+  bool t_tiled = g.tiled;
+  int t_block = g.sac_block;
+  if (tune_lookup(g.key, t_tiled, t_block)) {
+    g.tiled = g.tiled && t_tiled;
+    if (t_block == 128 || t_block == 256) g.sac_block = t_block;
+  }
+  CP_CUDA(cudaStreamSynchronize(s));
+  return CP_OK;
+}
+
+// One sweep of a group: reset counters, build pairs/tiles, test, commit,
+// select the instances with removals, propagate their removals.
+int batch_sweep_launches(cp_batch* b, BatchGroup& g, bool with_commit) {
+  cp_engine* e = b->e;
+  cudaStream_t s = e->stream;
+  BatchDev& B = g.B;
+  const int kg = B.k;
+  CP_CUDA(cudaMemsetAsync(B.nwork, 0, sizeof(int), s));
+  CP_CUDA(cudaMemsetAsync(B.cursor, 0, sizeof(int), s));
+  CP_CUDA(cudaMemsetAsync(B.ntiles, 0, sizeof(int), s));
+  CP_CUDA(cudaMemsetAsync(B.tcursor, 0, sizeof(int), s));
+  CP_CUDA(cudaMemsetAsync(B.ndeep, 0, sizeof(int), s));
+  CP_CUDA(cudaMemsetAsync(B.removed, 0, kg * sizeof(int), s));
+  CP_CUDA(cudaMemsetAsync(B.nevt, 0, kg * sizeof(int), s));
+  CP_CUDA(cudaMemsetAsync(B.evt_fb, 0, ((B.total_vars + 31) / 32) * sizeof(u32), s));
+  const size_t smem = g.cta_smem ? g.cta_bytes : 0;
+  CP_CUDA(launch_batch_build(g.W, B, g.tiled, s));
+  if (g.tiled) {
+    CP_CUDA(launch_batch_tile(g.W, B, g.slot_cap, g.max_n, b->d_stats, g.tile_grid, s));
+    CP_CUDA(launch_batch_sac(g.W, g.tables, B, true, b->d_stats, g.sac_block, g.sac_grid, smem, g.gscratch, g.gstride, s));
+  } else {
+    CP_CUDA(launch_batch_sac(g.W, g.tables, B, false, b->d_stats, g.sac_block, g.sac_grid, smem, g.gscratch, g.gstride, s));
+  }
+  e->launches += g.tiled ? 3 : 2;
+  if (with_commit) {
+    CP_CUDA(launch_batch_commit(g.W, B, b->d_stats, s));
+    CP_CUDA(cudaMemsetAsync(B.nact, 0, sizeof(int), s));
+    CP_CUDA(launch_batch_select(B, false, s));
+    CP_CUDA(launch_batch_node(g.W, g.tables, B, kOpEvents, b->d_stats, e->block_node, g.node_grid, smem, g.gscratch,
+                              g.gstride, s));
+    e->launches += 3;
+  }
+  return CP_OK;
+}
+
+int batch_root(cp_batch* b, BatchGroup& g) {
+  cp_engine* e = b->e;
+  cudaStream_t s = e->stream;
+  BatchDev& B = g.B;
+  const size_t smem = g.cta_smem ? g.cta_bytes : 0;
+  CP_CUDA(cudaMemsetAsync(B.inc, 0, B.k, s));
+  CP_CUDA(cudaMemsetAsync(B.removed, 0, B.k * sizeof(int), s));
+  CP_CUDA(cudaMemsetAsync(B.nact, 0, sizeof(int), s));
+  CP_CUDA(launch_batch_select(B, true, s));
+  CP_CUDA(launch_batch_node(g.W, g.tables, B, kOpRoot, b->d_stats, e->block_node, g.node_grid, smem, g.gscratch,
+                            g.gstride, s));
+  CP_CUDA(cudaMemsetAsync(B.nact, 0, sizeof(int), s));
+  CP_CUDA(launch_batch_select(B, true, s));
+  e->launches += 3;
+  return CP_OK;
+}
+
+int batch_stats_begin(cp_batch* b) {
+  KStats z{};
+  z.fail_var = -1;
+  *b->h_stats = z;
+  CP_CUDA(cudaMemcpyAsync(b->d_stats, b->h_stats, sizeof(KStats), cudaMemcpyHostToDevice, b->e->stream));
+  return CP_OK;
+}
+
+int batch_read_int(cp_batch* b, const int* d) {
+  CP_CUDA(cudaMemcpyAsync(b->h_int, d, sizeof(int), cudaMemcpyDeviceToHost, b->e->stream));
+  CP_CUDA(cudaStreamSynchronize(b->e->stream));
+  return CP_OK;
+}
+
+int batch_finish(cp_batch* b, cp_stats* st, uint8_t* inconsistent, int sweeps, int launches) {
+  cp_engine* e = b->e;
+  CP_CUDA(cudaEventRecord(e->ev1, e->stream));
+  CP_CUDA(cudaMemcpyAsync(b->h_stats, b->d_stats, sizeof(KStats), cudaMemcpyDeviceToHost, e->stream));
+  CP_CUDA(cudaStreamSynchronize(e->stream));
+  if (b->h_stats->error) return fail(b->h_stats->error, "device-side check failed in a batch");
+  if (inconsistent) {
+    for (auto& g : b->groups) {
+      std::vector<uint8_t> inc(g.B.k);
+      CP_CUDA(cudaMemcpy(inc.data(), g.B.inc, g.B.k, cudaMemcpyDeviceToHost));
+      for (int i = 0; i < g.B.k; ++i) inconsistent[g.members[i]] = inc[i];
+    }
+  }
+  if (st) {
+    const KStats& k = *b->h_stats;
+    cp_stats s{};
+    s.revisions = static_cast<int64_t>(k.revisions);
+    s.rows = static_cast<int64_t>(k.rows + k.tuples);
+    s.fixpoints = static_cast<int64_t>(k.fixpoints);
+    s.branches = static_cast<int64_t>(k.branches);
+    s.deletions = static_cast<int64_t>(k.removed);
+    s.rounds = k.rounds_max;
+    s.sweeps = sweeps;
+    s.launches = launches;
+    s.device_ms = elapsed_ms(e);
+    int ninc = 0;
+    for (auto& g : b->groups) {
+      std::vector<uint8_t> inc(g.B.k);
+      CP_CUDA(cudaMemcpy(inc.data(), g.B.inc, g.B.k, cudaMemcpyDeviceToHost));
+      for (uint8_t v : inc) ninc += v;
+    }
+    s.inconsistent = ninc;
+    *st = s;
+  }
+  return CP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cp_batch_create(cp_engine* e, int k, cp_net* const* nets, int level, cp_batch** out) {
+  if (!e || !out || k < 1 || !nets) return fail(CP_E_ARG, "bad batch arguments");
+  if (k >= 32768) return fail(CP_E_UNSUPPORTED, "at most 32767 instances per batch");
+  auto b = std::make_unique<cp_batch>();
+  b->e = e;
+  b->k = k;
+  b->level = level;
+  b->nets.assign(nets, nets + k);
+  for (int i = 0; i < k; ++i) {
+    if (!nets[i] || nets[i]->e != e) return fail(CP_E_ARG, "batch member not uploaded on this engine");
+    if (nets[i]->n >= 65536) return fail(CP_E_UNSUPPORTED, "batch members need n < 65536");
+    if (level < 0 || level >= nets[i]->levels) return fail(CP_E_ARG, "level out of range for a batch member");
+  }
+  for (int i = 0; i < k; ++i) {
+    const int W = nets[i]->W;
+    const bool tab = nets[i]->nt > 0;
+    BatchGroup* g = nullptr;
+    for (auto& gg : b->groups)
+      if (gg.W == W && gg.tables == tab) g = &gg;
+    if (!g) {
+      b->groups.emplace_back();
+      g = &b->groups.back();
+      g->W = W;
+      g->tables = tab;
+    }
+    g->members.push_back(i);
+  }
+  CP_CUDA(cudaMallocHost(reinterpret_cast<void**>(&b->h_stats), sizeof(KStats)));
+  CP_CUDA(cudaMallocHost(reinterpret_cast<void**>(&b->h_int), 4 * sizeof(int)));
+  CP_TRY(b->alloc(&b->d_stats, 1));
+  for (auto& g : b->groups) CP_TRY(batch_group_setup(b.get(), g));
+  ++e->live_nets;
+  *out = b.release();
+  return CP_OK;
+}
+
+int cp_batch_destroy(cp_batch* b) {
+  if (!b) return CP_OK;
+  cp_engine* e = b->e;
+  cudaStreamSynchronize(e->stream);
+  delete b;
+  --e->live_nets;  // a batch holds the engine like a network does
+  if (e->closed && e->live_nets == 0) engine_free(e);
+  return CP_OK;
+}
+
+int cp_batch_set_graphs(cp_batch* b, int use_graphs) {
+  if (!b) return fail(CP_E_ARG, "null batch");
+  b->use_graph = use_graphs != 0;
+  return CP_OK;
+}
+
+int cp_batch_ac(cp_batch* b, cp_stats* st, uint8_t* inconsistent) {
+  if (!b) return fail(CP_E_ARG, "null batch");
+  cp_engine* e = b->e;
+  CP_TRY(batch_stats_begin(b));
+  CP_CUDA(cudaEventRecord(e->ev0, e->stream));
+  int launches = 0;
+  for (auto& g : b->groups) {
+    CP_TRY(batch_root(b, g));
+    launches += 3;
+  }
+  return batch_finish(b, st, inconsistent, 0, launches);
+}
+
+int cp_batch_sac1(cp_batch* b, cp_stats* st, uint8_t* inconsistent) {
+  if (!b) return fail(CP_E_ARG, "null batch");
+  cp_engine* e = b->e;
+  cudaStream_t s = e->stream;
+  CP_TRY(batch_stats_begin(b));
+  CP_CUDA(cudaEventRecord(e->ev0, s));
+  int launches = 0, max_sweeps = 0;
+  for (auto& g : b->groups) {
+    CP_TRY(batch_root(b, g));
+    launches += 3;
+    if (b->use_graph && !g.exec) {
+      // Capture one sweep of this group; it is replayed until no instance
+      // changes (the grids are persistent, all counts are read on device).
+      cudaGraph_t graph;
+      CP_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      const int64_t l0 = e->launches;
+      int rc = batch_sweep_launches(b, g, true);
+      e->launches = l0;
+      cudaError_t ce = cudaStreamEndCapture(s, &graph);
+      if (rc != CP_OK) return rc;
+      CP_CUDA(ce);
+      CP_CUDA(cudaGraphInstantiate(&g.exec, graph, 0));
+      cudaGraphDestroy(graph);
+    }
+    int sweeps = 0;
+    for (;;) {
+      ++sweeps;
+      if (b->use_graph) {
+        CP_CUDA(cudaGraphLaunch(g.exec, s));
+        e->launches += g.tiled ? 6 : 5;
+      } else {
+        CP_TRY(batch_sweep_launches(b, g, true));
+      }
+      launches += g.tiled ? 6 : 5;
+      CP_TRY(batch_read_int(b, g.B.nact));
+      if (*b->h_int == 0) break;
+    }
+    max_sweeps = std::max(max_sweeps, sweeps);
+  }
+  return batch_finish(b, st, inconsistent, max_sweeps, launches);
+}
+
+// Times one sweep (without committing) of each group with the tiled and the
+// general kernel and with 128- and 256-thread general CTAs, keeps the fastest
+// and records it in the tuning cache ($CPGPU_TUNE_CACHE, default
+// ~/.cache/cpgpu_tune.txt) under the group's shape key.
+int cp_batch_tune(cp_batch* b) {
+  if (!b) return fail(CP_E_ARG, "null batch");
+  cp_engine* e = b->e;
+  cudaStream_t s = e->stream;
+  for (auto& g : b->groups) {
+    CP_TRY(batch_stats_begin(b));
+    CP_TRY(batch_root(b, g));
+    const bool can_tile = g.tile_grid > 0;
+    struct Cand {
+      bool tiled;
+      int block;
+    };
+    std::vector<Cand> cands = {{false, 256}, {false, 128}};
+    if (can_tile) cands.insert(cands.begin(), Cand{true, 256});
+    float best = 1e30f;
+    Cand pick = cands[0];
+    for (const Cand& c : cands) {
+      g.tiled = c.tiled;
+      g.sac_block = c.block;
+      float ms_best = 1e30f;
+      for (int rep = 0; rep < 2; ++rep) {
+        CP_CUDA(cudaEventRecord(e->ev0, s));
+        CP_TRY(batch_sweep_launches(b, g, false));
+        CP_CUDA(cudaEventRecord(e->ev1, s));
+        CP_CUDA(cudaEventSynchronize(e->ev1));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e->ev0, e->ev1);
+        ms_best = std::min(ms_best, ms);
+      }
+      if (ms_best < best) {
+        best = ms_best;
+        pick = c;
+      }
+    }
+    g.tiled = pick.tiled;
+    g.sac_block = pick.block;
+    if (g.exec) {
+      cudaGraphExecDestroy(g.exec);
+      g.exec = nullptr;
+    }
+    tune_store(g.key, g.tiled, g.sac_block);
+  }
+  return CP_OK;
+}
+
+int cp_batch_info(const cp_batch* b, int group, int* info) {
+  if (!b || !info || group < 0 || group >= static_cast<int>(b->groups.size()))
+    return fail(CP_E_ARG, "bad batch info arguments");
+  const BatchGroup& g = b->groups[group];
+  info[0] = static_cast<int>(b->groups.size());
+  info[1] = g.W;
+  info[2] = g.tables ? 1 : 0;
+  info[3] = static_cast<int>(g.members.size());
+  info[4] = g.tiled ? 1 : 0;
+  info[5] = g.sac_block;
+  info[6] = g.slot_cap;
+  info[7] = g.cta_smem ? 1 : 0;
+  return CP_OK;
 }
 
 }  // extern "C"

@@ -103,6 +103,49 @@ struct SacScratch {
 
 enum NodeOp { kOpRoot = 0, kOpAssign = 1, kOpRefute = 2, kOpSingleton = 3, kOpEvents = 4 };
 
+// A multi-instance batch: networks of one internal domain width, processed
+// together by one launch per phase. Work pairs and tiles carry the instance in
+// the high 16 bits of their variable field (instance < 32768, n < 65536).
+struct BatchDev {
+  int k = 0;                     // instances
+  int total_vars = 0;            // sum of n over instances
+  const DevNet* nets = nullptr;  // [k]
+  u64* const* roots = nullptr;   // [k] level each instance works on
+  const int* var_base = nullptr; // [k+1] global id of each instance's variable 0
+  const int* var_inst = nullptr; // [total_vars] instance of each global variable
+  uint8_t* inc = nullptr;        // [k] 1 once known inconsistent
+  uint8_t* act = nullptr;        // [k] takes part in the current sweep
+  int* removed = nullptr;        // [k] values removed by the last commit
+  int* evt = nullptr;            // [total_vars] changed variables, instance i at var_base[i]
+  int* nevt = nullptr;           // [k]
+  u32* evt_fb = nullptr;         // bitmap over global variables
+  int* act_list = nullptr;       // [k] instances for the node kernel
+  int* nact = nullptr;           // [1]
+  int2* work = nullptr;          // {inst << 16 | x, a}
+  int* nwork = nullptr;
+  uint8_t* ok = nullptr;
+  int* cursor = nullptr;
+  int4* tiles = nullptr;         // {inst << 16 | x, first value, first work index, live mask}
+  int* ntiles = nullptr;
+  int* tcursor = nullptr;
+  int* deep = nullptr;
+  int* ndeep = nullptr;
+};
+
+// Batch launch wrappers (cp_kernels.cu). W / tables select the template.
+cudaError_t launch_batch_node(int W, bool tables, const BatchDev& B, int op, KStats* st, int block, int grid,
+                              size_t smem, void* gscratch, size_t gstride, cudaStream_t s);
+int batch_node_blocks_per_sm(int W, bool tables, int block, size_t smem);
+cudaError_t launch_batch_build(int W, const BatchDev& B, bool with_tiles, cudaStream_t s);
+cudaError_t launch_batch_tile(int W, const BatchDev& B, int slot_cap, int max_n, KStats* st, int grid, cudaStream_t s);
+size_t batch_tile_smem(int W, int slot_cap, int max_n);
+int batch_tile_blocks_per_sm(int W, int slot_cap, int max_n);
+cudaError_t launch_batch_sac(int W, bool tables, const BatchDev& B, bool deep_only, KStats* st, int block, int grid,
+                             size_t smem, void* gscratch, size_t gstride, cudaStream_t s);
+int batch_sac_blocks_per_sm(int W, bool tables, int block, size_t smem);
+cudaError_t launch_batch_commit(int W, const BatchDev& B, KStats* st, cudaStream_t s);
+cudaError_t launch_batch_select(const BatchDev& B, bool initial, cudaStream_t s);
+
 // Shared-memory (or per-CTA scratch) bytes of the CTA-local fixpoint.
 size_t cta_state_bytes(const DevNet& N);
 

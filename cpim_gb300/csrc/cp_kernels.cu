@@ -694,31 +694,16 @@ __device__ __forceinline__ int pop_low(u64& m, int word) {
   return word * 64 + b;
 }
 
+// One tile: branches (x, base + l) for the live lanes l of `live`; work index
+// of the first live lane is b0. slot_of must be all -1 on entry and is left so;
+// s_fail / s_deep must be zero and visible to the whole CTA on entry. Ends
+// with the CTA synchronised.
 template <int WT>
-__global__ void __launch_bounds__(256) k_sac_tile(DevNet N, const u64* root, const int4* tiles, const int* ntiles,
-                                                  int* tcursor, uint8_t* ok, int* deep, int* ndeep, int slot_cap,
-                                                  KStats* st) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  u64* T = reinterpret_cast<u64*>(smem_raw);  // [slot_cap][32][WT]
-  int* slot_of = reinterpret_cast<int*>(smem_raw + static_cast<size_t>(slot_cap) * 32 * WT * 8);  // [n]
-  __shared__ int s_t;
-  __shared__ u32 s_fail, s_deep;
+__device__ __forceinline__ void tile_one(const DevNet& N, const u64* root, int x, int base, int b0, u32 live,
+                                         uint8_t* ok, int* deep, int* ndeep, int slot_cap, u64* T, int* slot_of,
+                                         u32& s_fail, u32& s_deep, u64& c_rev, u64& c_rows, u64& c_done) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  const int total = *ntiles;
-  for (int i = threadIdx.x; i < N.n; i += blockDim.x) slot_of[i] = -1;
-  u64 c_rev = 0, c_rows = 0, c_done = 0;
-  for (;;) {
-    if (threadIdx.x == 0) {
-      s_t = atomicAdd(tcursor, 1);
-      s_fail = 0;
-      s_deep = 0;
-    }
-    __syncthreads();
-    const int t = s_t;
-    if (t >= total) break;
-    const int4 tl = tiles[t];
-    const int x = tl.x, base = tl.y, b0 = tl.z;
-    const u32 live = static_cast<u32>(tl.w);
+  {
     const int a0 = N.arc_start[x], deg = N.arc_start[x + 1] - a0;
     const bool fits = deg <= slot_cap;
     if (fits) {
@@ -851,6 +836,9 @@ __global__ void __launch_bounds__(256) k_sac_tile(DevNet N, const u64* root, con
     }
     __syncthreads();
   }
+}
+
+__device__ __forceinline__ void flush_tile_counts(KStats* st, u64 c_rev, u64 c_rows, u64 c_done) {
   Cnt cn;
   cn.rev = c_rev;
   cn.rows = c_rows;
@@ -860,6 +848,34 @@ __global__ void __launch_bounds__(256) k_sac_tile(DevNet N, const u64* root, con
     atomicAdd(&st->branches, c_done);
     atomicMax(&st->rounds_max, 2);
   }
+}
+
+template <int WT>
+__global__ void __launch_bounds__(256) k_sac_tile(DevNet N, const u64* root, const int4* tiles, const int* ntiles,
+                                                  int* tcursor, uint8_t* ok, int* deep, int* ndeep, int slot_cap,
+                                                  KStats* st) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  u64* T = reinterpret_cast<u64*>(smem_raw);  // [slot_cap][32][WT]
+  int* slot_of = reinterpret_cast<int*>(smem_raw + static_cast<size_t>(slot_cap) * 32 * WT * 8);  // [n]
+  __shared__ int s_t;
+  __shared__ u32 s_fail, s_deep;
+  const int total = *ntiles;
+  for (int i = threadIdx.x; i < N.n; i += blockDim.x) slot_of[i] = -1;
+  u64 c_rev = 0, c_rows = 0, c_done = 0;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_t = atomicAdd(tcursor, 1);
+      s_fail = 0;
+      s_deep = 0;
+    }
+    __syncthreads();
+    const int t = s_t;
+    if (t >= total) break;
+    const int4 tl = tiles[t];
+    tile_one<WT>(N, root, tl.x, tl.y, tl.z, static_cast<u32>(tl.w), ok, deep, ndeep, slot_cap, T, slot_of, s_fail,
+                 s_deep, c_rev, c_rows, c_done);
+  }
+  flush_tile_counts(st, c_rev, c_rows, c_done);
 }
 
 __global__ void k_commit(int W, const int2* work, const int* nwork, const uint8_t* ok, u64* dom, int* evt, int* nevt,
@@ -929,6 +945,229 @@ __global__ void k_level_edit(int W, u64* dom, int var, int val, int op) {
     for (int w = 0; w < W; ++w) dv[w] = (w == (val >> 6)) ? (1ull << (val & 63)) : 0ull;
   } else {
     dv[val >> 6] &= ~(1ull << (val & 63));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Multi-instance batches: the same bodies, with the instance's DevNet copied
+// into shared memory by the CTA that takes a work item of that instance.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void load_net(DevNet* dst, const DevNet* src) {
+  if (threadIdx.x == 0) *dst = *src;
+}
+
+// Root or event AC of every listed instance; CTAs take instances in turn.
+template <int WT, bool kTab>
+__global__ void __launch_bounds__(512) k_batch_node(BatchDev B, int op, KStats* st, char* gscratch, size_t gstride) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_qlen[3], s_failed[2], s_failvar, s_err;
+  __shared__ DevNet sN;
+  char* base = gscratch ? gscratch + blockIdx.x * gstride : reinterpret_cast<char*>(smem_raw);
+  const int count = *B.nact;
+  if (threadIdx.x == 0) s_err = 0;
+  Cnt cn;
+  int rounds_max = 0;
+  u64 done = 0;
+  for (int i = blockIdx.x; i < count; i += gridDim.x) {
+    const int inst = B.act_list[i];
+    load_net(&sN, B.nets + inst);
+    __syncthreads();
+    const DevNet& N = sN;
+    Fix F = make_cta_fix(N, base, s_qlen, s_failed, &s_failvar);
+    const CtaLayout L = cta_layout(N);
+    const size_t words = static_cast<size_t>(N.n) * WT;
+    u64* dom = B.roots[inst];
+    block_copy(F.D, dom, words);
+    block_zero(reinterpret_cast<u32*>(base + L.fb0), (L.ts - L.fb0) / 4);
+    if (N.nt) block_zero(reinterpret_cast<u32*>(F.tstamp), N.nt);
+    if (threadIdx.x == 0) {
+      s_qlen[0] = s_qlen[1] = s_qlen[2] = 0;
+      s_failed[0] = s_failed[1] = 0;
+    }
+    __syncthreads();
+    if (op == kOpRoot) {
+      for (int z = threadIdx.x; z < N.n; z += blockDim.x) seed_var<WT>(N, F, z);
+    } else {
+      const int ne = B.nevt[inst];
+      const int* ev = B.evt + B.var_base[inst];
+      for (int j = threadIdx.x; j < ne; j += blockDim.x) seed_var<WT>(N, F, ev[j]);
+    }
+    __syncthreads();
+    const int rounds = cta_fixpoint<WT, kTab>(N, F, cn, &s_err);
+    rounds_max = max(rounds_max, rounds);
+    block_copy(dom, F.D, words);
+    if (threadIdx.x == 0 && (s_failed[0] | s_failed[1])) B.inc[inst] = 1;
+    ++done;
+    __syncthreads();
+  }
+  flush_counts(st, cn);
+  if (threadIdx.x == 0) {
+    atomicMax(&st->rounds_max, rounds_max);
+    if (done) atomicAdd(&st->fixpoints, done);
+    if (s_err) st->error = s_err;
+  }
+}
+
+// Live pairs (and tiles) of every active instance; one warp per variable.
+template <int WT>
+__global__ void k_batch_build(BatchDev B, int with_tiles) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int g = gw; g < B.total_vars; g += nw) {
+    const int inst = B.var_inst[g];
+    if (!B.act[inst] || B.inc[inst]) continue;
+    const int x = g - B.var_base[inst];
+    const int ds = B.nets[inst].dsize[x];
+    const u64* dom = B.roots[inst];
+    const int tag = (inst << 16) | x;
+    for (int base = 0; base < ds; base += 32) {
+      const u64 word = dom[static_cast<size_t>(x) * WT + (base >> 6)];
+      const u32 bits = static_cast<u32>(word >> (base & 32));
+      if (bits == 0) continue;
+      int b0 = 0;
+      if (lane == 0) {
+        b0 = atomicAdd(B.nwork, __popc(bits));
+        if (with_tiles) B.tiles[atomicAdd(B.ntiles, 1)] = make_int4(tag, base, b0, static_cast<int>(bits));
+      }
+      b0 = __shfl_sync(kFull, b0, 0);
+      if ((bits >> lane) & 1u) B.work[b0 + __popc(bits & ((1u << lane) - 1u))] = make_int2(tag, base + lane);
+    }
+  }
+}
+
+template <int WT>
+__global__ void __launch_bounds__(256) k_batch_tile(BatchDev B, int slot_cap, int max_n, KStats* st) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  u64* T = reinterpret_cast<u64*>(smem_raw);
+  int* slot_of = reinterpret_cast<int*>(smem_raw + static_cast<size_t>(slot_cap) * 32 * WT * 8);
+  __shared__ int s_t;
+  __shared__ u32 s_fail, s_deep;
+  __shared__ DevNet sN;
+  const int total = *B.ntiles;
+  for (int i = threadIdx.x; i < max_n; i += blockDim.x) slot_of[i] = -1;
+  u64 c_rev = 0, c_rows = 0, c_done = 0;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_t = atomicAdd(B.tcursor, 1);
+      s_fail = 0;
+      s_deep = 0;
+      if (s_t < total) sN = B.nets[B.tiles[s_t].x >> 16];
+    }
+    __syncthreads();
+    const int t = s_t;
+    if (t >= total) break;
+    const int4 tl = B.tiles[t];
+    const int inst = tl.x >> 16;
+    tile_one<WT>(sN, B.roots[inst], tl.x & 0xffff, tl.y, tl.z, static_cast<u32>(tl.w), B.ok, B.deep, B.ndeep,
+                 slot_cap, T, slot_of, s_fail, s_deep, c_rev, c_rows, c_done);
+  }
+  flush_tile_counts(st, c_rev, c_rows, c_done);
+}
+
+// General singleton tests over the batch: all pairs, or the deep list.
+template <int WT, bool kTab>
+__global__ void __launch_bounds__(256) k_batch_sac(BatchDev B, int deep_only, KStats* st, char* gscratch,
+                                                   size_t gstride) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_qlen[3], s_failed[2], s_failvar, s_err, s_b;
+  __shared__ DevNet sN;
+  char* base = gscratch ? gscratch + blockIdx.x * gstride : reinterpret_cast<char*>(smem_raw);
+  const int total = deep_only ? *B.ndeep : *B.nwork;
+  if (threadIdx.x == 0) s_err = 0;
+  Cnt cn;
+  int rounds_max = 0;
+  u64 done = 0;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_b = atomicAdd(B.cursor, 1);
+      if (s_b < total) {
+        const int b = deep_only ? B.deep[s_b] : s_b;
+        sN = B.nets[B.work[b].x >> 16];
+      }
+    }
+    __syncthreads();
+    const int i = s_b;
+    if (i >= total) break;
+    const int b = deep_only ? B.deep[i] : i;
+    const int2 pr = B.work[b];
+    const int inst = pr.x >> 16, x = pr.x & 0xffff, a = pr.y;
+    const DevNet& N = sN;
+    Fix F = make_cta_fix(N, base, s_qlen, s_failed, &s_failvar);
+    const CtaLayout L = cta_layout(N);
+    const size_t words = static_cast<size_t>(N.n) * WT;
+    block_copy(F.D, B.roots[inst], words);
+    block_zero(reinterpret_cast<u32*>(base + L.fb0), (L.ts - L.fb0) / 4);
+    if (N.nt) block_zero(reinterpret_cast<u32*>(F.tstamp), N.nt);
+    if (threadIdx.x == 0) {
+      s_qlen[0] = s_qlen[1] = s_qlen[2] = 0;
+      s_failed[0] = s_failed[1] = 0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      u64* dv = F.D + static_cast<size_t>(x) * WT;
+      for (int w = 0; w < WT; ++w) dv[w] = (w == (a >> 6)) ? (1ull << (a & 63)) : 0ull;
+      append_var(N, F.q0, F.fb0, F.qlen, x);
+    }
+    __syncthreads();
+    const int rounds = cta_fixpoint<WT, kTab>(N, F, cn, &s_err);
+    rounds_max = max(rounds_max, rounds);
+    if (threadIdx.x == 0) B.ok[b] = (s_failed[0] | s_failed[1]) ? 0 : 1;
+    ++done;
+    __syncthreads();
+  }
+  flush_counts(st, cn);
+  if (threadIdx.x == 0) {
+    atomicMax(&st->rounds_max, rounds_max);
+    if (done) {
+      atomicAdd(&st->fixpoints, done);
+      atomicAdd(&st->branches, done);
+    }
+    if (s_err) st->error = s_err;
+  }
+}
+
+// Removes failed pairs from their instance's level; collects changed
+// variables per instance.
+__global__ void k_batch_commit(BatchDev B, int W, KStats* st) {
+  const int total = *B.nwork;
+  u64 removed = 0;
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < total; b += gridDim.x * blockDim.x) {
+    if (B.ok[b]) continue;
+    const int2 pr = B.work[b];
+    const int inst = pr.x >> 16, x = pr.x & 0xffff, a = pr.y;
+    atomicAnd(B.roots[inst] + static_cast<size_t>(x) * W + (a >> 6), ~(1ull << (a & 63)));
+    atomicAdd(&B.removed[inst], 1);
+    ++removed;
+    const int g = B.var_base[inst] + x;
+    const u32 bit = 1u << (g & 31);
+    if (!(atomicOr(B.evt_fb + (g >> 5), bit) & bit)) B.evt[B.var_base[inst] + atomicAdd(&B.nevt[inst], 1)] = x;
+  }
+  if (removed) {
+    atomicAdd(&st->removed, removed);
+    atomicAdd(&st->deletions, removed);
+  }
+}
+
+// Next sweep's instances: initial = every consistent instance; otherwise the
+// consistent instances whose last commit removed values. Warp-ballot
+// compaction into act_list.
+__global__ void k_batch_select(BatchDev B, int initial) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int base = gw * 32; base < B.k; base += nw * 32) {
+    const int i = base + lane;
+    bool on = false;
+    if (i < B.k) {
+      on = !B.inc[i] && (initial || B.removed[i] > 0);
+      B.act[i] = on ? 1 : 0;
+    }
+    const u32 m = __ballot_sync(kFull, on);
+    int b0 = 0;
+    if (lane == 0 && m) b0 = atomicAdd(B.nact, __popc(m));
+    b0 = __shfl_sync(kFull, b0, 0);
+    if (on) B.act_list[b0 + __popc(m & ((1u << lane) - 1u))] = i;
   }
 }
 
@@ -1103,6 +1342,112 @@ cudaError_t launch_popcount(const DevNet& N, const u64* dom, int* sizes, cudaStr
 
 cudaError_t launch_level_edit(const DevNet& N, u64* dom, int var, int val, int op, cudaStream_t s) {
   k_level_edit<<<1, 1, 0, s>>>(N.W, dom, var, val, op);
+  return cudaGetLastError();
+}
+
+// ---- batches ----
+template <typename F>
+cudaError_t dispatch_wtab(int W, bool tables, F&& f) {
+  DevNet probe;
+  probe.W = W;
+  probe.nt = tables ? 1 : 0;
+  return dispatch_wt(probe, f);
+}
+
+int batch_node_blocks_per_sm(int W, bool tables, int block, size_t smem) {
+  int per_sm = 0;
+  cudaError_t e = dispatch_wtab(W, tables, [&](auto wt, auto tab) -> cudaError_t {
+    constexpr int WT = decltype(wt)::value;
+    constexpr bool TB = decltype(tab)::value;
+    cudaError_t e2 = allow_smem(k_batch_node<WT, TB>, smem);
+    if (e2 != cudaSuccess) return e2;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_node<WT, TB>, block, smem);
+  });
+  return e == cudaSuccess ? per_sm : 0;
+}
+
+cudaError_t launch_batch_node(int W, bool tables, const BatchDev& B, int op, KStats* st, int block, int grid,
+                              size_t smem, void* gscratch, size_t gstride, cudaStream_t s) {
+  return dispatch_wtab(W, tables, [&](auto wt, auto tab) -> cudaError_t {
+    constexpr int WT = decltype(wt)::value;
+    constexpr bool TB = decltype(tab)::value;
+    cudaError_t e = allow_smem(k_batch_node<WT, TB>, smem);
+    if (e != cudaSuccess) return e;
+    k_batch_node<WT, TB><<<grid, block, gscratch ? 0 : smem, s>>>(B, op, st, static_cast<char*>(gscratch), gstride);
+    return cudaGetLastError();
+  });
+}
+
+cudaError_t launch_batch_build(int W, const BatchDev& B, bool with_tiles, cudaStream_t s) {
+  return dispatch_w(W, [&](auto wt) -> cudaError_t {
+    constexpr int WT = decltype(wt)::value;
+    const int blocks = std::max(1, std::min(8192, (B.total_vars * 32 + 255) / 256));
+    k_batch_build<WT><<<blocks, 256, 0, s>>>(B, with_tiles ? 1 : 0);
+    return cudaGetLastError();
+  });
+}
+
+size_t batch_tile_smem(int W, int slot_cap, int max_n) {
+  return static_cast<size_t>(slot_cap) * 32 * W * 8 + static_cast<size_t>(max_n) * 4;
+}
+
+int batch_tile_blocks_per_sm(int W, int slot_cap, int max_n) {
+  const size_t smem = batch_tile_smem(W, slot_cap, max_n);
+  int per_sm = 0;
+  cudaError_t e = dispatch_w(W, [&](auto wt) -> cudaError_t {
+    constexpr int WT = decltype(wt)::value;
+    cudaError_t e2 = allow_smem(k_batch_tile<WT>, smem);
+    if (e2 != cudaSuccess) return e2;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_tile<WT>, 256, smem);
+  });
+  return e == cudaSuccess ? per_sm : 0;
+}
+
+cudaError_t launch_batch_tile(int W, const BatchDev& B, int slot_cap, int max_n, KStats* st, int grid,
+                              cudaStream_t s) {
+  const size_t smem = batch_tile_smem(W, slot_cap, max_n);
+  return dispatch_w(W, [&](auto wt) -> cudaError_t {
+    constexpr int WT = decltype(wt)::value;
+    cudaError_t e = allow_smem(k_batch_tile<WT>, smem);
+    if (e != cudaSuccess) return e;
+    k_batch_tile<WT><<<grid, 256, smem, s>>>(B, slot_cap, max_n, st);
+    return cudaGetLastError();
+  });
+}
+
+int batch_sac_blocks_per_sm(int W, bool tables, int block, size_t smem) {
+  int per_sm = 0;
+  cudaError_t e = dispatch_wtab(W, tables, [&](auto wt, auto tab) -> cudaError_t {
+    constexpr int WT = decltype(wt)::value;
+    constexpr bool TB = decltype(tab)::value;
+    cudaError_t e2 = allow_smem(k_batch_sac<WT, TB>, smem);
+    if (e2 != cudaSuccess) return e2;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_sac<WT, TB>, block, smem);
+  });
+  return e == cudaSuccess ? per_sm : 0;
+}
+
+cudaError_t launch_batch_sac(int W, bool tables, const BatchDev& B, bool deep_only, KStats* st, int block, int grid,
+                             size_t smem, void* gscratch, size_t gstride, cudaStream_t s) {
+  return dispatch_wtab(W, tables, [&](auto wt, auto tab) -> cudaError_t {
+    constexpr int WT = decltype(wt)::value;
+    constexpr bool TB = decltype(tab)::value;
+    cudaError_t e = allow_smem(k_batch_sac<WT, TB>, smem);
+    if (e != cudaSuccess) return e;
+    k_batch_sac<WT, TB><<<grid, block, gscratch ? 0 : smem, s>>>(B, deep_only ? 1 : 0, st,
+                                                                 static_cast<char*>(gscratch), gstride);
+    return cudaGetLastError();
+  });
+}
+
+cudaError_t launch_batch_commit(int W, const BatchDev& B, KStats* st, cudaStream_t s) {
+  k_batch_commit<<<2048, 256, 0, s>>>(B, W, st);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_select(const BatchDev& B, bool initial, cudaStream_t s) {
+  const int blocks = std::max(1, std::min(1024, (B.k + 255) / 256));
+  k_batch_select<<<blocks, 256, 0, s>>>(B, initial ? 1 : 0);
   return cudaGetLastError();
 }
 

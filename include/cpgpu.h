@@ -126,6 +126,28 @@ int cp_enforce_sac1(cp_net* net, int level, cp_stats* st);
 int cp_singletons(cp_net* net, int level, int count, const int* vars, const int* vals, uint8_t* ok,
                   int mode, cp_stats* st);
 
+/* ---- multi-instance batches ----------------------------------------------
+ * Many independent networks (each uploaded with cp_net_upload, of any sizes)
+ * propagated together: one launch per phase for all members of the same
+ * domain width, the sweep loop replayed from a captured CUDA graph. Works on
+ * level `level` of every member. No counterpart in the reference beyond its
+ * per-instance AC / SAC1 calls, which it batches. */
+typedef struct cp_batch cp_batch;
+int cp_batch_create(cp_engine* e, int k, cp_net* const* nets, int level, cp_batch** out);
+int cp_batch_destroy(cp_batch* b);
+/* Root AC of every member; inconsistent[i] (optional, k bytes) = verdict. */
+int cp_batch_ac(cp_batch* b, cp_stats* st, uint8_t* inconsistent);
+/* AC then SAC closure of every member. */
+int cp_batch_sac1(cp_batch* b, cp_stats* st, uint8_t* inconsistent);
+/* 1 (default): replay the sweep from a captured CUDA graph; 0: plain launches. */
+int cp_batch_set_graphs(cp_batch* b, int use_graphs);
+/* Autotuner: times tiled / general sweeps and CTA sizes per member group and
+ * caches the choice on disk ($CPGPU_TUNE_CACHE). */
+int cp_batch_tune(cp_batch* b);
+/* info[0..7] = groups, W, has tables, members, tiled, CTA size, slot capacity,
+ * CTA state in shared memory. */
+int cp_batch_info(const cp_batch* b, int group, int* info);
+
 /* ---- search: MAC on device-resident domains -------------------------------
  * MAC::enforce (src/MAC.cpp:100-165) with the reference's variable and value
  * heuristics (include/Solver.h:55-66: var 1 = VRH_DOM_MIN, value 0 =
