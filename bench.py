@@ -317,6 +317,80 @@ def run_ours(args):
     return 0
 
 
+UNEVEN_WORKLOAD = ("uneven multi-instance batch: {k} random binary CSPs, n~U[20,400], d in {{8..256}}, "
+                   "density~U[0.05,0.3], tightness~U[0.2,0.6], seeds 7*1000003+i; AC + SAC1 of every instance")
+
+
+def run_uneven(args):
+    """Config-4 measurement: AC + SAC1 of every instance of the uneven batch in
+    one launch per phase (graph-replayed sweeps), against the same instances
+    run one by one through cp_enforce_sac1."""
+    import torch
+    import cpim_gb300 as cp
+
+    torch.cuda.set_device(0)
+    K = args.instances
+    eng = cp.Engine(0)
+    t0 = time.time()
+    nets = []
+    for i in range(K):
+        net = cp.upload_uneven_device(eng, 7 * 1000003 + i, 20, 400, 256, max_levels=2)
+        net.level_copy(0, 1)
+        nets.append(net)
+    gen_s = time.time() - t0
+    dev_bytes = sum(n.device_bytes for n in nets)
+    batch = cp.Batch(eng, nets, level=0)
+    batch.tune()
+    launches0 = eng.launches
+
+    def step():
+        batch.copy_level(1)
+        return batch.sac1()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    launches0 = eng.launches
+    sts = []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            sts.append(step())
+    torch.cuda.synchronize()
+    gpu_launches = eng.launches - launches0
+    ms = [s.device_ms for s, _ in sts]
+    st, inc = sts[-1]
+    inst_rate = K / (statistics.median(ms) / 1e3)
+    branch_rate = st.branches / (statistics.median(ms) / 1e3)
+    # One instance at a time through the single-instance entry point.
+    M = min(K, args.per_instance_sample)
+    t_dev = 0.0
+    t0 = time.perf_counter()
+    for net in nets[:M]:
+        net.level_copy(1, 0)
+        t_dev += net.enforce_sac1(0).device_ms
+    t_wall = time.perf_counter() - t0
+    per_inst = M / (t_dev / 1e3)
+    per_inst_wall = M / t_wall
+    line = {"metric": "instance AC+SAC fixpoints/s (uneven batch, bit-exact)", "value": inst_rate,
+            "unit": "instances/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": statistics.median(ms), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded, relations generated on the device)",
+            "config": {"workload": UNEVEN_WORKLOAD.format(k=K), "instances": K,
+                       "device_bytes": dev_bytes, "generate_upload_s": gen_s,
+                       "inconsistent_instances": int(inc.sum()), "sweeps": int(st.sweeps),
+                       "groups": [batch.info(g) for g in range(batch.info(0)["groups"])]},
+            "branch_fixpoints_per_s": branch_rate, "branches_per_step": int(st.branches),
+            "per_instance_launches": {"instances": M, "value_device": per_inst, "value_wall": per_inst_wall,
+                                      "unit": "instances/s", "batched_over_per_instance": inst_rate / per_inst},
+            "gpu_launches": int(gpu_launches), "clocks": clk.summary()}
+    print(json.dumps(line))
+    batch.close()
+    for n in nets:
+        n.close()
+    eng.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -324,9 +398,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="timed steps only (for profiling)")
+    ap.add_argument("--workload", default="sac", choices=["sac", "uneven"],
+                    help="sac: the batched SAC sweep (headline); uneven: the uneven multi-instance batch")
+    ap.add_argument("--instances", type=int, default=4096, help="uneven workload: instances")
+    ap.add_argument("--per-instance-sample", type=int, default=256, help="uneven workload: one-by-one sample")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "uneven":
+        return run_uneven(args)
     return run_ours(args)
 
 

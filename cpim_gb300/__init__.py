@@ -110,6 +110,9 @@ def lib():
         "cp_gen_sizes": ([vp, C.POINTER(C.c_int64)], i),
         "cp_gen_export": ([vp, PI, P64, PI, P64, PI, PI, PI, PI], i),
         "cp_net_upload_instance": ([vp, vp, i, PV], i),
+        "cp_gen_binary_device": ([vp, i, i, i64, d, d, d, u64, i, PV], i),
+        "cp_gen_uneven_device": ([vp, u64, i, i, i, i, PV], i),
+        "cp_net_rows_get": ([vp, P64], i),
         "cp_batch_create": ([vp, i, PV, i, PV], i),
         "cp_batch_destroy": ([vp], i),
         "cp_batch_ac": ([vp, C.POINTER(Stats), PU8], i),
@@ -117,6 +120,7 @@ def lib():
         "cp_batch_set_graphs": ([vp, i], i),
         "cp_batch_tune": ([vp], i),
         "cp_batch_info": ([vp, i, PI], i),
+        "cp_batch_copy_level": ([vp, i], i),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -373,8 +377,72 @@ class Batch:
     def tune(self):
         _check(lib().cp_batch_tune(self._h))
 
+    def copy_level(self, src: int):
+        """Restores every member's batch level from level `src`."""
+        _check(lib().cp_batch_copy_level(self._h, src))
+
     def info(self, group: int = 0):
         out = np.zeros(8, np.int32)
         _check(lib().cp_batch_info(self._h, group, _p(out, C.c_int)))
         keys = ["groups", "W", "tables", "members", "tiled", "cta_threads", "slot_cap", "cta_in_smem"]
         return dict(zip(keys, out.tolist()))
+
+
+class _GeneratedNet(Net):
+    """A Net whose relation rows were generated on the device."""
+
+    def __init__(self, engine: Engine, h, n: int, W: int):
+        self.engine = engine
+        self.n, self.W = n, W
+        self._h = h
+
+    def rows(self, total_words: int) -> np.ndarray:
+        out = np.zeros(total_words, np.uint64)
+        _check(lib().cp_net_rows_get(self._h, _p(out, C.c_uint64)))
+        return out
+
+
+def upload_binary_device(engine: Engine, n, d, e, p_lo, p_hi=None, remove=0.0, seed=1, max_levels=0) -> Net:
+    """gen_binary's network with its rows generated on the device."""
+    h = C.c_void_p()
+    _check(lib().cp_gen_binary_device(engine._h, n, d, e, p_lo, p_lo if p_hi is None else p_hi, remove, seed,
+                                      max_levels, C.byref(h)))
+    return _GeneratedNet(engine, h, n, (d + 63) // 64)
+
+
+def upload_uneven_device(engine: Engine, seed, n_lo=20, n_hi=400, d_cap=256, max_levels=0):
+    """gen_uneven's network with its rows generated on the device. Returns
+    (net, n, d) where (n, d) is the drawn shape."""
+    h = C.c_void_p()
+    _check(lib().cp_gen_uneven_device(engine._h, seed, n_lo, n_hi, d_cap, max_levels, C.byref(h)))
+    # The shape is not returned by the C ABI; recover it from the host shape
+    # draw, which the device generator shares.
+    inst_shape = _uneven_shape(seed, n_lo, n_hi, d_cap)
+    return _GeneratedNet(engine, h, inst_shape[0], (inst_shape[1] + 63) // 64)
+
+
+def _uneven_shape(seed, n_lo, n_hi, d_cap):
+    # Same draws as cpgen::uneven_shape (cp_gen.h): splitmix-based stream.
+    M = 0xFFFFFFFFFFFFFFFF
+
+    def mix(z):
+        z = (z + 0x9e3779b97f4a7c15) & M
+        z = ((z ^ (z >> 30)) * 0xbf58476d1ce4e5b9) & M
+        z = ((z ^ (z >> 27)) * 0x94d049bb133111eb) & M
+        return z ^ (z >> 31)
+
+    s = mix((seed ^ 0xA11CE) ^ 0x5eed5eed5eed)
+    state = [s]
+
+    def nxt():
+        state[0] = (state[0] + 0x9e3779b97f4a7c15) & M
+        return mix(state[0])
+
+    def below(k):
+        return (nxt() * k) >> 64
+
+    n = n_lo + below(n_hi - n_lo + 1)
+    ds = [8, 16, 32, 64, 128, 256]
+    choices = sum(1 for v in ds if v <= d_cap)
+    d = ds[below(max(1, choices))]
+    return n, d

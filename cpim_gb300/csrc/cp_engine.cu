@@ -303,14 +303,17 @@ int cp_engine_set_sac_mode(cp_engine* e, int mode) {
   return CP_OK;
 }
 
-int cp_net_upload(cp_engine* e, int n, const int* dom, int W, const uint64_t* init, int n_bin, const int* bin_scope,
-                  const uint64_t* bin_rows, int n_tab, const int* tab_arity, const int* tab_scope,
-                  const int* tab_ntup, const int* tab_tuples, int max_levels, cp_net** out) {
+// rows_later: the binary rows are filled afterwards on the device (seeded
+// generator), so bin_rows may be null.
+static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uint64_t* init, int n_bin,
+                           const int* bin_scope, const uint64_t* bin_rows, int n_tab, const int* tab_arity,
+                           const int* tab_scope, const int* tab_ntup, const int* tab_tuples, int max_levels,
+                           cp_net** out, bool rows_later) {
   if (!e || !out) return fail(CP_E_ARG, "null engine or output");
   if (n < 1 || n >= kMaxVars) return fail(CP_E_ARG, "n out of range");
   if (!dom || !init) return fail(CP_E_ARG, "null dom or init");
   if (n_bin < 0 || n_tab < 0) return fail(CP_E_ARG, "negative constraint count");
-  if (n_bin > 0 && (!bin_scope || !bin_rows)) return fail(CP_E_ARG, "null binary arrays");
+  if (n_bin > 0 && (!bin_scope || (!bin_rows && !rows_later))) return fail(CP_E_ARG, "null binary arrays");
   if (n_tab > 0 && (!tab_arity || !tab_scope || !tab_ntup || !tab_tuples)) return fail(CP_E_ARG, "null table arrays");
   const int Wi = internal_words(W);
   if (W < 1 || Wi < 0) return fail(CP_E_UNSUPPORTED, "domains wider than 512 values are not supported");
@@ -570,13 +573,19 @@ int cp_net_upload(cp_engine* e, int n, const int* dom, int W, const uint64_t* in
   return CP_OK;
 }
 
+int cp_net_upload(cp_engine* e, int n, const int* dom, int W, const uint64_t* init, int n_bin, const int* bin_scope,
+                  const uint64_t* bin_rows, int n_tab, const int* tab_arity, const int* tab_scope,
+                  const int* tab_ntup, const int* tab_tuples, int max_levels, cp_net** out) {
+  return net_upload_impl(e, n, dom, W, init, n_bin, bin_scope, bin_rows, n_tab, tab_arity, tab_scope, tab_ntup,
+                         tab_tuples, max_levels, out, false);
+}
+
 int cp_net_reload(cp_net* net, const uint64_t* init, const uint64_t* bin_rows) {
   if (!net) return fail(CP_E_ARG, "null net");
   cp_engine* e = net->e;
   cudaStream_t s = e->stream;
   const int W = net->W_user, Wi = net->W, n = net->n;
-  if (net->nb > 0) {
-    if (!bin_rows) return fail(CP_E_ARG, "null rows");
+  if (net->nb > 0 && bin_rows) {
     if (W == Wi) {
       CP_CUDA(cudaMemcpyAsync(net->d_rel, bin_rows, static_cast<size_t>(net->relA_words) * 8, cudaMemcpyHostToDevice, s));
     } else {
@@ -1219,6 +1228,81 @@ int cp_gen_export(const cp_instance* inst, int* dom, uint64_t* init, int* bin_sc
   return CP_OK;
 }
 
+// Seeded instances whose relation rows are generated on the device: the host
+// draws the structure (scopes, tightness, removed values) from the same
+// stream as cp_gen_binary / cp_gen_uneven, the rows come from relation_word
+// on the GPU, so the network equals an upload of the host-generated one.
+static int upload_generated(cp_engine* e, const cpgen::Instance& I, int max_levels, cp_net** out) {
+  std::vector<int> scope(2 * static_cast<size_t>(I.n_bin()));
+  for (int c = 0; c < I.n_bin(); ++c) {
+    scope[2 * c] = I.bx[c];
+    scope[2 * c + 1] = I.by[c];
+  }
+  cp_net* net = nullptr;
+  CP_TRY(net_upload_impl(e, I.n, I.dom.data(), I.W, I.init.data(), I.n_bin(), scope.data(), nullptr, 0, nullptr,
+                         nullptr, nullptr, nullptr, max_levels, &net, true));
+  if (I.n_bin() > 0) {
+    u64* d_seed = nullptr;
+    u32* d_thr = nullptr;
+    cudaError_t err = cudaMalloc(&d_seed, I.bseed.size() * sizeof(u64));
+    if (err == cudaSuccess) err = cudaMalloc(&d_thr, I.bthr.size() * sizeof(u32));
+    if (err == cudaSuccess)
+      err = cudaMemcpyAsync(d_seed, I.bseed.data(), I.bseed.size() * sizeof(u64), cudaMemcpyHostToDevice, e->stream);
+    if (err == cudaSuccess)
+      err = cudaMemcpyAsync(d_thr, I.bthr.data(), I.bthr.size() * sizeof(u32), cudaMemcpyHostToDevice, e->stream);
+    if (err == cudaSuccess)
+      err = launch_gen_rows(net->dn, net->d_rel, net->d_bx, net->d_by, net->d_offA, d_seed, d_thr, e->stream);
+    if (err == cudaSuccess) {
+      err = cudaMemsetAsync(net->d_rel + net->relA_words, 0, static_cast<size_t>(net->relB_words) * 8, e->stream);
+      if (err == cudaSuccess)
+        err = launch_transpose(net->dn, net->d_rel, net->d_bx, net->d_by, net->d_offA, net->d_offB, e->stream);
+    }
+    if (err == cudaSuccess) err = cudaStreamSynchronize(e->stream);
+    e->launches += 2;
+    cudaFree(d_seed);
+    cudaFree(d_thr);
+    if (err != cudaSuccess) {
+      cp_net_destroy(net);
+      return fail(CP_E_CUDA, std::string("device generator: ") + cudaGetErrorString(err));
+    }
+  }
+  *out = net;
+  return CP_OK;
+}
+
+int cp_gen_binary_device(cp_engine* e, int n, int d, int64_t ne, double p_lo, double p_hi, double remove,
+                         uint64_t seed, int max_levels, cp_net** out) {
+  if (!e || !out || n < 2 || d < 1 || ne < 0) return fail(CP_E_ARG, "bad generator arguments");
+  cpgen::Instance I;
+  try {
+    I = cpgen::random_binary(n, d, ne, p_lo, p_hi, remove, seed, false);
+  } catch (const std::exception& ex) {
+    return fail(CP_E_ARG, ex.what());
+  }
+  return upload_generated(e, I, max_levels, out);
+}
+
+int cp_gen_uneven_device(cp_engine* e, uint64_t seed, int n_lo, int n_hi, int d_cap, int max_levels, cp_net** out) {
+  if (!e || !out || n_lo < 2 || n_hi < n_lo || d_cap < 8) return fail(CP_E_ARG, "bad generator arguments");
+  const cpgen::Instance I = cpgen::uneven_instance(seed, n_lo, n_hi, d_cap, false);
+  return upload_generated(e, I, max_levels, out);
+}
+
+int cp_net_rows_get(cp_net* net, uint64_t* out) {
+  if (!net || !out) return fail(CP_E_ARG, "null argument");
+  const int W = net->W_user, Wi = net->W;
+  std::vector<u64> rows(static_cast<size_t>(net->relA_words));
+  CP_CUDA(cudaMemcpy(rows.data(), net->d_rel, rows.size() * 8, cudaMemcpyDeviceToHost));
+  int64_t src = 0, dst = 0;
+  for (int c = 0; c < net->nb; ++c)
+    for (int a = 0; a < net->dom[net->bx[c]]; ++a) {
+      for (int w = 0; w < W; ++w) out[dst + w] = rows[src + w];
+      src += Wi;
+      dst += W;
+    }
+  return CP_OK;
+}
+
 int cp_net_upload_instance(cp_engine* e, const cp_instance* inst, int max_levels, cp_net** out) {
   if (!inst) return fail(CP_E_ARG, "null instance");
   const auto& I = inst->I;
@@ -1706,6 +1790,18 @@ int cp_batch_tune(cp_batch* b) {
     }
     tune_store(g.key, g.tiled, g.sac_block);
   }
+  return CP_OK;
+}
+
+int cp_batch_copy_level(cp_batch* b, int src) {
+  if (!b) return fail(CP_E_ARG, "null batch");
+  for (cp_net* n : b->nets)
+    if (src < 0 || src >= n->levels) return fail(CP_E_ARG, "source level out of range for a batch member");
+  for (auto& g : b->groups) {
+    CP_CUDA(launch_batch_copy(g.W, g.B, src - b->level, b->e->stream));
+    ++b->e->launches;
+  }
+  CP_CUDA(cudaStreamSynchronize(b->e->stream));
   return CP_OK;
 }
 

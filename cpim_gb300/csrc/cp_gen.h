@@ -17,9 +17,15 @@
 #include <unordered_set>
 #include <vector>
 
+#ifdef __CUDACC__
+#define CPGEN_HD __host__ __device__
+#else
+#define CPGEN_HD
+#endif
+
 namespace cpgen {
 
-inline uint64_t mix64(uint64_t z) {
+CPGEN_HD inline uint64_t mix64(uint64_t z) {
   z += 0x9e3779b97f4a7c15ull;
   z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
   z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
@@ -63,6 +69,8 @@ struct Instance {
   std::vector<int> tntup;           // tuples per table
   std::vector<int64_t> ttup_off;    // offset into ttup (in ints)
   std::vector<int> ttup;            // tuples, row-major (arity ints each)
+  std::vector<uint64_t> bseed;      // per binary constraint: relation seed
+  std::vector<uint32_t> bthr;       // per binary constraint: tightness threshold
 
   int n_bin() const { return static_cast<int>(bx.size()); }
   int n_tab() const { return static_cast<int>(tarity.size()); }
@@ -91,7 +99,7 @@ inline void init_full_domains(Instance& I) {
 // Support word w of row a of a binary relation with tightness threshold thr16
 // (a tuple is forbidden iff a 16-bit uniform draw is below thr16). Counter
 // based, so any word can be generated independently.
-inline uint64_t relation_word(uint64_t cseed, int a, int w, uint32_t thr16, int dom_y) {
+CPGEN_HD inline uint64_t relation_word(uint64_t cseed, int a, int w, uint32_t thr16, int dom_y) {
   uint64_t out = 0;
   for (int q = 0; q < 16; ++q) {
     const uint64_t h = mix64(cseed ^ mix64((uint64_t(uint32_t(a)) << 32) | (uint64_t(w) << 8) | uint64_t(q)));
@@ -115,8 +123,11 @@ inline uint32_t tightness_threshold(double p) {
 // Appends e binary constraints on distinct unordered variable pairs drawn
 // uniformly; constraint c forbids each tuple independently with probability
 // p_c, p_c uniform in [p_lo, p_hi] (p_lo == p_hi gives a fixed tightness).
+// make_rows = false records each constraint's seed and threshold (bseed,
+// bthr) without materialising the rows, for generators that build the rows
+// on a GPU with the same relation_word.
 inline void add_random_binary(Instance& I, int64_t e, double p_lo, double p_hi, Stream& S,
-                              uint64_t seed) {
+                              uint64_t seed, bool make_rows = true) {
   const int64_t total = int64_t(I.n) * (I.n - 1) / 2;
   if (e > total) throw std::invalid_argument("more binary constraints than variable pairs");
   std::unordered_set<uint64_t> seen;
@@ -136,6 +147,9 @@ inline void add_random_binary(Instance& I, int64_t e, double p_lo, double p_hi, 
     const uint32_t thr = tightness_threshold(p);
     const uint64_t cseed = mix64(seed ^ mix64(0xB1A5B1A5ull + uint64_t(c)));
     const int x = I.bx[c], y = I.by[c];
+    I.bseed.push_back(cseed);
+    I.bthr.push_back(thr);
+    if (!make_rows) continue;
     I.brow_off.push_back(int64_t(I.brows.size()));
     for (int a = 0; a < I.dom[x]; ++a)
       for (int w = 0; w < I.W; ++w) I.brows.push_back(w < words_for(I.dom[y]) ? relation_word(cseed, a, w, thr, I.dom[y]) : 0ull);
@@ -211,10 +225,10 @@ inline Instance empty_instance(int n, int d) {
 // e constraints on distinct pairs, tightness uniform in [p_lo, p_hi], then a
 // fraction `remove` of all (variable, value) pairs cleared.
 inline Instance random_binary(int n, int d, int64_t e, double p_lo, double p_hi, double remove,
-                              uint64_t seed) {
+                              uint64_t seed, bool make_rows = true) {
   Instance I = empty_instance(n, d);
   Stream S(seed);
-  add_random_binary(I, e, p_lo, p_hi, S, seed);
+  add_random_binary(I, e, p_lo, p_hi, S, seed, make_rows);
   remove_random_values(I, remove, S);
   return I;
 }
@@ -258,9 +272,10 @@ inline UnevenShape uneven_shape(uint64_t seed, int n_lo = 20, int n_hi = 400, in
   return s;
 }
 
-inline Instance uneven_instance(uint64_t seed, int n_lo = 20, int n_hi = 400, int d_cap = 256) {
+inline Instance uneven_instance(uint64_t seed, int n_lo = 20, int n_hi = 400, int d_cap = 256,
+                                bool make_rows = true) {
   const UnevenShape s = uneven_shape(seed, n_lo, n_hi, d_cap);
-  return random_binary(s.n, s.d, s.e, s.p, s.p, 0.0, seed);
+  return random_binary(s.n, s.d, s.e, s.p, s.p, 0.0, seed, make_rows);
 }
 
 // FNV-1a over every array of the instance: a fingerprint stored beside golden

@@ -145,6 +145,8 @@ cudaError_t launch_batch_sac(int W, bool tables, const BatchDev& B, bool deep_on
 int batch_sac_blocks_per_sm(int W, bool tables, int block, size_t smem);
 cudaError_t launch_batch_commit(int W, const BatchDev& B, KStats* st, cudaStream_t s);
 cudaError_t launch_batch_select(const BatchDev& B, bool initial, cudaStream_t s);
+// Copies level (batch level + delta) onto the batch level for every member.
+cudaError_t launch_batch_copy(int W, const BatchDev& B, int delta, cudaStream_t s);
 
 // Shared-memory (or per-CTA scratch) bytes of the CTA-local fixpoint.
 size_t cta_state_bytes(const DevNet& N);
@@ -181,6 +183,10 @@ cudaError_t launch_commit(const DevNet& N, u64* dom, SacScratch S, KStats* st, c
 // Builds the B blocks (transposes) of the binary relations.
 cudaError_t launch_transpose(const DevNet& N, u64* rel, const int* bx, const int* by, const int64_t* offA,
                              const int64_t* offB, cudaStream_t s);
+// Fills the A blocks of seeded random relations on the device (cp_gen.h's
+// relation_word, the same bits as the host generator).
+cudaError_t launch_gen_rows(const DevNet& N, u64* rel, const int* bx, const int* by, const int64_t* offA,
+                            const u64* cseed, const u32* thr, cudaStream_t s);
 // Sets the message returned by cp_last_error_string on this thread.
 void set_last_error(const std::string& msg);
 // Level helpers.

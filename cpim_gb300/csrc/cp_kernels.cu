@@ -25,6 +25,7 @@
 #include <cstdio>
 #include <type_traits>
 
+#include "cp_gen.h"
 #include "cp_internal.h"
 
 namespace cpgpu {
@@ -929,6 +930,25 @@ __global__ void k_transpose(DevNet N, u64* rel, const int* bx, const int* by, co
   }
 }
 
+// A blocks of seeded random relations generated on the device with the same
+// counter-based relation_word as the host generator (cp_gen.h): one warp per
+// constraint, lanes over its words.
+__global__ void k_gen_rows(int nb, int W, const int* dsize, u64* rel, const int* bx, const int* by,
+                           const int64_t* offA, const u64* cseed, const u32* thr) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int c = gw; c < nb; c += nw) {
+    const int dx = dsize[bx[c]], dy = dsize[by[c]];
+    const int wy = (dy + 63) / 64;
+    const int total = dx * W;
+    for (int i = lane; i < total; i += 32) {
+      const int a = i / W, w = i % W;
+      rel[offA[c] + i] = w < wy ? cpgen::relation_word(cseed[c], a, w, thr[c], dy) : 0ull;
+    }
+  }
+}
+
 template <int WT>
 __global__ void k_popcount(int n, const u64* dom, int* sizes) {
   for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x) {
@@ -1149,6 +1169,17 @@ __global__ void k_batch_commit(BatchDev B, int W, KStats* st) {
   }
 }
 
+// Copies level (batch level + delta) of every member onto the batch level,
+// one CTA per member in turn.
+__global__ void k_batch_copy(BatchDev B, int W, int delta) {
+  for (int i = blockIdx.x; i < B.k; i += gridDim.x) {
+    const size_t words = static_cast<size_t>(B.nets[i].n) * W;
+    u64* dst = B.roots[i];
+    const u64* src = dst + static_cast<ptrdiff_t>(delta) * static_cast<ptrdiff_t>(words);
+    for (size_t j = threadIdx.x; j < words; j += blockDim.x) dst[j] = src[j];
+  }
+}
+
 // Next sweep's instances: initial = every consistent instance; otherwise the
 // consistent instances whose last commit removed values. Warp-ballot
 // compaction into act_list.
@@ -1345,6 +1376,14 @@ cudaError_t launch_level_edit(const DevNet& N, u64* dom, int var, int val, int o
   return cudaGetLastError();
 }
 
+cudaError_t launch_gen_rows(const DevNet& N, u64* rel, const int* bx, const int* by, const int64_t* offA,
+                            const u64* cseed, const u32* thr, cudaStream_t s) {
+  if (N.nb == 0) return cudaSuccess;
+  const int blocks = std::max(1, std::min(16384, (N.nb * 32 + 255) / 256));
+  k_gen_rows<<<blocks, 256, 0, s>>>(N.nb, N.W, N.dsize, rel, bx, by, offA, cseed, thr);
+  return cudaGetLastError();
+}
+
 // ---- batches ----
 template <typename F>
 cudaError_t dispatch_wtab(int W, bool tables, F&& f) {
@@ -1442,6 +1481,11 @@ cudaError_t launch_batch_sac(int W, bool tables, const BatchDev& B, bool deep_on
 
 cudaError_t launch_batch_commit(int W, const BatchDev& B, KStats* st, cudaStream_t s) {
   k_batch_commit<<<2048, 256, 0, s>>>(B, W, st);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_copy(int W, const BatchDev& B, int delta, cudaStream_t s) {
+  k_batch_copy<<<std::max(1, std::min(B.k, 4096)), 256, 0, s>>>(B, W, delta);
   return cudaGetLastError();
 }
 

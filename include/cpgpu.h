@@ -147,6 +147,9 @@ int cp_batch_tune(cp_batch* b);
 /* info[0..7] = groups, W, has tables, members, tiled, CTA size, slot capacity,
  * CTA state in shared memory. */
 int cp_batch_info(const cp_batch* b, int group, int* info);
+/* Copies level src of every member onto the batch's level (one launch per
+ * member group), e.g. to restore pristine domains kept at another level. */
+int cp_batch_copy_level(cp_batch* b, int src);
 
 /* ---- search: MAC on device-resident domains -------------------------------
  * MAC::enforce (src/MAC.cpp:100-165) with the reference's variable and value
@@ -183,6 +186,14 @@ int cp_gen_export(const cp_instance* inst, int* dom, uint64_t* init, int* bin_sc
                   int* tab_arity, int* tab_scope, int* tab_ntup, int* tab_tuples);
 /* Uploads an instance directly (no host export). */
 int cp_net_upload_instance(cp_engine* e, const cp_instance* inst, int max_levels, cp_net** out);
+/* The same seeded networks as cp_gen_binary / cp_gen_uneven, with the
+ * relation rows generated on the device (bit-identical), for workloads whose
+ * relations are too large to generate on the host quickly. */
+int cp_gen_binary_device(cp_engine* e, int n, int d, int64_t ne, double p_lo, double p_hi, double remove,
+                         uint64_t seed, int max_levels, cp_net** out);
+int cp_gen_uneven_device(cp_engine* e, uint64_t seed, int n_lo, int n_hi, int d_cap, int max_levels, cp_net** out);
+/* Copies a network's binary support rows (the upload format) back to the host. */
+int cp_net_rows_get(cp_net* net, uint64_t* out);
 
 /* ---- allocation-free AC fixpoint ------------------------------------------
  * No counterpart in the reference. For callers that must not allocate device

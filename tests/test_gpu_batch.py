@@ -103,3 +103,47 @@ def test_batch_with_tables_matches_oracle():
             if ok:
                 assert np.array_equal(nets[k].dom_get(0), d)
         b.close()
+
+
+def test_device_generator_matches_host():
+    with cp.Engine(0) as eng:
+        for args in [(50, 16, 250, 0.3, 0.3, 0.0, 1), (40, 100, 160, 0.8, 0.8, 0.2, 3), (60, 256, 300, 0.5, 0.5, 0.1, 2)]:
+            inst = cp.gen_binary(*args)
+            net = cp.upload_binary_device(eng, *args, max_levels=2)
+            assert np.array_equal(net.rows(inst.bin_rows.size), inst.bin_rows)
+            assert np.array_equal(net.dom_get(0), inst.init)
+            net.close()
+        for s in range(6):
+            seed = 7 * 1000003 + s
+            inst = cp.gen_uneven(seed, 20, 120, 256)
+            net = cp.upload_uneven_device(eng, seed, 20, 120, 256, max_levels=2)
+            assert (net.n, net.W) == (inst.n, inst.W)
+            assert np.array_equal(net.rows(inst.bin_rows.size), inst.bin_rows)
+            st = net.enforce_sac1(0)
+            ref = eng.upload(inst, max_levels=2)
+            st2 = ref.enforce_sac1(0)
+            assert st.inconsistent == st2.inconsistent
+            if not st.inconsistent:
+                assert np.array_equal(net.dom_get(0), ref.dom_get(0))
+            net.close()
+            ref.close()
+
+
+def test_batch_copy_level_restores():
+    insts = _members(8, 11)
+    with cp.Engine(0) as eng:
+        nets = [eng.upload(i, max_levels=2) for i in insts]
+        for n in nets:
+            n.level_copy(0, 1)
+        b = cp.Batch(eng, nets)
+        st1, inc1 = b.sac1()
+        d1 = [n.dom_get(0) for n in nets]
+        b.copy_level(1)
+        for n, inst in zip(nets, insts):
+            assert np.array_equal(n.dom_get(0), inst.init)
+        st2, inc2 = b.sac1()
+        assert np.array_equal(inc1, inc2)
+        for n, d, bad in zip(nets, d1, inc1):
+            if not bad:  # after a wipe-out only the verdict is defined
+                assert np.array_equal(n.dom_get(0), d)
+        b.close()
