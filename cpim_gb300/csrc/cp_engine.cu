@@ -104,6 +104,7 @@ struct cp_net {
   bool cta_in_smem = true;
   bool prefer_grid = false;
   int64_t device_bytes = 0;
+  int max_deg = 0;     // largest number of binary arcs at one variable
 
   ~cp_net() {
     for (void* p : allocs) cudaFree(p);
@@ -551,12 +552,16 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   if (net->grid_blocks < 1) return fail(CP_E_UNSUPPORTED, "grid fixpoint kernel does not fit");
   // Tiled SAC sweep (binary networks): shared memory holds the round-one
   // domains of up to slot_cap neighbours for 32 branches, plus a slot map.
+  for (int x = 0; x < n; ++x) net->max_deg = std::max(net->max_deg, arc_deg[x]);
   if (n_tab == 0) {
-    const size_t budget = std::min<size_t>(e->smem_optin > 4096 ? e->smem_optin - 4096 : 0, 100 * 1024);
     const size_t per_slot = static_cast<size_t>(32) * Wi * 8;
-    int cap = 0;
-    for (int x = 0; x < n; ++x) cap = std::max(cap, arc_deg[x]);
-    cap = std::max(cap, 1);
+    int cap = std::max(net->max_deg, 1);
+    // 100 KB keeps two or more tile CTAs per SM; a network whose densest
+    // variable needs more gets up to the opt-in limit (fewer, larger CTAs)
+    // rather than sending those variables' branches to the general kernel.
+    const size_t optin = e->smem_optin > 4096 ? e->smem_optin - 4096 : 0;
+    const size_t need = static_cast<size_t>(n) * 4 + per_slot * static_cast<size_t>(cap);
+    const size_t budget = std::min<size_t>(optin, std::max<size_t>(100 * 1024, need));
     if (static_cast<size_t>(n) * 4 + per_slot * 8 <= budget) {
       const size_t fit = (budget - static_cast<size_t>(n) * 4) / per_slot;
       net->slot_cap = static_cast<int>(std::min<size_t>(static_cast<size_t>(cap), fit));
@@ -1325,6 +1330,7 @@ namespace {
 struct BatchGroup {
   int W = 1;
   bool tables = false;
+  bool dense = false;  // members whose densest variable overflows a 100 KB tile
   std::vector<int> members;  // indices into cp_batch::nets
   BatchDev B;
   int max_n = 0;
@@ -1501,8 +1507,10 @@ int batch_group_setup(cp_batch* b, BatchGroup& g) {
   g.tiled = false;
   g.tile_grid = 0;
   if (!g.tables && g.max_n < 65536) {
-    const size_t budget = std::min<size_t>(e->smem_optin > 4096 ? e->smem_optin - 4096 : 0, 100 * 1024);
     const size_t per_slot = static_cast<size_t>(32) * g.W * 8;
+    const size_t optin = e->smem_optin > 4096 ? e->smem_optin - 4096 : 0;
+    const size_t need = static_cast<size_t>(g.max_n) * 4 + per_slot * static_cast<size_t>(max_deg);
+    const size_t budget = std::min<size_t>(optin, g.dense ? need : 100 * 1024);
     if (static_cast<size_t>(g.max_n) * 4 + per_slot * 8 <= budget) {
       g.slot_cap = static_cast<int>(std::min<size_t>(max_deg, (budget - static_cast<size_t>(g.max_n) * 4) / per_slot));
       const int per_sm_t = batch_tile_blocks_per_sm(g.W, g.slot_cap, g.max_n);
@@ -1653,14 +1661,19 @@ int cp_batch_create(cp_engine* e, int k, cp_net* const* nets, int level, cp_batc
   for (int i = 0; i < k; ++i) {
     const int W = nets[i]->W;
     const bool tab = nets[i]->nt > 0;
+    // Members whose densest variable does not fit a 100 KB tile form their
+    // own group, whose tiles get the larger shared-memory budget.
+    const bool dense = !tab && static_cast<size_t>(nets[i]->n) * 4 +
+                                       static_cast<size_t>(32) * W * 8 * nets[i]->max_deg > 100 * 1024;
     BatchGroup* g = nullptr;
     for (auto& gg : b->groups)
-      if (gg.W == W && gg.tables == tab) g = &gg;
+      if (gg.W == W && gg.tables == tab && gg.dense == dense) g = &gg;
     if (!g) {
       b->groups.emplace_back();
       g = &b->groups.back();
       g->W = W;
       g->tables = tab;
+      g->dense = dense;
     }
     g->members.push_back(i);
   }

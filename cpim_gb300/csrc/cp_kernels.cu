@@ -207,12 +207,16 @@ __device__ __forceinline__ void revise_arc(const DevNet& N, const Fix& F, u32* q
 #pragma unroll
   for (int w = 0; w < WT; ++w) rm[w] = 0;
   if (cy < cz) {
-    // Union of the supports (in z) of the live values of y.
-    u64 acc[WT];
+    // Union of the supports (in z) of the live values of y, 32 rows per
+    // step; stops as soon as the union covers D(z) (nothing to remove).
+    u64 acc[WT], cov[WT];
 #pragma unroll
-    for (int w = 0; w < WT; ++w) acc[w] = 0;
+    for (int w = 0; w < WT; ++w) acc[w] = cov[w] = 0;
+    int loaded = 0;
+    bool covered = false;
 #pragma unroll
     for (int base = 0; base < 64 * WT; base += 32) {
+      if (covered) break;
       const u32 bits = static_cast<u32>(dy[base >> 6] >> (base & 32));
       if (bits == 0) continue;
       if ((bits >> lane) & 1u) {
@@ -221,10 +225,18 @@ __device__ __forceinline__ void revise_arc(const DevNet& N, const Fix& F, u32* q
 #pragma unroll
         for (int w = 0; w < WT; ++w) acc[w] |= r[w];
       }
+      loaded += __popc(bits);
+      u64 gap = 0;
+#pragma unroll
+      for (int w = 0; w < WT; ++w) {
+        cov[w] = warp_or64(acc[w]);
+        gap |= dz[w] & ~cov[w];
+      }
+      covered = gap == 0;
     }
 #pragma unroll
-    for (int w = 0; w < WT; ++w) rm[w] = dz[w] & ~warp_or64(acc[w]);
-    if (lane == 0) cn.rows += cy;
+    for (int w = 0; w < WT; ++w) rm[w] = dz[w] & ~cov[w];
+    if (lane == 0) cn.rows += loaded;
   } else {
     // Every live value of z tests its support row against D(y).
 #pragma unroll
