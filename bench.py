@@ -402,6 +402,97 @@ def run_uneven(args):
     return 0
 
 
+SERVING_WORKLOAD = ("serving: Poisson arrivals, requests propagate:SAC:MAC-solve = 70:20:10 on {r} resident networks "
+                    "(random binary CSPs, n~U[20,400], d in {{8..256}}, density~U[0.05,0.3], tightness~U[0.2,0.6], "
+                    "seeds 5*1000003+i), 0-3 random variable choices per request, HBM budget 150 GB")
+
+
+def _serving_trace(rng, rate, k, ids, shapes):
+    """k requests: Poisson arrivals at `rate`, types 70:20:10, a uniformly
+    drawn resident network, 0-3 (var, value) choices."""
+    import numpy as np
+    types = rng.choice(3, size=k, p=[0.7, 0.2, 0.1])
+    gaps = rng.exponential(1.0 / rate, size=k)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    reqs = []
+    for t in types:
+        j = int(rng.integers(0, len(ids)))
+        n, d = shapes[j]
+        ch = [(int(rng.integers(0, n)), int(rng.integers(0, d))) for _ in range(int(rng.integers(0, 4)))]
+        reqs.append((int(t), ids[j], ch))
+    return arrivals, reqs, types
+
+
+def run_serving(args):
+    """Config-5 measurement: request latency and throughput of the server
+    with continuous batching, beside the one-request-per-launch path."""
+    import numpy as np
+    import torch
+    import cpim_gb300 as cp
+
+    torch.cuda.set_device(0)
+    R = args.networks
+    seeds = [5 * 1000003 + i for i in range(R)]
+    t0 = time.time()
+    hs = [cp.InstanceHandle.uneven(sd, 20, 400, 256) for sd in seeds]
+    shapes = [cp._uneven_shape(sd, 20, 400, 256) for sd in seeds]
+    gen_s = time.time() - t0
+    rates = [float(x) for x in args.rates.split(",")]
+    modes = [("batched", True), ("plain", False)]
+    results = {}
+    launches = 0
+    with ClockSampler(0) as clk:
+        for mode, batching in modes:
+            rng = np.random.default_rng(11)
+            with cp.Server(budget_bytes=150 * 10**9, max_batch=args.max_batch, batching=batching,
+                           solve_time_limit_ms=args.solve_limit_ms, solvers=args.solvers) as srv:
+                t1 = time.time()
+                ids = [srv.register(h, slots=args.slots) for h in hs]
+                reg_s = time.time() - t1
+                # Warm-up: pools, tuning cache, solver copies.
+                arr, reqs, _ = _serving_trace(rng, 2000.0, 200, ids, shapes)
+                srv.run_trace(arr, reqs)
+                l0 = srv.eA.launches + srv.eB.launches
+                pts = []
+                for rate in rates:
+                    k = int(min(args.requests, max(50, rate * args.duration)))
+                    arr, reqs, types = _serving_trace(rng, rate, k, ids, shapes)
+                    lat, st, stats = srv.run_trace(arr, reqs)
+                    ok = st == 2
+                    pt = {"offered_rps": rate, "requests": k, "completed": int(ok.sum()),
+                          "errors": int((~ok).sum()), "wall_s": stats[2], "throughput_rps": k / stats[2],
+                          "p50_ms": float(np.percentile(lat[ok], 50)) if ok.any() else None,
+                          "p99_ms": float(np.percentile(lat[ok], 99)) if ok.any() else None,
+                          "ticks": int(stats[0]), "mean_batch": (stats[1] / stats[0]) if stats[0] else 0.0,
+                          "peak_admitted_gb": stats[3] / 1e9, "busy_propagate_s": stats[4],
+                          "busy_sac_s": stats[5], "busy_solvers_s": stats[6], "mac_timeouts": int(stats[7])}
+                    for t, name in ((0, "propagate"), (1, "sac"), (2, "mac")):
+                        sel = ok & (types == t)
+                        if sel.any():
+                            pt[name + "_p50_ms"] = float(np.percentile(lat[sel], 50))
+                            pt[name + "_p99_ms"] = float(np.percentile(lat[sel], 99))
+                    pts.append(pt)
+                launches += srv.eA.launches + srv.eB.launches - l0
+                results[mode] = {"points": pts, "register_s": reg_s}
+    best = max(p["throughput_rps"] for p in results["batched"]["points"])
+    best_plain = max(p["throughput_rps"] for p in results["plain"]["points"])
+    line = {"metric": "served requests/s (propagate/SAC/MAC mix, p50/p99 latency)", "value": best,
+            "unit": "requests/s", "n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u64", "data": "synthetic (seeded generator)",
+            "config": {"workload": SERVING_WORKLOAD.format(r=R), "networks": R, "slots_per_network": args.slots,
+                       "max_batch": args.max_batch, "solvers": args.solvers,
+                       "solve_time_limit_ms": args.solve_limit_ms, "rates_rps": rates,
+                       "requests_per_rate": "min(%d, rate x %.1f s)" % (args.requests, args.duration),
+                       "generate_s": gen_s},
+            "batched": results["batched"], "plain": results["plain"],
+            "batched_over_plain_peak_throughput": best / best_plain if best_plain else None,
+            "gpu_launches": int(launches), "clocks": clk.summary(),
+            "note": "latency = submit to result on the host (trace replayed by the native server); "
+                    "throughput = requests / (last completion - first arrival) per rate point"}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -409,15 +500,26 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="timed steps only (for profiling)")
-    ap.add_argument("--workload", default="sac", choices=["sac", "uneven"],
-                    help="sac: the batched SAC sweep (headline); uneven: the uneven multi-instance batch")
+    ap.add_argument("--workload", default="sac", choices=["sac", "uneven", "serving"],
+                    help="sac: the batched SAC sweep (headline); uneven: the uneven multi-instance batch; "
+                         "serving: the request server under Poisson load")
     ap.add_argument("--instances", type=int, default=4096, help="uneven workload: instances")
     ap.add_argument("--per-instance-sample", type=int, default=256, help="uneven workload: one-by-one sample")
+    ap.add_argument("--networks", type=int, default=64, help="serving: resident networks")
+    ap.add_argument("--slots", type=int, default=16, help="serving: working levels per resident network")
+    ap.add_argument("--rates", default="100,300,1000,3000,10000,50000", help="serving: offered loads, req/s")
+    ap.add_argument("--requests", type=int, default=2000, help="serving: most requests per rate point")
+    ap.add_argument("--duration", type=float, default=2.0, help="serving: seconds of arrivals per rate point")
+    ap.add_argument("--max-batch", type=int, default=256, help="serving: requests per batch tick")
+    ap.add_argument("--solvers", type=int, default=4, help="serving: MAC solver threads")
+    ap.add_argument("--solve-limit-ms", type=int, default=500, help="serving: MAC solve time limit")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "uneven":
         return run_uneven(args)
+    if args.workload == "serving":
+        return run_serving(args)
     return run_ours(args)
 
 

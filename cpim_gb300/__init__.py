@@ -121,6 +121,27 @@ def lib():
         "cp_batch_tune": ([vp], i),
         "cp_batch_info": ([vp, i, PI], i),
         "cp_batch_copy_level": ([vp, i], i),
+        "cp_batch_create_levels": ([vp, i, PV, PI, PV], i),
+        "cp_batch_load": ([vp, i, i, PI, PI, PI], i),
+        "cp_batch_dom_get": ([vp, P64], i),
+        "cp_server_create": ([vp, vp, i64, i, i, PV], i),
+        "cp_server_destroy": ([vp], i),
+        "cp_server_set_solve_limit": ([vp, i64], i),
+        "cp_server_set_solvers": ([vp, i], i),
+        "cp_engine_device": ([vp], i),
+        "cp_engine_set_priority": ([vp, i], i),
+        "cp_engine_set_cta_quota": ([vp, i], i),
+        "cp_submit_instance": ([vp, i, vp, C.POINTER(C.c_int64)], i),
+        "cp_wait": ([vp, i64, i64, vp], i),
+        "cp_result_domains": ([vp, i64, P64], i),
+        "cp_result_solution": ([vp, i64, PI], i),
+        "cp_release": ([vp, i64], i),
+        "cp_server_run_trace": ([vp, i, C.POINTER(C.c_double), vp, C.POINTER(C.c_double),
+                                 C.POINTER(C.c_int32), C.POINTER(C.c_double)], i),
+        "cp_server_register": ([vp, vp, i, C.POINTER(C.c_int64)], i),
+        "cp_server_unregister": ([vp, i64], i),
+        "cp_submit": ([vp, vp, C.POINTER(C.c_int64)], i),
+        "cp_cancel": ([vp, i64], i),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -232,6 +253,14 @@ class Engine:
     def set_tuning(self, block=0, chunk=0, ctas_per_sm=0):
         _check(lib().cp_engine_set_tuning(self._h, block, chunk, ctas_per_sm))
 
+    def set_priority(self, priority: int):
+        """Stream priority: -1 low, 0 default, 1 high (before any upload)."""
+        _check(lib().cp_engine_set_priority(self._h, int(priority)))
+
+    def set_cta_quota(self, quota: int):
+        """Batch sweep CTAs retire after `quota` units (0: persistent)."""
+        _check(lib().cp_engine_set_cta_quota(self._h, int(quota)))
+
     def set_sac_mode(self, mode: int):
         """0: tiled SAC sweep where eligible; 1: general per-branch kernel only."""
         _check(lib().cp_engine_set_sac_mode(self._h, mode))
@@ -341,12 +370,19 @@ class Net:
 class Batch:
     """Many independent networks propagated together (cp_batch_*)."""
 
-    def __init__(self, engine: Engine, nets, level: int = 0):
+    def __init__(self, engine: Engine, nets, level: int = 0, levels=None):
+        """levels: per-member working levels (one network may then appear
+        several times at distinct levels); default `level` for all."""
         self.engine = engine
         self.nets = list(nets)
         arr = (C.c_void_p * len(self.nets))(*[n._h.value for n in self.nets])
         self._h = C.c_void_p()
-        _check(lib().cp_batch_create(engine._h, len(self.nets), arr, level, C.byref(self._h)))
+        if levels is None:
+            _check(lib().cp_batch_create(engine._h, len(self.nets), arr, level, C.byref(self._h)))
+        else:
+            self._levels = np.ascontiguousarray(levels, dtype=np.int32)
+            _check(lib().cp_batch_create_levels(engine._h, len(self.nets), arr, _p(self._levels, C.c_int),
+                                                C.byref(self._h)))
 
     def close(self):
         if self._h:
@@ -380,6 +416,20 @@ class Batch:
     def copy_level(self, src: int):
         """Restores every member's batch level from level `src`."""
         _check(lib().cp_batch_copy_level(self._h, src))
+
+    def load(self, src_level: int, edits=()):
+        """Every member's working level := its level src_level, then each
+        (member, var, val) edit reduces that variable to the value."""
+        e = np.asarray(edits, dtype=np.int32).reshape(-1, 3)
+        m, v, a = (np.ascontiguousarray(e[:, j]) for j in range(3))
+        _check(lib().cp_batch_load(self._h, src_level, len(e), _p(m, C.c_int), _p(v, C.c_int), _p(a, C.c_int)))
+
+    def dom_get(self):
+        """Working domains of all members (list of per-member word arrays)."""
+        sizes = [n.n * n.W for n in self.nets]
+        out = np.zeros(sum(sizes), np.uint64)
+        _check(lib().cp_batch_dom_get(self._h, _p(out, C.c_uint64)))
+        return np.split(out, np.cumsum(sizes)[:-1])
 
     def info(self, group: int = 0):
         out = np.zeros(8, np.int32)
@@ -446,3 +496,163 @@ def _uneven_shape(seed, n_lo, n_hi, d_cap):
     choices = sum(1 for v in ds if v <= d_cap)
     d = ds[below(max(1, choices))]
     return n, d
+
+
+class Result(C.Structure):
+    _fields_ = [("status", C.c_int32), ("inconsistent", C.c_int32), ("deletions", C.c_int64),
+                ("num_positive", C.c_int64), ("num_negative", C.c_int64), ("mac_status", C.c_int32),
+                ("type", C.c_int32), ("queue_ms", C.c_double), ("latency_ms", C.c_double)]
+
+
+class Request(C.Structure):
+    """cp_request: type (0 propagate, 1 SAC, 2 MAC solve), choices, and either
+    a registered network id or an instance carried by the request."""
+    _fields_ = [("type", C.c_int32), ("n_choice", C.c_int32), ("net_id", C.c_int64), ("inst", C.c_void_p),
+                ("choice_var", C.POINTER(C.c_int)), ("choice_val", C.POINTER(C.c_int))]
+
+
+def _requests(reqs):
+    """(type, target, choices) tuples -> a cp_request array and the arrays it
+    points into. target: registered network id (int) or InstanceHandle."""
+    arr = (Request * len(reqs))()
+    keep = []
+    for r, (t, target, choices) in zip(arr, reqs):
+        r.type = int(t)
+        if isinstance(target, InstanceHandle):
+            r.net_id, r.inst = 0, target._h.value
+        else:
+            r.net_id, r.inst = int(target), None
+        ch = np.asarray(choices, dtype=np.int32).reshape(-1, 2)
+        v, a = np.ascontiguousarray(ch[:, 0]), np.ascontiguousarray(ch[:, 1])
+        keep += [v, a]
+        r.n_choice = len(ch)
+        r.choice_var = _p(v, C.c_int)
+        r.choice_val = _p(a, C.c_int)
+    return arr, keep
+
+
+class InstanceHandle:
+    """A generated instance kept in native memory (for server requests)."""
+
+    def __init__(self, h, n, W):
+        self._h, self.n, self.W = h, n, W
+
+    @staticmethod
+    def binary(n, d, e, p_lo, p_hi=None, remove=0.0, seed=1):
+        h = C.c_void_p()
+        _check(lib().cp_gen_binary(n, d, e, p_lo, p_lo if p_hi is None else p_hi, remove, seed, C.byref(h)))
+        return InstanceHandle(h, n, (d + 63) // 64)
+
+    @staticmethod
+    def uneven(seed, n_lo=20, n_hi=400, d_cap=256):
+        h = C.c_void_p()
+        _check(lib().cp_gen_uneven(seed, n_lo, n_hi, d_cap, C.byref(h)))
+        sz = (C.c_int64 * 8)()
+        _check(lib().cp_gen_sizes(h, sz))
+        return InstanceHandle(h, int(sz[0]), int(sz[1]))
+
+    def export(self) -> Instance:
+        L = lib()
+        sz = (C.c_int64 * 8)()
+        _check(L.cp_gen_sizes(self._h, sz))
+        n, W, nb, nt, nrows, nsc, ntup, fp = list(sz)
+        inst = Instance(n=n, W=W, dom=np.zeros(n, np.int32), init=np.zeros(n * W, np.uint64),
+                        bin_scope=np.zeros(2 * nb, np.int32), bin_rows=np.zeros(nrows, np.uint64),
+                        tab_arity=np.zeros(nt, np.int32), tab_scope=np.zeros(nsc, np.int32),
+                        tab_ntup=np.zeros(nt, np.int32), tab_tuples=np.zeros(ntup, np.int32),
+                        fingerprint="%016x" % (fp & 0xFFFFFFFFFFFFFFFF))
+        _check(L.cp_gen_export(self._h, _p(inst.dom, C.c_int), _p(inst.init, C.c_uint64),
+                               _p(inst.bin_scope, C.c_int), _p(inst.bin_rows, C.c_uint64),
+                               _p(inst.tab_arity, C.c_int), _p(inst.tab_scope, C.c_int), _p(inst.tab_ntup, C.c_int),
+                               _p(inst.tab_tuples, C.c_int)))
+        return inst
+
+    def __del__(self):
+        try:
+            if self._h:
+                lib().cp_gen_free(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching request server (cp_server_*). Request types:
+    0 propagate, 1 SAC, 2 MAC solve."""
+
+    def __init__(self, budget_bytes=150 * 10**9, max_batch=256, batching=True, device=0, solve_time_limit_ms=0,
+                 solvers=1):
+        self.eA, self.eB = Engine(device), Engine(device)
+        self._h = C.c_void_p()
+        _check(lib().cp_server_create(self.eA._h, self.eB._h, int(budget_bytes), max_batch, 1 if batching else 0,
+                                      C.byref(self._h)))
+        if solve_time_limit_ms:
+            _check(lib().cp_server_set_solve_limit(self._h, int(solve_time_limit_ms)))
+        if solvers > 1:
+            _check(lib().cp_server_set_solvers(self._h, int(solvers)))
+
+    def register(self, inst: InstanceHandle, slots: int = 8) -> int:
+        """Makes a network resident with `slots` working levels; returns its id."""
+        t = C.c_int64()
+        _check(lib().cp_server_register(self._h, inst._h, int(slots), C.byref(t)))
+        return t.value
+
+    def unregister(self, net_id: int):
+        _check(lib().cp_server_unregister(self._h, int(net_id)))
+
+    def submit(self, rtype: int, target, choices=()) -> int:
+        """target: an InstanceHandle (uploaded for the request) or a registered
+        network id; choices: (var, val) pairs fixed before the request runs."""
+        arr, keep = _requests([(rtype, target, choices)])
+        t = C.c_int64()
+        _check(lib().cp_submit(self._h, C.cast(arr, C.c_void_p), C.byref(t)))
+        return t.value
+
+    def cancel(self, ticket: int):
+        _check(lib().cp_cancel(self._h, ticket))
+
+    def wait(self, ticket: int, timeout_ms: int = 600000) -> Result:
+        r = Result()
+        _check(lib().cp_wait(self._h, ticket, timeout_ms, C.byref(r)))
+        return r
+
+    def domains(self, ticket: int, n: int, W: int) -> np.ndarray:
+        out = np.zeros(n * W, np.uint64)
+        _check(lib().cp_result_domains(self._h, ticket, _p(out, C.c_uint64)))
+        return out
+
+    def solution(self, ticket: int, n: int):
+        out = np.zeros(n, np.int32)
+        _check(lib().cp_result_solution(self._h, ticket, _p(out, C.c_int)))
+        return out.tolist()
+
+    def release(self, ticket: int):
+        _check(lib().cp_release(self._h, ticket))
+
+    def run_trace(self, arrivals_s, reqs):
+        """reqs: (type, target, choices) per request, submitted at arrivals_s
+        seconds; returns latencies (ms), statuses, and [ticks, batched
+        requests, wall seconds, peak admitted bytes, propagate-lane busy s,
+        SAC-lane busy s, solver busy s, MAC solves that hit the limit]."""
+        k = len(reqs)
+        arr = np.ascontiguousarray(arrivals_s, dtype=np.float64)
+        rq, keep = _requests(reqs)
+        lat = np.zeros(k, np.float64)
+        st = np.zeros(k, np.int32)
+        stats = np.zeros(8, np.float64)
+        _check(lib().cp_server_run_trace(self._h, k, _p(arr, C.c_double), C.cast(rq, C.c_void_p),
+                                         _p(lat, C.c_double), _p(st, C.c_int32), _p(stats, C.c_double)))
+        return lat, st, stats
+
+    def close(self):
+        if self._h:
+            lib().cp_server_destroy(self._h)
+            self._h = C.c_void_p()
+        self.eA.close()
+        self.eB.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -16,7 +16,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libcpgpu.so")
-SOURCES = ["cp_kernels.cu", "cp_engine.cu", "cp_static.cu"]
+SOURCES = ["cp_kernels.cu", "cp_engine.cu", "cp_static.cu", "cp_server.cpp"]
 HEADERS = ["cp_internal.h", "cp_gen.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
@@ -41,7 +41,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     objs = []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
+        o = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
         objs.append(o)
         if force or _stale(o, [s] + hdrs):
             jobs.append((s, o))
@@ -60,7 +60,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
             if verbose:
                 print("compiled", s)
     if force or jobs or _stale(LIB, objs):
-        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs
+        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))

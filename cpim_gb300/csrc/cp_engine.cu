@@ -9,7 +9,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -69,6 +71,90 @@ struct cp_engine {
   int chunk = 0;
   int ctas_per_sm = 0;
   int sac_mode = 0;  // 0: tiled sweep where eligible, 1: general kernel only
+  int cta_quota = 0;  // batch sweep CTAs retire after this many units (0: persistent)
+  int priority = 0;   // stream priority class: -1 low, 0 default, 1 high
+  // Device memory of this engine's networks and batches comes from a
+  // stream-ordered pool on the engine stream: allocation is a sub-allocation
+  // and release does not synchronise the device, which keeps per-request
+  // upload and teardown cheap while other streams run.
+  cudaMemPool_t pool = nullptr;
+  // Pinned host blocks by power-of-two size class, recycled across networks.
+  std::multimap<size_t, void*> pinned_free;
+
+  int dev_alloc(void** p, size_t bytes) {
+    // 256 extra bytes let the caller align the block's start.
+    cudaError_t err = cudaMallocFromPoolAsync(p, bytes, pool, stream);
+    if (err != cudaSuccess) {
+      cudaGetLastError();
+      return fail(err == cudaErrorMemoryAllocation ? CP_E_OOM : CP_E_CUDA,
+                  "device allocation of " + std::to_string(bytes) + " bytes: " + cudaGetErrorString(err));
+    }
+    return CP_OK;
+  }
+  void dev_free(void* p) {
+    if (p) cudaFreeAsync(p, stream);
+  }
+  static size_t pinned_class(size_t bytes) {
+    size_t c = 4096;
+    while (c < bytes) c <<= 1;
+    return c;
+  }
+  int pinned_get(size_t bytes, void** p) {
+    const size_t c = pinned_class(bytes);
+    auto it = pinned_free.find(c);
+    if (it != pinned_free.end()) {
+      *p = it->second;
+      pinned_free.erase(it);
+      return CP_OK;
+    }
+    cudaError_t err = cudaMallocHost(p, c);
+    if (err != cudaSuccess) {
+      cudaGetLastError();
+      return fail(CP_E_OOM, std::string("pinned host allocation: ") + cudaGetErrorString(err));
+    }
+    return CP_OK;
+  }
+  void pinned_put(void* p, size_t bytes) {
+    if (p) pinned_free.emplace(pinned_class(bytes), p);
+  }
+};
+
+// Several host arrays packed at 256-byte offsets of one block.
+struct MetaPack {
+  struct Part {
+    void** dst;
+    const void* src;
+    size_t bytes;
+    size_t off;
+  };
+  std::vector<Part> parts;
+  size_t total = 0;
+  template <typename T>
+  void add(T** dst, const T* src, size_t count) {
+    const size_t bytes = count * sizeof(T);
+    parts.push_back(Part{reinterpret_cast<void**>(dst), src, bytes, total});
+    total += (std::max<size_t>(bytes, 16) + 255) & ~size_t(255);
+  }
+};
+
+// A pinned host block borrowed from the engine for the duration of one call;
+// the engine stream is drained before the block goes back, so copies that
+// read from it have finished.
+struct PinnedLease {
+  cp_engine* e;
+  void* p = nullptr;
+  size_t bytes = 0;
+  explicit PinnedLease(cp_engine* eng) : e(eng) {}
+  int get(size_t n) {
+    bytes = n;
+    return e->pinned_get(n, &p);
+  }
+  ~PinnedLease() {
+    if (p) {
+      cudaStreamSynchronize(e->stream);
+      e->pinned_put(p, bytes);
+    }
+  }
 };
 
 struct cp_net {
@@ -106,33 +192,40 @@ struct cp_net {
   int64_t device_bytes = 0;
   int max_deg = 0;     // largest number of binary arcs at one variable
 
+  void* h_block = nullptr;  // pinned block holding h_stats, h_dom, h_sizes
+  size_t h_block_bytes = 0;
+
   ~cp_net() {
-    for (void* p : allocs) cudaFree(p);
-    if (h_stats) cudaFreeHost(h_stats);
-    if (h_dom) cudaFreeHost(h_dom);
-    if (h_sizes) cudaFreeHost(h_sizes);
-    if (e) --e->live_nets;
+    if (e) {
+      for (void* p : allocs) e->dev_free(p);
+      e->pinned_put(h_block, h_block_bytes);
+      --e->live_nets;
+    }
   }
 
+  // Allocations start on 256-byte boundaries (vector and bulk loads).
   template <typename T>
   int alloc(T** p, size_t count) {
     void* raw = nullptr;
-    const size_t bytes = std::max<size_t>(count * sizeof(T), 16);
-    cudaError_t e = cudaMalloc(&raw, bytes);
-    if (e != cudaSuccess) {
-      cudaGetLastError();
-      return fail(e == cudaErrorMemoryAllocation ? CP_E_OOM : CP_E_CUDA,
-                  "cudaMalloc of " + std::to_string(bytes) + " bytes: " + cudaGetErrorString(e));
-    }
+    const size_t bytes = (std::max<size_t>(count * sizeof(T), 16) + 255) & ~size_t(255);
+    CP_TRY(e->dev_alloc(&raw, bytes + 256));
     allocs.push_back(raw);
     device_bytes += static_cast<int64_t>(bytes);
-    *p = static_cast<T*>(raw);
+    *p = reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(raw) + 255) & ~uintptr_t(255));
     return CP_OK;
   }
   u64* level_ptr(int level) { return d_levels + static_cast<size_t>(level) * n * W; }
 };
 
 namespace {
+
+// Device-to-host copy ordered after everything queued on the engine stream.
+int d2h(cp_engine* e, void* dst, const void* src, size_t bytes) {
+  if (bytes == 0) return CP_OK;
+  CP_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, e->stream));
+  CP_CUDA(cudaStreamSynchronize(e->stream));
+  return CP_OK;
+}
 
 // ---- stats --------------------------------------------------------------
 int stats_begin(cp_net* net) {
@@ -253,6 +346,13 @@ int cp_engine_create(int device, cp_engine** out) {
   e->sm_count = prop.multiProcessorCount;
   e->smem_optin = prop.sharedMemPerBlockOptin;
   CP_CUDA(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+  cudaMemPoolProps props{};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = device;
+  CP_CUDA(cudaMemPoolCreate(&e->pool, &props));
+  uint64_t keep = UINT64_MAX;  // freed blocks stay in the pool for the next network
+  CP_CUDA(cudaMemPoolSetAttribute(e->pool, cudaMemPoolAttrReleaseThreshold, &keep));
   CP_CUDA(cudaEventCreate(&e->ev0));
   CP_CUDA(cudaEventCreate(&e->ev1));
   CP_CUDA(cudaEventCreate(&e->evk0));
@@ -266,6 +366,8 @@ int cp_engine_create(int device, cp_engine** out) {
 static void engine_free(cp_engine* e) {
   cudaSetDevice(e->device);
   if (e->stream) cudaStreamSynchronize(e->stream);
+  for (auto& kv : e->pinned_free) cudaFreeHost(kv.second);
+  if (e->pool) cudaMemPoolDestroy(e->pool);
   if (e->ev0) cudaEventDestroy(e->ev0);
   if (e->ev1) cudaEventDestroy(e->ev1);
   if (e->evk0) cudaEventDestroy(e->evk0);
@@ -283,6 +385,7 @@ int cp_engine_destroy(cp_engine* e) {
 }
 
 int64_t cp_engine_launches(const cp_engine* e) { return e ? e->launches : 0; }
+int cp_engine_device(const cp_engine* e) { return e ? e->device : -1; }
 
 int cp_engine_set_tuning(cp_engine* e, int block, int chunk, int ctas_per_sm) {
   if (!e) return fail(CP_E_ARG, "null engine");
@@ -301,6 +404,30 @@ int cp_engine_set_sac_mode(cp_engine* e, int mode) {
   if (!e) return fail(CP_E_ARG, "null engine");
   if (mode != 0 && mode != 1) return fail(CP_E_ARG, "SAC mode must be 0 (tiled where eligible) or 1 (general)");
   e->sac_mode = mode;
+  return CP_OK;
+}
+
+int cp_engine_set_priority(cp_engine* e, int priority) {
+  if (!e) return fail(CP_E_ARG, "null engine");
+  if (priority < -1 || priority > 1) return fail(CP_E_ARG, "priority must be -1, 0 or 1");
+  if (e->live_nets > 0) return fail(CP_E_STATE, "stream priority is set before any network is uploaded");
+  CP_CUDA(cudaSetDevice(e->device));
+  int least = 0, greatest = 0;
+  CP_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+  const int p = priority > 0 ? greatest : (priority < 0 ? least : 0);
+  cudaStream_t ns = nullptr;
+  CP_CUDA(cudaStreamCreateWithPriority(&ns, cudaStreamNonBlocking, p));
+  CP_CUDA(cudaStreamSynchronize(e->stream));
+  CP_CUDA(cudaStreamDestroy(e->stream));
+  e->stream = ns;
+  e->priority = priority;
+  return CP_OK;
+}
+
+int cp_engine_set_cta_quota(cp_engine* e, int quota) {
+  if (!e) return fail(CP_E_ARG, "null engine");
+  if (quota < 0) return fail(CP_E_ARG, "negative quota");
+  e->cta_quota = quota;
   return CP_OK;
 }
 
@@ -447,41 +574,33 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   int *d_tar, *d_tsc, *d_tnt;
   int64_t* d_toff;
   uint16_t* d_ttup;
-  CP_TRY(net->alloc(&d_dsize, n));
-  CP_TRY(net->alloc(&d_arc_start, n + 1));
-  CP_TRY(net->alloc(&d_arcs, arcs.size()));
-  CP_TRY(net->alloc(&d_tinc, n + 1));
-  CP_TRY(net->alloc(&d_vtab, vtab.size()));
-  CP_TRY(net->alloc(&d_tar, n_tab));
-  CP_TRY(net->alloc(&d_tsc, t_scope.size()));
-  CP_TRY(net->alloc(&d_tnt, n_tab));
-  CP_TRY(net->alloc(&d_toff, n_tab));
-  CP_TRY(net->alloc(&d_ttup, t_tup.size()));
+  // Metadata arrays: one device block, filled by one copy from pinned staging.
+  MetaPack mp;
+  mp.add(&d_dsize, dom, n);
+  mp.add(&d_arc_start, arc_start.data(), n + 1);
+  mp.add(&d_arcs, arcs.data(), arcs.size());
+  mp.add(&d_tinc, tinc_start.data(), n + 1);
+  mp.add(&d_vtab, vtab.data(), vtab.size());
+  mp.add(&d_tar, t_arity.data(), n_tab);
+  mp.add(&d_tsc, t_scope.data(), t_scope.size());
+  mp.add(&d_tnt, t_ntup.data(), n_tab);
+  mp.add(&d_toff, t_off.data(), n_tab);
+  mp.add(&d_ttup, t_tup.data(), t_tup.size());
+  mp.add(&net->d_bx, net->bx.data(), n_bin);
+  mp.add(&net->d_by, net->by.data(), n_bin);
+  mp.add(&net->d_offA, offA.data(), n_bin);
+  mp.add(&net->d_offB, offB.data(), n_bin);
+  char* d_meta = nullptr;
+  CP_TRY(net->alloc(&d_meta, mp.total));
+  PinnedLease stage(e);
+  CP_TRY(stage.get(mp.total));
+  for (const auto& q : mp.parts) {
+    if (q.bytes) std::memcpy(static_cast<char*>(stage.p) + q.off, q.src, q.bytes);
+    *q.dst = d_meta + q.off;
+  }
+  CP_CUDA(cudaMemcpyAsync(d_meta, stage.p, mp.total, cudaMemcpyHostToDevice, s));
   CP_TRY(net->alloc(&net->d_rel, static_cast<size_t>(ta + tb)));
-  CP_TRY(net->alloc(&net->d_bx, n_bin));
-  CP_TRY(net->alloc(&net->d_by, n_bin));
-  CP_TRY(net->alloc(&net->d_offA, n_bin));
-  CP_TRY(net->alloc(&net->d_offB, n_bin));
   CP_TRY(net->alloc(&net->d_levels, static_cast<size_t>(net->levels) * n * Wi));
-  CP_CUDA(cudaMemcpyAsync(d_dsize, dom, n * sizeof(int), cudaMemcpyHostToDevice, s));
-  CP_CUDA(cudaMemcpyAsync(d_arc_start, arc_start.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
-  if (!arcs.empty()) CP_CUDA(cudaMemcpyAsync(d_arcs, arcs.data(), arcs.size() * sizeof(Arc), cudaMemcpyHostToDevice, s));
-  CP_CUDA(cudaMemcpyAsync(d_tinc, tinc_start.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
-  if (!vtab.empty()) CP_CUDA(cudaMemcpyAsync(d_vtab, vtab.data(), vtab.size() * sizeof(int), cudaMemcpyHostToDevice, s));
-  if (n_tab) {
-    CP_CUDA(cudaMemcpyAsync(d_tar, t_arity.data(), n_tab * sizeof(int), cudaMemcpyHostToDevice, s));
-    CP_CUDA(cudaMemcpyAsync(d_tsc, t_scope.data(), t_scope.size() * sizeof(int), cudaMemcpyHostToDevice, s));
-    CP_CUDA(cudaMemcpyAsync(d_tnt, t_ntup.data(), n_tab * sizeof(int), cudaMemcpyHostToDevice, s));
-    CP_CUDA(cudaMemcpyAsync(d_toff, t_off.data(), n_tab * sizeof(int64_t), cudaMemcpyHostToDevice, s));
-    if (!t_tup.empty())
-      CP_CUDA(cudaMemcpyAsync(d_ttup, t_tup.data(), t_tup.size() * sizeof(uint16_t), cudaMemcpyHostToDevice, s));
-  }
-  if (n_bin) {
-    CP_CUDA(cudaMemcpyAsync(net->d_bx, net->bx.data(), n_bin * sizeof(int), cudaMemcpyHostToDevice, s));
-    CP_CUDA(cudaMemcpyAsync(net->d_by, net->by.data(), n_bin * sizeof(int), cudaMemcpyHostToDevice, s));
-    CP_CUDA(cudaMemcpyAsync(net->d_offA, offA.data(), n_bin * sizeof(int64_t), cudaMemcpyHostToDevice, s));
-    CP_CUDA(cudaMemcpyAsync(net->d_offB, offB.data(), n_bin * sizeof(int64_t), cudaMemcpyHostToDevice, s));
-  }
   D.dsize = d_dsize;
   D.arc_start = d_arc_start;
   D.arcs = d_arcs;
@@ -525,9 +644,16 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   CP_TRY(net->alloc(&net->d_evt, n));
   CP_TRY(net->alloc(&net->d_sizes, n));
   CP_TRY(net->alloc(&net->d_ok1, total_values));
-  CP_CUDA(cudaMallocHost(reinterpret_cast<void**>(&net->h_stats), sizeof(KStats)));
-  CP_CUDA(cudaMallocHost(reinterpret_cast<void**>(&net->h_dom), static_cast<size_t>(n) * Wi * 8));
-  CP_CUDA(cudaMallocHost(reinterpret_cast<void**>(&net->h_sizes), static_cast<size_t>(n) * sizeof(int)));
+  {
+    const size_t st_bytes = (sizeof(KStats) + 255) & ~size_t(255);
+    const size_t dom_bytes = (static_cast<size_t>(n) * Wi * 8 + 255) & ~size_t(255);
+    net->h_block_bytes = st_bytes + dom_bytes + static_cast<size_t>(n) * sizeof(int);
+    CP_TRY(e->pinned_get(net->h_block_bytes, &net->h_block));
+    char* hb = static_cast<char*>(net->h_block);
+    net->h_stats = reinterpret_cast<KStats*>(hb);
+    net->h_dom = reinterpret_cast<u64*>(hb + st_bytes);
+    net->h_sizes = reinterpret_cast<int*>(hb + st_bytes + dom_bytes);
+  }
 
   // CTA-local state: shared memory when it fits, else global scratch.
   const size_t cta_bytes = cta_state_bytes(D);
@@ -1249,8 +1375,10 @@ static int upload_generated(cp_engine* e, const cpgen::Instance& I, int max_leve
   if (I.n_bin() > 0) {
     u64* d_seed = nullptr;
     u32* d_thr = nullptr;
-    cudaError_t err = cudaMalloc(&d_seed, I.bseed.size() * sizeof(u64));
-    if (err == cudaSuccess) err = cudaMalloc(&d_thr, I.bthr.size() * sizeof(u32));
+    cudaError_t err = cudaMallocFromPoolAsync(reinterpret_cast<void**>(&d_seed), I.bseed.size() * sizeof(u64),
+                                              e->pool, e->stream);
+    if (err == cudaSuccess)
+      err = cudaMallocFromPoolAsync(reinterpret_cast<void**>(&d_thr), I.bthr.size() * sizeof(u32), e->pool, e->stream);
     if (err == cudaSuccess)
       err = cudaMemcpyAsync(d_seed, I.bseed.data(), I.bseed.size() * sizeof(u64), cudaMemcpyHostToDevice, e->stream);
     if (err == cudaSuccess)
@@ -1264,8 +1392,8 @@ static int upload_generated(cp_engine* e, const cpgen::Instance& I, int max_leve
     }
     if (err == cudaSuccess) err = cudaStreamSynchronize(e->stream);
     e->launches += 2;
-    cudaFree(d_seed);
-    cudaFree(d_thr);
+    e->dev_free(d_seed);
+    e->dev_free(d_thr);
     if (err != cudaSuccess) {
       cp_net_destroy(net);
       return fail(CP_E_CUDA, std::string("device generator: ") + cudaGetErrorString(err));
@@ -1297,7 +1425,7 @@ int cp_net_rows_get(cp_net* net, uint64_t* out) {
   if (!net || !out) return fail(CP_E_ARG, "null argument");
   const int W = net->W_user, Wi = net->W;
   std::vector<u64> rows(static_cast<size_t>(net->relA_words));
-  CP_CUDA(cudaMemcpy(rows.data(), net->d_rel, rows.size() * 8, cudaMemcpyDeviceToHost));
+  CP_TRY(d2h(net->e, rows.data(), net->d_rel, rows.size() * 8));
   int64_t src = 0, dst = 0;
   for (int c = 0; c < net->nb; ++c)
     for (int a = 0; a < net->dom[net->bx[c]]; ++a) {
@@ -1345,6 +1473,8 @@ struct BatchGroup {
   int sac_grid = 0;
   int sac_block = 256;
   int64_t total_values = 0;
+  int64_t tiles_upper = 0;  // sum over members' variables of ceil(d / 32)
+  int quota = 0;            // CTA quota of the sweep kernels (0: persistent grids)
   cudaGraphExec_t exec = nullptr;
   std::string key;  // autotuner cache key
 };
@@ -1356,25 +1486,42 @@ std::string tune_cache_path() {
   return std::string(h && *h ? h : "/tmp") + "/.cache/cpgpu_tune.txt";
 }
 
-// Cache lines: "<key> <tiled> <sac_block>".
-bool tune_lookup(const std::string& key, bool& tiled, int& block) {
-  FILE* f = std::fopen(tune_cache_path().c_str(), "r");
-  if (!f) return false;
+// Cache lines: "<key> <tiled> <sac_block>"; the last line of a key wins. The
+// file is read once per path and kept in memory (batches are created per
+// request tick by the server).
+std::mutex g_tune_mu;
+std::string g_tune_path;
+std::map<std::string, std::pair<bool, int>> g_tune;
+
+void tune_load_locked(const std::string& path) {
+  if (path == g_tune_path) return;
+  g_tune_path = path;
+  g_tune.clear();
+  FILE* f = std::fopen(path.c_str(), "r");
+  if (!f) return;
   char k[256];
   int t = 0, b = 0;
-  bool found = false;
-  while (std::fscanf(f, "%255s %d %d", k, &t, &b) == 3)
-    if (key == k) {
-      tiled = t != 0;
-      block = b;
-      found = true;
-    }
+  while (std::fscanf(f, "%255s %d %d", k, &t, &b) == 3) g_tune[k] = {t != 0, b};
   std::fclose(f);
-  return found;
+}
+
+bool tune_lookup(const std::string& key, bool& tiled, int& block) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  tune_load_locked(tune_cache_path());
+  auto it = g_tune.find(key);
+  if (it == g_tune.end()) return false;
+  tiled = it->second.first;
+  block = it->second.second;
+  return true;
 }
 
 void tune_store(const std::string& key, bool tiled, int block) {
   const std::string path = tune_cache_path();
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    tune_load_locked(path);
+    g_tune[key] = {tiled, block};
+  }
   const size_t slash = path.rfind('/');
   if (slash != std::string::npos) {
     const std::string dir = path.substr(0, slash);
@@ -1395,32 +1542,34 @@ void tune_store(const std::string& key, bool tiled, int block) {
 struct cp_batch {
   cp_engine* e = nullptr;
   int k = 0;
-  int level = 0;
+  std::vector<int> levels;  // working level of each member
   std::vector<cp_net*> nets;
+  std::vector<std::pair<int, int>> where;  // member -> (group, index in the group)
+  std::vector<int64_t> out_off;            // member -> word offset in a gathered domain buffer
+  int64_t gather_words = 0;
+  u64* d_gather = nullptr;
+  int* d_edit = nullptr;  // member / var / val lists of cp_batch_load
+  int64_t edit_cap = 0;
   std::vector<BatchGroup> groups;
   std::vector<void*> allocs;
   KStats* d_stats = nullptr;
   KStats* h_stats = nullptr;
   int* h_int = nullptr;
   bool use_graph = true;
+  void* h_block = nullptr;  // pinned: h_stats, h_int
   ~cp_batch() {
     for (auto& g : groups)
       if (g.exec) cudaGraphExecDestroy(g.exec);
-    for (void* p : allocs) cudaFree(p);
-    if (h_stats) cudaFreeHost(h_stats);
-    if (h_int) cudaFreeHost(h_int);
+    for (void* p : allocs) e->dev_free(p);
+    e->pinned_put(h_block, 512);
   }
   template <typename T>
   int alloc(T** p, size_t count) {
     void* raw = nullptr;
-    cudaError_t err = cudaMalloc(&raw, std::max<size_t>(count * sizeof(T), 16));
-    if (err != cudaSuccess) {
-      cudaGetLastError();
-      return fail(err == cudaErrorMemoryAllocation ? CP_E_OOM : CP_E_CUDA,
-                  std::string("batch cudaMalloc: ") + cudaGetErrorString(err));
-    }
+    const size_t bytes = (std::max<size_t>(count * sizeof(T), 16) + 255) & ~size_t(255);
+    CP_TRY(e->dev_alloc(&raw, bytes + 256));
     allocs.push_back(raw);
-    *p = static_cast<T*>(raw);
+    *p = reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(raw) + 255) & ~uintptr_t(255));
     return CP_OK;
   }
 };
@@ -1432,7 +1581,9 @@ int batch_group_setup(cp_batch* b, BatchGroup& g) {
   cudaStream_t s = e->stream;
   const int kg = static_cast<int>(g.members.size());
   std::vector<DevNet> nets(kg);
-  std::vector<u64*> roots(kg);
+  std::vector<u64*> roots(kg), bases(kg);
+  std::vector<int64_t> offs(kg);
+  std::vector<int> wuser(kg);
   std::vector<int> var_base(kg + 1, 0);
   int max_deg = 1;
   g.cta_bytes = 0;
@@ -1440,14 +1591,16 @@ int batch_group_setup(cp_batch* b, BatchGroup& g) {
   for (int i = 0; i < kg; ++i) {
     cp_net* n = b->nets[g.members[i]];
     nets[i] = n->dn;
-    roots[i] = n->level_ptr(b->level);
+    roots[i] = n->level_ptr(b->levels[g.members[i]]);
+    bases[i] = n->d_levels;
+    offs[i] = b->out_off[g.members[i]];
+    wuser[i] = n->W_user;
     var_base[i + 1] = var_base[i] + n->n;
     g.max_n = std::max(g.max_n, n->n);
     g.cta_bytes = std::max(g.cta_bytes, cta_state_bytes(n->dn));
     g.total_values += n->dn.total_values;
-    std::vector<int> deg(n->n + 1);
-    CP_CUDA(cudaMemcpy(deg.data(), n->dn.arc_start, (n->n + 1) * sizeof(int), cudaMemcpyDeviceToHost));
-    for (int x = 0; x < n->n; ++x) max_deg = std::max(max_deg, deg[x + 1] - deg[x]);
+    for (int d : n->dom) g.tiles_upper += (d + 31) / 32;
+    max_deg = std::max(max_deg, n->max_deg);
   }
   const int tv = var_base[kg];
   std::vector<int> var_inst(tv);
@@ -1456,19 +1609,34 @@ int batch_group_setup(cp_batch* b, BatchGroup& g) {
   BatchDev& B = g.B;
   B.k = kg;
   B.total_vars = tv;
+  // Member descriptors: one device block, one copy from pinned staging.
   DevNet* d_nets;
   u64** d_roots;
-  int *d_vb, *d_vi;
-  CP_TRY(b->alloc(&d_nets, kg));
-  CP_TRY(b->alloc(&d_roots, kg));
-  CP_TRY(b->alloc(&d_vb, kg + 1));
-  CP_TRY(b->alloc(&d_vi, tv));
-  CP_CUDA(cudaMemcpyAsync(d_nets, nets.data(), kg * sizeof(DevNet), cudaMemcpyHostToDevice, s));
-  CP_CUDA(cudaMemcpyAsync(d_roots, roots.data(), kg * sizeof(u64*), cudaMemcpyHostToDevice, s));
-  CP_CUDA(cudaMemcpyAsync(d_vb, var_base.data(), (kg + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
-  CP_CUDA(cudaMemcpyAsync(d_vi, var_inst.data(), tv * sizeof(int), cudaMemcpyHostToDevice, s));
+  u64** d_bases;
+  int64_t* d_offs;
+  int *d_vb, *d_vi, *d_wu;
+  MetaPack mp;
+  mp.add(&d_nets, nets.data(), kg);
+  mp.add(&d_roots, roots.data(), kg);
+  mp.add(&d_bases, bases.data(), kg);
+  mp.add(&d_offs, offs.data(), kg);
+  mp.add(&d_wu, wuser.data(), kg);
+  mp.add(&d_vb, var_base.data(), kg + 1);
+  mp.add(&d_vi, var_inst.data(), tv);
+  char* d_meta = nullptr;
+  CP_TRY(b->alloc(&d_meta, mp.total));
+  PinnedLease stage(e);
+  CP_TRY(stage.get(mp.total));
+  for (const auto& q : mp.parts) {
+    if (q.bytes) std::memcpy(static_cast<char*>(stage.p) + q.off, q.src, q.bytes);
+    *q.dst = d_meta + q.off;
+  }
+  CP_CUDA(cudaMemcpyAsync(d_meta, stage.p, mp.total, cudaMemcpyHostToDevice, s));
   B.nets = d_nets;
   B.roots = d_roots;
+  B.bases = d_bases;
+  B.out_off = d_offs;
+  B.wuser = d_wu;
   B.var_base = d_vb;
   B.var_inst = d_vi;
   CP_TRY(b->alloc(&B.inc, kg));
@@ -1490,6 +1658,8 @@ int batch_group_setup(cp_batch* b, BatchGroup& g) {
   CP_TRY(b->alloc(&B.ndeep, 4));
   // CTA-local state: shared memory when it fits.
   g.cta_smem = g.cta_bytes + 2048 <= e->smem_optin;
+  // Per-CTA global scratch is indexed by CTA: quotas need shared-memory state.
+  g.quota = g.cta_smem ? e->cta_quota : 0;
   const size_t smem = g.cta_smem ? g.cta_bytes : 0;
   int per_sm_node = batch_node_blocks_per_sm(g.W, g.tables, e->block_node, smem);
   int per_sm_sac = batch_sac_blocks_per_sm(g.W, g.tables, g.sac_block, smem);
@@ -1555,11 +1725,19 @@ int batch_sweep_launches(cp_batch* b, BatchGroup& g, bool with_commit) {
   CP_CUDA(cudaMemsetAsync(B.evt_fb, 0, ((B.total_vars + 31) / 32) * sizeof(u32), s));
   const size_t smem = g.cta_smem ? g.cta_bytes : 0;
   CP_CUDA(launch_batch_build(g.W, B, g.tiled, s));
+  // With a CTA quota the grids cover every tile / branch (upper bounds); CTAs
+  // past the actual count retire at once.
+  const int q = g.quota;
+  auto cover = [&](int64_t units, int persistent) {
+    return q > 0 ? static_cast<int>(std::min<int64_t>((units + q - 1) / q, int64_t(1) << 30)) : persistent;
+  };
   if (g.tiled) {
-    CP_CUDA(launch_batch_tile(g.W, B, g.slot_cap, g.max_n, b->d_stats, g.tile_grid, s));
-    CP_CUDA(launch_batch_sac(g.W, g.tables, B, true, b->d_stats, g.sac_block, g.sac_grid, smem, g.gscratch, g.gstride, s));
+    CP_CUDA(launch_batch_tile(g.W, B, g.slot_cap, g.max_n, b->d_stats, cover(g.tiles_upper, g.tile_grid), q, s));
+    CP_CUDA(launch_batch_sac(g.W, g.tables, B, true, b->d_stats, g.sac_block, cover(g.total_values, g.sac_grid), smem,
+                             g.gscratch, g.gstride, q, s));
   } else {
-    CP_CUDA(launch_batch_sac(g.W, g.tables, B, false, b->d_stats, g.sac_block, g.sac_grid, smem, g.gscratch, g.gstride, s));
+    CP_CUDA(launch_batch_sac(g.W, g.tables, B, false, b->d_stats, g.sac_block, cover(g.total_values, g.sac_grid), smem,
+                             g.gscratch, g.gstride, q, s));
   }
   e->launches += g.tiled ? 3 : 2;
   if (with_commit) {
@@ -1613,7 +1791,7 @@ int batch_finish(cp_batch* b, cp_stats* st, uint8_t* inconsistent, int sweeps, i
   if (inconsistent) {
     for (auto& g : b->groups) {
       std::vector<uint8_t> inc(g.B.k);
-      CP_CUDA(cudaMemcpy(inc.data(), g.B.inc, g.B.k, cudaMemcpyDeviceToHost));
+      CP_TRY(d2h(e, inc.data(), g.B.inc, g.B.k));
       for (int i = 0; i < g.B.k; ++i) inconsistent[g.members[i]] = inc[i];
     }
   }
@@ -1632,7 +1810,7 @@ int batch_finish(cp_batch* b, cp_stats* st, uint8_t* inconsistent, int sweeps, i
     int ninc = 0;
     for (auto& g : b->groups) {
       std::vector<uint8_t> inc(g.B.k);
-      CP_CUDA(cudaMemcpy(inc.data(), g.B.inc, g.B.k, cudaMemcpyDeviceToHost));
+      CP_TRY(d2h(e, inc.data(), g.B.inc, g.B.k));
       for (uint8_t v : inc) ninc += v;
     }
     s.inconsistent = ninc;
@@ -1646,18 +1824,36 @@ int batch_finish(cp_batch* b, cp_stats* st, uint8_t* inconsistent, int sweeps, i
 extern "C" {
 
 int cp_batch_create(cp_engine* e, int k, cp_net* const* nets, int level, cp_batch** out) {
-  if (!e || !out || k < 1 || !nets) return fail(CP_E_ARG, "bad batch arguments");
+  if (k < 1 || k >= 32768) return fail(CP_E_UNSUPPORTED, "a batch holds 1 to 32767 instances");
+  std::vector<int> levels(static_cast<size_t>(k), level);
+  return cp_batch_create_levels(e, k, nets, levels.data(), out);
+}
+
+int cp_batch_create_levels(cp_engine* e, int k, cp_net* const* nets, const int* levels, cp_batch** out) {
+  if (!e || !out || k < 1 || !nets || !levels) return fail(CP_E_ARG, "bad batch arguments");
   if (k >= 32768) return fail(CP_E_UNSUPPORTED, "at most 32767 instances per batch");
+  CP_CUDA(cudaSetDevice(e->device));
   auto b = std::make_unique<cp_batch>();
   b->e = e;
   b->k = k;
-  b->level = level;
+  b->levels.assign(levels, levels + k);
   b->nets.assign(nets, nets + k);
+  b->out_off.resize(k);
+  std::vector<std::pair<const cp_net*, int>> seen;
   for (int i = 0; i < k; ++i) {
-    if (!nets[i] || nets[i]->e != e) return fail(CP_E_ARG, "batch member not uploaded on this engine");
+    // Members may live on another engine of the same device: the batch only
+    // reads their relations and writes their working levels, in the batch
+    // engine's stream order; the caller keeps other users off those levels.
+    if (!nets[i] || nets[i]->e->device != e->device) return fail(CP_E_ARG, "batch member on another device");
     if (nets[i]->n >= 65536) return fail(CP_E_UNSUPPORTED, "batch members need n < 65536");
-    if (level < 0 || level >= nets[i]->levels) return fail(CP_E_ARG, "level out of range for a batch member");
+    if (levels[i] < 0 || levels[i] >= nets[i]->levels) return fail(CP_E_ARG, "level out of range for a batch member");
+    seen.emplace_back(nets[i], levels[i]);
+    b->out_off[i] = b->gather_words;
+    b->gather_words += static_cast<int64_t>(nets[i]->n) * nets[i]->W_user;
   }
+  std::sort(seen.begin(), seen.end());
+  if (std::adjacent_find(seen.begin(), seen.end()) != seen.end())
+    return fail(CP_E_ARG, "two batch members share a network level");
   for (int i = 0; i < k; ++i) {
     const int W = nets[i]->W;
     const bool tab = nets[i]->nt > 0;
@@ -1677,8 +1873,14 @@ int cp_batch_create(cp_engine* e, int k, cp_net* const* nets, int level, cp_batc
     }
     g->members.push_back(i);
   }
-  CP_CUDA(cudaMallocHost(reinterpret_cast<void**>(&b->h_stats), sizeof(KStats)));
-  CP_CUDA(cudaMallocHost(reinterpret_cast<void**>(&b->h_int), 4 * sizeof(int)));
+  b->where.resize(k);
+  for (size_t gi = 0; gi < b->groups.size(); ++gi)
+    for (size_t j = 0; j < b->groups[gi].members.size(); ++j)
+      b->where[b->groups[gi].members[j]] = {static_cast<int>(gi), static_cast<int>(j)};
+  static_assert(sizeof(KStats) <= 256, "batch pinned block layout");
+  CP_TRY(e->pinned_get(512, &b->h_block));
+  b->h_stats = static_cast<KStats*>(b->h_block);
+  b->h_int = reinterpret_cast<int*>(static_cast<char*>(b->h_block) + 256);
   CP_TRY(b->alloc(&b->d_stats, 1));
   for (auto& g : b->groups) CP_TRY(batch_group_setup(b.get(), g));
   ++e->live_nets;
@@ -1806,15 +2008,67 @@ int cp_batch_tune(cp_batch* b) {
   return CP_OK;
 }
 
-int cp_batch_copy_level(cp_batch* b, int src) {
+int cp_batch_copy_level(cp_batch* b, int src) { return cp_batch_load(b, src, 0, nullptr, nullptr, nullptr); }
+
+int cp_batch_load(cp_batch* b, int src_level, int n_edit, const int* member, const int* var, const int* val) {
   if (!b) return fail(CP_E_ARG, "null batch");
+  if (n_edit < 0 || (n_edit > 0 && (!member || !var || !val))) return fail(CP_E_ARG, "bad edit list");
   for (cp_net* n : b->nets)
-    if (src < 0 || src >= n->levels) return fail(CP_E_ARG, "source level out of range for a batch member");
-  for (auto& g : b->groups) {
-    CP_CUDA(launch_batch_copy(g.W, g.B, src - b->level, b->e->stream));
-    ++b->e->launches;
+    if (src_level < 0 || src_level >= n->levels) return fail(CP_E_ARG, "source level out of range for a batch member");
+  for (int j = 0; j < n_edit; ++j) {
+    if (member[j] < 0 || member[j] >= b->k) return fail(CP_E_ARG, "edit member out of range");
+    CP_TRY(check_var_val(b->nets[member[j]], var[j], val[j]));
   }
-  CP_CUDA(cudaStreamSynchronize(b->e->stream));
+  cp_engine* e = b->e;
+  cudaStream_t s = e->stream;
+  for (auto& g : b->groups) {
+    CP_CUDA(launch_batch_copy(g.W, g.B, src_level, s));
+    ++e->launches;
+  }
+  if (n_edit > 0) {
+    if (n_edit > b->edit_cap) {  // a smaller earlier list buffer stays until the batch goes
+      b->edit_cap = std::max<int64_t>(n_edit, 2 * b->edit_cap);
+      CP_TRY(b->alloc(&b->d_edit, 3 * static_cast<size_t>(b->edit_cap)));
+    }
+    // Edits ordered by group: [member in group | var | val] per group.
+    const int ng = static_cast<int>(b->groups.size());
+    std::vector<int> cnt(ng + 1, 0);
+    for (int j = 0; j < n_edit; ++j) ++cnt[b->where[member[j]].first + 1];
+    for (int gi = 0; gi < ng; ++gi) cnt[gi + 1] += cnt[gi];
+    PinnedLease stage(e);
+    CP_TRY(stage.get(3 * sizeof(int) * static_cast<size_t>(n_edit)));
+    int* h = static_cast<int*>(stage.p);
+    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+    for (int j = 0; j < n_edit; ++j) {
+      const auto& w = b->where[member[j]];
+      const int at = fill[w.first]++;
+      h[at] = w.second;
+      h[n_edit + at] = var[j];
+      h[2 * n_edit + at] = val[j];
+    }
+    CP_CUDA(cudaMemcpyAsync(b->d_edit, h, 3 * sizeof(int) * static_cast<size_t>(n_edit), cudaMemcpyHostToDevice, s));
+    for (int gi = 0; gi < ng; ++gi) {
+      const int c = cnt[gi + 1] - cnt[gi];
+      if (c == 0) continue;
+      const int o = cnt[gi];
+      CP_CUDA(launch_batch_edit(b->groups[gi].W, b->groups[gi].B, c, b->d_edit + o, b->d_edit + n_edit + o,
+                                b->d_edit + 2 * n_edit + o, s));
+      ++e->launches;
+    }
+  }
+  CP_CUDA(cudaStreamSynchronize(s));
+  return CP_OK;
+}
+
+int cp_batch_dom_get(cp_batch* b, uint64_t* out) {
+  if (!b || !out) return fail(CP_E_ARG, "null argument");
+  cp_engine* e = b->e;
+  if (!b->d_gather) CP_TRY(b->alloc(&b->d_gather, static_cast<size_t>(std::max<int64_t>(1, b->gather_words))));
+  for (auto& g : b->groups) {
+    CP_CUDA(launch_batch_gather(g.W, g.B, b->d_gather, e->stream));
+    ++e->launches;
+  }
+  CP_TRY(d2h(e, out, b->d_gather, static_cast<size_t>(b->gather_words) * 8));
   return CP_OK;
 }
 

@@ -111,6 +111,9 @@ struct BatchDev {
   int total_vars = 0;            // sum of n over instances
   const DevNet* nets = nullptr;  // [k]
   u64* const* roots = nullptr;   // [k] level each instance works on
+  u64* const* bases = nullptr;   // [k] level 0 of each instance's level stack
+  const int64_t* out_off = nullptr;  // [k] word offset of the instance in a gathered domain buffer
+  const int* wuser = nullptr;    // [k] caller's words per domain (<= W)
   const int* var_base = nullptr; // [k+1] global id of each instance's variable 0
   const int* var_inst = nullptr; // [total_vars] instance of each global variable
   uint8_t* inc = nullptr;        // [k] 1 once known inconsistent
@@ -137,16 +140,20 @@ cudaError_t launch_batch_node(int W, bool tables, const BatchDev& B, int op, KSt
                               size_t smem, void* gscratch, size_t gstride, cudaStream_t s);
 int batch_node_blocks_per_sm(int W, bool tables, int block, size_t smem);
 cudaError_t launch_batch_build(int W, const BatchDev& B, bool with_tiles, cudaStream_t s);
-cudaError_t launch_batch_tile(int W, const BatchDev& B, int slot_cap, int max_n, KStats* st, int grid, cudaStream_t s);
+cudaError_t launch_batch_tile(int W, const BatchDev& B, int slot_cap, int max_n, KStats* st, int grid, int quota,
+                              cudaStream_t s);
 size_t batch_tile_smem(int W, int slot_cap, int max_n);
 int batch_tile_blocks_per_sm(int W, int slot_cap, int max_n);
 cudaError_t launch_batch_sac(int W, bool tables, const BatchDev& B, bool deep_only, KStats* st, int block, int grid,
-                             size_t smem, void* gscratch, size_t gstride, cudaStream_t s);
+                             size_t smem, void* gscratch, size_t gstride, int quota, cudaStream_t s);
 int batch_sac_blocks_per_sm(int W, bool tables, int block, size_t smem);
 cudaError_t launch_batch_commit(int W, const BatchDev& B, KStats* st, cudaStream_t s);
 cudaError_t launch_batch_select(const BatchDev& B, bool initial, cudaStream_t s);
 // Copies level (batch level + delta) onto the batch level for every member.
-cudaError_t launch_batch_copy(int W, const BatchDev& B, int delta, cudaStream_t s);
+cudaError_t launch_batch_copy(int W, const BatchDev& B, int src_level, cudaStream_t s);
+cudaError_t launch_batch_edit(int W, const BatchDev& B, int n_edit, const int* member, const int* var, const int* val,
+                              cudaStream_t s);
+cudaError_t launch_batch_gather(int W, const BatchDev& B, u64* out, cudaStream_t s);
 
 // Shared-memory (or per-CTA scratch) bytes of the CTA-local fixpoint.
 size_t cta_state_bytes(const DevNet& N);

@@ -1069,7 +1069,9 @@ __global__ void k_batch_build(BatchDev B, int with_tiles) {
 }
 
 template <int WT>
-__global__ void __launch_bounds__(256) k_batch_tile(BatchDev B, int slot_cap, int max_n, KStats* st) {
+// quota > 0: a CTA takes at most quota tiles and retires (the grid then
+// covers every tile), so that CTAs of other streams get SMs between tiles.
+__global__ void __launch_bounds__(256) k_batch_tile(BatchDev B, int slot_cap, int max_n, KStats* st, int quota) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   u64* T = reinterpret_cast<u64*>(smem_raw);
   int* slot_of = reinterpret_cast<int*>(smem_raw + static_cast<size_t>(slot_cap) * 32 * WT * 8);
@@ -1079,7 +1081,7 @@ __global__ void __launch_bounds__(256) k_batch_tile(BatchDev B, int slot_cap, in
   const int total = *B.ntiles;
   for (int i = threadIdx.x; i < max_n; i += blockDim.x) slot_of[i] = -1;
   u64 c_rev = 0, c_rows = 0, c_done = 0;
-  for (;;) {
+  for (int taken = 0; quota == 0 || taken < quota; ++taken) {
     if (threadIdx.x == 0) {
       s_t = atomicAdd(B.tcursor, 1);
       s_fail = 0;
@@ -1100,7 +1102,7 @@ __global__ void __launch_bounds__(256) k_batch_tile(BatchDev B, int slot_cap, in
 // General singleton tests over the batch: all pairs, or the deep list.
 template <int WT, bool kTab>
 __global__ void __launch_bounds__(256) k_batch_sac(BatchDev B, int deep_only, KStats* st, char* gscratch,
-                                                   size_t gstride) {
+                                                   size_t gstride, int quota) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_qlen[3], s_failed[2], s_failvar, s_err, s_b;
   __shared__ DevNet sN;
@@ -1110,7 +1112,7 @@ __global__ void __launch_bounds__(256) k_batch_sac(BatchDev B, int deep_only, KS
   Cnt cn;
   int rounds_max = 0;
   u64 done = 0;
-  for (;;) {
+  for (int taken = 0; quota == 0 || taken < quota; ++taken) {
     if (threadIdx.x == 0) {
       s_b = atomicAdd(B.cursor, 1);
       if (s_b < total) {
@@ -1183,12 +1185,44 @@ __global__ void k_batch_commit(BatchDev B, int W, KStats* st) {
 
 // Copies level (batch level + delta) of every member onto the batch level,
 // one CTA per member in turn.
-__global__ void k_batch_copy(BatchDev B, int W, int delta) {
+// Each instance's working level := level src_level of its own stack (a
+// no-op where they coincide).
+__global__ void k_batch_copy(BatchDev B, int W, int src_level) {
   for (int i = blockIdx.x; i < B.k; i += gridDim.x) {
     const size_t words = static_cast<size_t>(B.nets[i].n) * W;
     u64* dst = B.roots[i];
-    const u64* src = dst + static_cast<ptrdiff_t>(delta) * static_cast<ptrdiff_t>(words);
+    const u64* src = B.bases[i] + static_cast<size_t>(src_level) * words;
+    if (src == dst) continue;
     for (size_t j = threadIdx.x; j < words; j += blockDim.x) dst[j] = src[j];
+  }
+}
+
+// Edit e reduces variable var[e] of instance member[e] (group-local index) to
+// the single value val[e] (the empty set if val[e] is not in the domain).
+// Several edits may hit one variable: the words are ANDed atomically.
+__global__ void k_batch_edit(BatchDev B, int W, int n_edit, const int* member, const int* var, const int* val) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_edit) return;
+  u64* dom = B.roots[member[e]] + static_cast<size_t>(var[e]) * W;
+  const int a = val[e];
+  for (int w = 0; w < W; ++w) {
+    const u64 keep = (w == (a >> 6)) ? (1ull << (a & 63)) : 0ull;
+    atomicAnd(reinterpret_cast<unsigned long long*>(dom + w), static_cast<unsigned long long>(keep));
+  }
+}
+
+// Working domains of every instance into one buffer at the caller's width:
+// instance i's variable x, word w at out[out_off[i] + x * wuser[i] + w].
+__global__ void k_batch_gather(BatchDev B, int W, u64* out) {
+  for (int i = blockIdx.x; i < B.k; i += gridDim.x) {
+    const int n = B.nets[i].n, wu = B.wuser[i];
+    const u64* src = B.roots[i];
+    u64* dst = out + B.out_off[i];
+    const int words = n * wu;
+    for (int j = threadIdx.x; j < words; j += blockDim.x) {
+      const int x = j / wu, w = j - x * wu;
+      dst[j] = src[static_cast<size_t>(x) * W + w];
+    }
   }
 }
 
@@ -1454,14 +1488,14 @@ int batch_tile_blocks_per_sm(int W, int slot_cap, int max_n) {
   return e == cudaSuccess ? per_sm : 0;
 }
 
-cudaError_t launch_batch_tile(int W, const BatchDev& B, int slot_cap, int max_n, KStats* st, int grid,
+cudaError_t launch_batch_tile(int W, const BatchDev& B, int slot_cap, int max_n, KStats* st, int grid, int quota,
                               cudaStream_t s) {
   const size_t smem = batch_tile_smem(W, slot_cap, max_n);
   return dispatch_w(W, [&](auto wt) -> cudaError_t {
     constexpr int WT = decltype(wt)::value;
     cudaError_t e = allow_smem(k_batch_tile<WT>, smem);
     if (e != cudaSuccess) return e;
-    k_batch_tile<WT><<<grid, 256, smem, s>>>(B, slot_cap, max_n, st);
+    k_batch_tile<WT><<<grid, 256, smem, s>>>(B, slot_cap, max_n, st, quota);
     return cudaGetLastError();
   });
 }
@@ -1479,14 +1513,14 @@ int batch_sac_blocks_per_sm(int W, bool tables, int block, size_t smem) {
 }
 
 cudaError_t launch_batch_sac(int W, bool tables, const BatchDev& B, bool deep_only, KStats* st, int block, int grid,
-                             size_t smem, void* gscratch, size_t gstride, cudaStream_t s) {
+                             size_t smem, void* gscratch, size_t gstride, int quota, cudaStream_t s) {
   return dispatch_wtab(W, tables, [&](auto wt, auto tab) -> cudaError_t {
     constexpr int WT = decltype(wt)::value;
     constexpr bool TB = decltype(tab)::value;
     cudaError_t e = allow_smem(k_batch_sac<WT, TB>, smem);
     if (e != cudaSuccess) return e;
     k_batch_sac<WT, TB><<<grid, block, gscratch ? 0 : smem, s>>>(B, deep_only ? 1 : 0, st,
-                                                                 static_cast<char*>(gscratch), gstride);
+                                                                 static_cast<char*>(gscratch), gstride, quota);
     return cudaGetLastError();
   });
 }
@@ -1496,8 +1530,20 @@ cudaError_t launch_batch_commit(int W, const BatchDev& B, KStats* st, cudaStream
   return cudaGetLastError();
 }
 
-cudaError_t launch_batch_copy(int W, const BatchDev& B, int delta, cudaStream_t s) {
-  k_batch_copy<<<std::max(1, std::min(B.k, 4096)), 256, 0, s>>>(B, W, delta);
+cudaError_t launch_batch_copy(int W, const BatchDev& B, int src_level, cudaStream_t s) {
+  k_batch_copy<<<std::max(1, std::min(B.k, 4096)), 256, 0, s>>>(B, W, src_level);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_edit(int W, const BatchDev& B, int n_edit, const int* member, const int* var, const int* val,
+                              cudaStream_t s) {
+  if (n_edit <= 0) return cudaSuccess;
+  k_batch_edit<<<(n_edit + 255) / 256, 256, 0, s>>>(B, W, n_edit, member, var, val);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_gather(int W, const BatchDev& B, u64* out, cudaStream_t s) {
+  k_batch_gather<<<std::max(1, std::min(B.k, 4096)), 256, 0, s>>>(B, W, out);
   return cudaGetLastError();
 }
 

@@ -39,11 +39,13 @@ enum {
   CP_E_CUDA = -3,     /* CUDA runtime error */
   CP_E_TIMEOUT = -4,  /* a device-side bounded wait ran out (kernel returned) */
   CP_E_UNSUPPORTED = -5,
-  CP_E_STATE = -6     /* call not valid in the current state */
+  CP_E_STATE = -6,    /* call not valid in the current state */
+  CP_E_CANCELLED = -7 /* a server request cancelled before it ran */
 };
 
 typedef struct cp_engine cp_engine;
 typedef struct cp_net cp_net;
+typedef struct cp_instance cp_instance;
 
 /* Result of one propagation call (ConsistencyState of include/Solver.h:84-97
  * and GacStats of include/GModel.cuh:17-21, widened). */
@@ -70,6 +72,8 @@ int cp_engine_destroy(cp_engine* e);
 const char* cp_last_error_string(void);
 /* Kernel launches issued by this engine so far. */
 int64_t cp_engine_launches(const cp_engine* e);
+/* CUDA device index the engine was created on (-1 for a null engine). */
+int cp_engine_device(const cp_engine* e);
 /* Engine knobs (normally chosen by the autotuner): 0 = automatic.
  * block: threads per CTA; chunk: incidences per work item; ctas_per_sm:
  * resident CTAs per SM for the batched kernels. */
@@ -78,6 +82,15 @@ int cp_engine_set_tuning(cp_engine* e, int block, int chunk, int ctas_per_sm);
  * test, deeper branches re-run by the general kernel) wherever the network is
  * binary and fits, 1 = general per-branch kernel only. Results are identical. */
 int cp_engine_set_sac_mode(cp_engine* e, int mode);
+/* Stream priority of the engine (-1 low, 0 default, 1 high); only before the
+ * first network is uploaded. CTAs of a high-priority stream are scheduled
+ * first whenever SM resources free up. */
+int cp_engine_set_priority(cp_engine* e, int priority);
+/* Batch sweeps with quota > 0 launch CTAs that each take at most `quota`
+ * tiles or branches and retire, instead of persistent CTAs, so that
+ * higher-priority work on other streams gets SMs during long sweeps. Results
+ * are unchanged. Applies to batches created afterwards. */
+int cp_engine_set_cta_quota(cp_engine* e, int quota);
 
 /* ---- networks ------------------------------------------------------------ */
 /* Uploads a network; replaces GModelAdapter::Build
@@ -150,6 +163,97 @@ int cp_batch_info(const cp_batch* b, int group, int* info);
 /* Copies level src of every member onto the batch's level (one launch per
  * member group), e.g. to restore pristine domains kept at another level. */
 int cp_batch_copy_level(cp_batch* b, int src);
+/* A batch whose member i works on level levels[i] of nets[i]; one network may
+ * appear several times at distinct levels (independent queries on one
+ * resident network, each on its own level). */
+int cp_batch_create_levels(cp_engine* e, int k, cp_net* const* nets, const int* levels, cp_batch** out);
+/* Every member's working level := level src_level of its network, then edit j
+ * reduces variable var[j] of member member[j] to the value val[j] (an empty
+ * domain if val[j] is no longer in it; several edits of one variable
+ * intersect). */
+int cp_batch_load(cp_batch* b, int src_level, int n_edit, const int* member, const int* var, const int* val);
+/* Working domains of all members, concatenated in member order at each
+ * member's own word width (n_i * W_i words each), in one device-to-host copy. */
+int cp_batch_dom_get(cp_batch* b, uint64_t* out);
+
+/* ---- request server (continuous batching) ----------------------------------
+ * Propagate (type 0: AC / GAC), SAC (type 1) and MAC-solve (type 2: dom/min +
+ * min value) requests on one GPU. No counterpart in the reference (it has no
+ * server); every result equals the same request run alone through the calls
+ * above.
+ *
+ * Networks: registered once (cp_server_register) they stay resident in HBM,
+ * level 0 holding the initial domains and levels 1..slots serving as working
+ * levels of concurrent requests; or carried by a request (inst) and uploaded
+ * for its lifetime. A request may fix variables to values (choices): the
+ * working domains start from the initial ones with D(var[j]) reduced to
+ * {val[j]} (a value outside the initial domain, or two values for one
+ * variable, answers "inconsistent" without touching the device).
+ *
+ * A scheduler thread admits queued requests in arrival order while their
+ * estimated device footprint fits hbm_budget_bytes (resident networks count
+ * for as long as they are registered). The propagate and SAC requests
+ * admitted together run as one multi-instance batch per type on batch_engine
+ * (up to max_batch per tick; batching = 0 runs them one by one, the
+ * one-request-per-launch path). Solves run on solver threads, each on its own
+ * engine (solve_engine first). Requests that arrive while a batch is on the
+ * GPU are admitted as memory and working levels free up. An instance passed
+ * to a request must stay alive until its result is released; register copies
+ * the instance. */
+typedef struct cp_server cp_server;
+typedef struct cp_request {
+  int32_t type;               /* 0 propagate, 1 SAC, 2 MAC solve */
+  int32_t n_choice;
+  int64_t net_id;             /* registered network, or 0: use inst */
+  const cp_instance* inst;    /* network carried by the request (net_id == 0) */
+  const int* choice_var;      /* n_choice variables ... */
+  const int* choice_val;      /* ... fixed to these values */
+} cp_request;
+typedef struct cp_result {
+  int32_t status;        /* 0 queued, 1 running, 2 done, < 0 error code */
+  int32_t inconsistent;
+  int64_t deletions;     /* values removed from the initial domains (consistent results) */
+  int64_t num_positive;  /* MAC solves */
+  int64_t num_negative;
+  int32_t mac_status;    /* 1 solution, 0 unsatisfiable, 2 time out */
+  int32_t type;
+  double queue_ms;       /* submit to admission */
+  double latency_ms;     /* submit to completion */
+} cp_result;
+int cp_server_create(cp_engine* batch_engine, cp_engine* solve_engine, int64_t hbm_budget_bytes, int max_batch,
+                     int batching, cp_server** out);
+int cp_server_destroy(cp_server* s);
+/* Time limit of each MAC solve (default 600000 ms; then mac_status = 2). */
+int cp_server_set_solve_limit(cp_server* s, int64_t ms);
+/* Runs MAC solves on k threads (default 1), each on its own engine/stream;
+ * the count only grows. */
+int cp_server_set_solvers(cp_server* s, int k);
+/* Uploads a resident network with `slots` working levels; CP_E_OOM if its
+ * footprint does not fit the budget next to what is already admitted. */
+int cp_server_register(cp_server* s, const cp_instance* inst, int slots, int64_t* net_id);
+/* Frees a resident network; CP_E_STATE while requests on it are queued or
+ * running. */
+int cp_server_unregister(cp_server* s, int64_t net_id);
+int cp_submit(cp_server* s, const cp_request* req, int64_t* ticket);
+/* cp_submit of {type, no choices, the network inst}. */
+int cp_submit_instance(cp_server* s, int type, const cp_instance* inst, int64_t* ticket);
+/* Cancels a queued request (its status becomes CP_E_CANCELLED); CP_E_STATE
+ * once it has been admitted. */
+int cp_cancel(cp_server* s, int64_t ticket);
+/* Waits up to timeout_ms for a request; CP_E_TIMEOUT if still running. */
+int cp_wait(cp_server* s, int64_t ticket, int64_t timeout_ms, cp_result* res);
+/* n*W words of a done propagate / SAC request (unspecified if inconsistent);
+ * CP_E_STATE if there are none. */
+int cp_result_domains(cp_server* s, int64_t ticket, uint64_t* out);
+int cp_result_solution(cp_server* s, int64_t ticket, int* out);      /* n values */
+int cp_release(cp_server* s, int64_t ticket);
+/* Replays an arrival trace (request i submitted t_arrival_s[i] seconds after
+ * the call starts) and waits for all; fills latency_ms[i] and status[i];
+ * stats[0..7] = lane batches, batched requests, wall seconds, peak admitted
+ * bytes, busy seconds of the propagate lane, the SAC lane and the solvers
+ * (summed), MAC solves that hit the time limit. */
+int cp_server_run_trace(cp_server* s, int k, const double* t_arrival_s, const cp_request* reqs, double* latency_ms,
+                        int32_t* status, double* stats);
 
 /* ---- search: MAC on device-resident domains -------------------------------
  * MAC::enforce (src/MAC.cpp:100-165) with the reference's variable and value
@@ -171,7 +275,6 @@ int cp_mac_solve(cp_net* net, int var_heuristic, int val_heuristic, int64_t time
 int cp_gsolver_solve(cp_net* net, int64_t time_limit_ms, cp_search_result* res, int* solution);
 
 /* ---- instance generator (seeded, shared with the tests and benchmarks) --- */
-typedef struct cp_instance cp_instance;
 int cp_gen_binary(int n, int d, int64_t e, double p_lo, double p_hi, double remove, uint64_t seed,
                   cp_instance** out);
 int cp_gen_mixed(int n, int d, int64_t e, double p_lo, double p_hi, int k3, int ntup, double remove,

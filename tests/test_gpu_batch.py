@@ -147,3 +147,97 @@ def test_batch_copy_level_restores():
             if not bad:  # after a wipe-out only the verdict is defined
                 assert np.array_equal(n.dom_get(0), d)
         b.close()
+
+
+def _edits_for(inst, rng, count):
+    """Random (var, val) choices with val in the variable's initial domain."""
+    out = []
+    for _ in range(count):
+        x = int(rng.integers(0, inst.n))
+        words = inst.init[x * inst.W:(x + 1) * inst.W]
+        vals = [w * 64 + b for w in range(inst.W) for b in range(64) if (int(words[w]) >> b) & 1]
+        out.append((x, int(vals[int(rng.integers(0, len(vals)))])))
+    return out
+
+
+@pytest.mark.parametrize("op", ["ac", "sac1"])
+def test_batch_levels_one_network_many_queries(op):
+    """One resident network queried on several levels in one batch, with
+    per-query variable choices, beside other networks: each member equals the
+    same query run alone; the gathered domains equal per-member reads."""
+    rng = np.random.default_rng(17)
+    shared = cp.gen_uneven(424242, 40, 80, 64)
+    others = [cp.gen_uneven(31337 + i, 20, 60, 128) for i in range(3)]
+    slots = 5
+    with cp.Engine(0) as eng:
+        net_s = eng.upload(shared, max_levels=1 + slots)
+        net_o = [eng.upload(i, max_levels=2) for i in others]
+        members = [net_s] * slots + net_o
+        levels = list(range(1, slots + 1)) + [1] * len(net_o)
+        b = cp.Batch(eng, members, levels=levels)
+        queries = [_edits_for(shared, rng, k % 3) for k in range(slots)] + [_edits_for(o, rng, 1) for o in others]
+        edits = [(m, x, a) for m, q in enumerate(queries) for x, a in q]
+        b.load(0, edits)
+        st, inc = (b.ac() if op == "ac" else b.sac1())
+        doms = b.dom_get()
+        insts = [shared] * slots + others
+        for m, (inst, q) in enumerate(zip(insts, queries)):
+            with cp.Engine(0) as e1:
+                one = e1.upload(inst, max_levels=2)
+                for x, a in q:
+                    one.reduce_to(0, x, a)
+                s1 = one.enforce_ac(0) if op == "ac" else one.enforce_sac1(0)
+                assert bool(inc[m]) == bool(s1.inconsistent), m
+                if not s1.inconsistent:
+                    assert np.array_equal(doms[m], one.dom_get(0)), m
+                one.close()
+        # Level 0 of the shared network is untouched by the queries.
+        assert np.array_equal(net_s.dom_get(0), shared.init)
+        b.close()
+        net_s.close()
+        for n in net_o:
+            n.close()
+
+
+def test_batch_rejects_repeated_member_level():
+    inst = cp.gen_uneven(5, 20, 30, 16)
+    with cp.Engine(0) as eng:
+        net = eng.upload(inst, max_levels=3)
+        with pytest.raises(cp.CPError):
+            cp.Batch(eng, [net, net], levels=[1, 1])
+        b = cp.Batch(eng, [net, net], levels=[1, 2])
+        with pytest.raises(cp.CPError):
+            b.load(0, [(0, inst.n, 0)])  # variable out of range
+        with pytest.raises(cp.CPError):
+            b.load(0, [(2, 0, 0)])  # member out of range
+        b.close()
+        net.close()
+
+
+@pytest.mark.parametrize("quota", [1, 3])
+def test_batch_cta_quota_and_priority_keep_results(quota):
+    """Retiring sweep CTAs (quota) on a low-priority stream, with members
+    uploaded on another engine, give the persistent sweep's results."""
+    insts = _members(10, 21)
+    with cp.Engine(0) as up, cp.Engine(0) as eq, cp.Engine(0) as ep:
+        eq.set_priority(-1)
+        eq.set_cta_quota(quota)
+        ep.set_priority(1)
+        nets = [up.upload(i, max_levels=3) for i in insts]
+        for n in nets:
+            n.level_copy(0, 1)
+            n.level_copy(0, 2)
+        bq = cp.Batch(eq, nets, level=1)
+        bp = cp.Batch(ep, nets, level=2)
+        sq, iq = bq.sac1()
+        sp, ip = bp.sac1()
+        assert np.array_equal(iq, ip)
+        dq, dp = bq.dom_get(), bp.dom_get()
+        for k in range(len(nets)):
+            if not ip[k]:
+                assert np.array_equal(dq[k], dp[k]), k
+        assert sq.branches == sp.branches
+        bq.close()
+        bp.close()
+        for n in nets:
+            n.close()
