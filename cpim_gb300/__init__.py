@@ -130,6 +130,12 @@ def lib():
         "cp_server_set_solvers": ([vp, i], i),
         "cp_engine_device": ([vp], i),
         "cp_engine_set_priority": ([vp, i], i),
+        "cp_engine_set_search_mode": ([vp, i], i),
+        "cp_mac_batch_start": ([vp, i, PV, PI, PI, PI, i, i, i64, PV], i),
+        "cp_mac_batch_poll": ([vp, PU8, C.POINTER(SearchResult), PI], i),
+        "cp_mac_batch_wait": ([vp, C.POINTER(SearchResult)], i),
+        "cp_mac_batch_solution": ([vp, i, PI], i),
+        "cp_mac_batch_destroy": ([vp], i),
         "cp_engine_set_cta_quota": ([vp, i], i),
         "cp_submit_instance": ([vp, i, vp, C.POINTER(C.c_int64)], i),
         "cp_wait": ([vp, i64, i64, vp], i),
@@ -256,6 +262,10 @@ class Engine:
     def set_priority(self, priority: int):
         """Stream priority: -1 low, 0 default, 1 high (before any upload)."""
         _check(lib().cp_engine_set_priority(self._h, int(priority)))
+
+    def set_search_mode(self, mode: int):
+        """0: MAC searches run whole on the device (one CTA); 1: host-driven."""
+        _check(lib().cp_engine_set_search_mode(self._h, int(mode)))
 
     def set_cta_quota(self, quota: int):
         """Batch sweep CTAs retire after `quota` units (0: persistent)."""
@@ -502,6 +512,58 @@ class Result(C.Structure):
     _fields_ = [("status", C.c_int32), ("inconsistent", C.c_int32), ("deletions", C.c_int64),
                 ("num_positive", C.c_int64), ("num_negative", C.c_int64), ("mac_status", C.c_int32),
                 ("type", C.c_int32), ("queue_ms", C.c_double), ("latency_ms", C.c_double)]
+
+
+class MacBatch:
+    """Many MAC searches in one launch (cp_mac_batch_*): jobs are (net,
+    choices) pairs; one network may appear several times."""
+
+    def __init__(self, engine: Engine, jobs, var_h=VarHeuristic.VRH_DOM_MIN, val_h=ValHeuristic.VLH_MIN,
+                 time_limit_ms=600000):
+        self.engine = engine
+        self.nets = [n for n, _ in jobs]
+        k = len(jobs)
+        arr = (C.c_void_p * k)(*[n._h.value for n in self.nets])
+        nch = np.array([len(c) for _, c in jobs], np.int32)
+        flat = np.array([xv for _, c in jobs for xv in c], np.int32).reshape(-1, 2)
+        cv, ca = np.ascontiguousarray(flat[:, 0]), np.ascontiguousarray(flat[:, 1])
+        self._h = C.c_void_p()
+        _check(lib().cp_mac_batch_start(engine._h, k, arr, _p(nch, C.c_int), _p(cv, C.c_int), _p(ca, C.c_int),
+                                        int(var_h), int(val_h), int(time_limit_ms), C.byref(self._h)))
+
+    def poll(self):
+        k = len(self.nets)
+        done = np.zeros(k, np.uint8)
+        res = (SearchResult * k)()
+        nd = C.c_int()
+        _check(lib().cp_mac_batch_poll(self._h, _p(done, C.c_uint8), res, C.byref(nd)))
+        return done, [self._dict(i, res[i]) if done[i] else None for i in range(k)]
+
+    def wait(self):
+        k = len(self.nets)
+        res = (SearchResult * k)()
+        _check(lib().cp_mac_batch_wait(self._h, res))
+        return [self._dict(i, res[i]) for i in range(k)]
+
+    def _dict(self, i, r):
+        d = {"status": r.status, "num_positive": r.num_positive, "num_negative": r.num_negative,
+             "propagations": r.propagations, "solve_ms": r.solve_ms, "solution": []}
+        if r.status == 1:
+            sol = np.zeros(self.nets[i].n, np.int32)
+            _check(lib().cp_mac_batch_solution(self._h, i, _p(sol, C.c_int)))
+            d["solution"] = sol.tolist()
+        return d
+
+    def close(self):
+        if self._h:
+            lib().cp_mac_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Request(C.Structure):

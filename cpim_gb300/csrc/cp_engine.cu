@@ -5,6 +5,7 @@
 #include <sys/stat.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -72,6 +73,8 @@ struct cp_engine {
   int ctas_per_sm = 0;
   int sac_mode = 0;  // 0: tiled sweep where eligible, 1: general kernel only
   int cta_quota = 0;  // batch sweep CTAs retire after this many units (0: persistent)
+  int search_mode = 0;  // 0: MAC searches run on the device where they fit one CTA; 1: host-driven nodes
+  std::multimap<size_t, void*> mapped_free;  // host-mapped pinned blocks (device-written results)
   int priority = 0;   // stream priority class: -1 low, 0 default, 1 high
   // Device memory of this engine's networks and batches comes from a
   // stream-ordered pool on the engine stream: allocation is a sub-allocation
@@ -116,6 +119,24 @@ struct cp_engine {
   }
   void pinned_put(void* p, size_t bytes) {
     if (p) pinned_free.emplace(pinned_class(bytes), p);
+  }
+  int mapped_get(size_t bytes, void** p) {
+    const size_t c = pinned_class(bytes);
+    auto it = mapped_free.find(c);
+    if (it != mapped_free.end()) {
+      *p = it->second;
+      mapped_free.erase(it);
+      return CP_OK;
+    }
+    cudaError_t err = cudaHostAlloc(p, c, cudaHostAllocMapped);
+    if (err != cudaSuccess) {
+      cudaGetLastError();
+      return fail(CP_E_OOM, std::string("mapped host allocation: ") + cudaGetErrorString(err));
+    }
+    return CP_OK;
+  }
+  void mapped_put(void* p, size_t bytes) {
+    if (p) mapped_free.emplace(pinned_class(bytes), p);
   }
 };
 
@@ -367,6 +388,7 @@ static void engine_free(cp_engine* e) {
   cudaSetDevice(e->device);
   if (e->stream) cudaStreamSynchronize(e->stream);
   for (auto& kv : e->pinned_free) cudaFreeHost(kv.second);
+  for (auto& kv : e->mapped_free) cudaFreeHost(kv.second);
   if (e->pool) cudaMemPoolDestroy(e->pool);
   if (e->ev0) cudaEventDestroy(e->ev0);
   if (e->ev1) cudaEventDestroy(e->ev1);
@@ -1271,6 +1293,191 @@ class DeviceGSolver {
 
 }  // namespace
 
+// ---- device-resident MAC searches --------------------------------------
+// A launch runs each search for at most this long; searches still open are
+// resumed by the next launch, so no kernel of the search runs for long.
+constexpr long long kMacSliceNs = 50ll * 1000 * 1000;
+
+struct MacSpec {
+  cp_net* net = nullptr;
+  const u64* init = nullptr;  // domains before the choices
+  u64* stack = nullptr;       // level stack (null: allocated for the search)
+  int levels = 0;
+  std::vector<int2> choices;
+};
+
+struct cp_mac_batch {
+  cp_engine* e = nullptr;
+  int k = 0;
+  std::vector<int> n_of;
+  std::vector<int64_t> sol_off;
+  std::vector<void*> allocs;  // device pool blocks
+  void* h_block = nullptr;    // host-mapped: MacOut[k], then the solutions
+  size_t h_bytes = 0;
+  void* stage = nullptr;      // pinned staging of the job descriptors
+  size_t stage_bytes = 0;
+  MacOut* outs = nullptr;
+  int* sols = nullptr;
+  std::vector<uint8_t> reported;
+  std::vector<cp_search_result> res;
+  cudaEvent_t ev = nullptr;
+  std::chrono::steady_clock::time_point t0;
+  // Launch parameters, kept for the relaunches that resume suspended searches.
+  DevNet* d_dn = nullptr;
+  MacJob* d_jobs = nullptr;
+  int* d_cursor = nullptr;
+  MacOut* d_outs = nullptr;
+  int block = 0, grid = 0;
+  size_t smem = 0, gstride = 0;
+  char* gscratch = nullptr;
+  int launches = 0;
+  int launch() {
+    cudaStream_t s = e->stream;
+    CP_CUDA(cudaMemsetAsync(d_cursor, 0, sizeof(int), s));
+    CP_CUDA(launch_mac(d_dn, d_jobs, k, d_cursor, d_outs, block, grid, smem, gscratch, gstride, kMacSliceNs, s));
+    ++e->launches;
+    ++launches;
+    CP_CUDA(cudaEventRecord(ev, s));
+    return CP_OK;
+  }
+  ~cp_mac_batch() {
+    if (!e) return;
+    if (ev) {
+      cudaEventSynchronize(ev);
+      cudaEventDestroy(ev);
+    }
+    for (void* p : allocs) e->dev_free(p);
+    e->mapped_put(h_block, h_bytes);
+    e->pinned_put(stage, stage_bytes);
+    --e->live_nets;
+    if (e->closed && e->live_nets == 0) engine_free(e);
+  }
+};
+
+namespace {
+
+// Lays out and launches one k_mac grid over the specs.
+int mac_start(cp_engine* e, std::vector<MacSpec>& specs, int varh, int64_t time_limit_ms, cp_mac_batch* b) {
+  CP_CUDA(cudaSetDevice(e->device));
+  cudaStream_t s = e->stream;
+  const int k = static_cast<int>(specs.size());
+  b->e = e;
+  ++e->live_nets;  // a MAC batch holds the engine like a network does
+  b->k = k;
+  b->n_of.resize(k);
+  b->sol_off.resize(k + 1, 0);
+  b->reported.assign(k, 0);
+  b->res.resize(k);
+  size_t max_state = 0;
+  for (int i = 0; i < k; ++i) {
+    b->n_of[i] = specs[i].net->n;
+    b->sol_off[i + 1] = b->sol_off[i] + specs[i].net->n;
+    max_state = std::max(max_state, cta_state_bytes(specs[i].net->dn));
+  }
+  // Host-visible results.
+  const size_t out_bytes = (sizeof(MacOut) * static_cast<size_t>(k) + 255) & ~size_t(255);
+  b->h_bytes = out_bytes + static_cast<size_t>(b->sol_off[k]) * sizeof(int);
+  CP_TRY(e->mapped_get(b->h_bytes, &b->h_block));
+  std::memset(b->h_block, 0, b->h_bytes);
+  void* d_host = nullptr;
+  CP_CUDA(cudaHostGetDevicePointer(&d_host, b->h_block, 0));
+  b->outs = static_cast<MacOut*>(b->h_block);
+  b->sols = reinterpret_cast<int*>(static_cast<char*>(b->h_block) + out_bytes);
+  MacOut* d_outs = static_cast<MacOut*>(d_host);
+  int* d_sols = reinterpret_cast<int*>(static_cast<char*>(d_host) + out_bytes);
+  // Device block: [networks | jobs | choices | cursor] copied, then scratch.
+  std::vector<DevNet> dn(k);
+  std::vector<MacJob> jobs(k);
+  std::vector<int2> ch;
+  std::vector<int64_t> ch_off(k + 1, 0);
+  for (int i = 0; i < k; ++i) {
+    dn[i] = specs[i].net->dn;
+    ch.insert(ch.end(), specs[i].choices.begin(), specs[i].choices.end());
+    ch_off[i + 1] = static_cast<int64_t>(ch.size());
+  }
+  int zero = 0;
+  DevNet* d_dn = nullptr;
+  MacJob* d_jobs = nullptr;
+  int2* d_ch = nullptr;
+  int* d_cursor = nullptr;
+  MetaPack mp;
+  mp.add(&d_dn, dn.data(), k);
+  mp.add(&d_jobs, jobs.data(), k);  // filled below, before the copy
+  mp.add(&d_ch, ch.data(), ch.size());
+  mp.add(&d_cursor, &zero, 1);
+  size_t scratch = 0;
+  std::vector<size_t> off_stack(k), off_assigned(k), off_path(k);
+  auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
+  const size_t off_state = scratch;
+  scratch += up(sizeof(MacState) * static_cast<size_t>(k));
+  for (int i = 0; i < k; ++i) {
+    const cp_net* n = specs[i].net;
+    const size_t words = static_cast<size_t>(n->n) * n->W;
+    off_stack[i] = scratch;
+    if (!specs[i].stack) scratch += up(static_cast<size_t>(specs[i].levels) * words * 8);
+    off_assigned[i] = scratch;
+    scratch += up(static_cast<size_t>(specs[i].levels) * n->n);
+    off_path[i] = scratch;
+    scratch += up(static_cast<size_t>(n->n + 1) * sizeof(int2));
+  }
+  // CTA state: shared memory when the largest fits, else per-CTA scratch.
+  const bool smem_mode = max_state + 2048 <= e->smem_optin;
+  const int block = std::min(e->block_node, 256);
+  const int per_sm = mac_blocks_per_sm(block, smem_mode ? max_state : 0);
+  if (per_sm < 1) return fail(CP_E_UNSUPPORTED, "MAC kernel does not fit on an SM");
+  const int grid = std::min(k, per_sm * e->sm_count);
+  const size_t gstride = smem_mode ? 0 : up(max_state);
+  const size_t g_off = scratch;
+  scratch += gstride * static_cast<size_t>(grid);
+  char* d_block = nullptr;
+  {
+    void* raw = nullptr;
+    CP_TRY(e->dev_alloc(&raw, mp.total + scratch + 256));
+    b->allocs.push_back(raw);
+    d_block = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(raw) + 255) & ~uintptr_t(255));
+  }
+  char* d_scratch = d_block + mp.total;
+  const long long limit_ns = time_limit_ms > 0 ? static_cast<long long>(time_limit_ms) * 1000000ll : 0;
+  for (int i = 0; i < k; ++i) {
+    MacJob& J = jobs[i];
+    J.state = reinterpret_cast<MacState*>(d_scratch + off_state) + i;
+    J.net = i;
+    J.levels = specs[i].levels;
+    J.varh = varh;
+    J.n_choice = static_cast<int>(ch_off[i + 1] - ch_off[i]);
+    J.init = specs[i].init;
+    J.stack_dom = specs[i].stack ? specs[i].stack : reinterpret_cast<u64*>(d_scratch + off_stack[i]);
+    J.assigned = reinterpret_cast<uint8_t*>(d_scratch + off_assigned[i]);
+    J.path = reinterpret_cast<int2*>(d_scratch + off_path[i]);
+    J.choices = nullptr;  // set from the packed block below
+    J.solution = d_sols + b->sol_off[i];
+    J.limit_ns = limit_ns;
+  }
+  // The staging block stays with the batch until the copy has surely ended.
+  b->stage_bytes = mp.total;
+  CP_TRY(e->pinned_get(mp.total, &b->stage));
+  for (const auto& q : mp.parts) *q.dst = d_block + q.off;
+  for (int i = 0; i < k; ++i) jobs[i].choices = jobs[i].n_choice ? d_ch + ch_off[i] : nullptr;
+  for (const auto& q : mp.parts)
+    if (q.bytes) std::memcpy(static_cast<char*>(b->stage) + q.off, q.src, q.bytes);
+  CP_CUDA(cudaMemcpyAsync(d_block, b->stage, mp.total, cudaMemcpyHostToDevice, s));
+  CP_CUDA(cudaMemsetAsync(d_scratch + off_state, 0, sizeof(MacState) * static_cast<size_t>(k), s));
+  CP_CUDA(cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming));
+  b->t0 = std::chrono::steady_clock::now();
+  b->d_dn = d_dn;
+  b->d_jobs = d_jobs;
+  b->d_cursor = d_cursor;
+  b->d_outs = d_outs;
+  b->block = block;
+  b->grid = grid;
+  b->smem = smem_mode ? max_state : 0;
+  b->gscratch = smem_mode ? nullptr : d_scratch + g_off;
+  b->gstride = gstride;
+  return b->launch();
+}
+
+}  // namespace
+
 extern "C" {
 
 int cp_mac_solve(cp_net* net, int var_heuristic, int val_heuristic, int64_t time_limit_ms, cp_search_result* res,
@@ -1279,8 +1486,128 @@ int cp_mac_solve(cp_net* net, int var_heuristic, int val_heuristic, int64_t time
   if (var_heuristic != 0 && var_heuristic != 1)
     return fail(CP_E_UNSUPPORTED, "variable heuristic: 0 (VRH_LEX) or 1 (VRH_DOM_MIN)");
   if (val_heuristic != 0) return fail(CP_E_UNSUPPORTED, "value heuristic: 0 (VLH_MIN)");
+  if (net->e->search_mode == 0 && !net->prefer_grid) {
+    // The whole search in one CTA, on the network's own level stack.
+    std::vector<MacSpec> spec(1);
+    spec[0].net = net;
+    spec[0].init = net->level_ptr(0);
+    spec[0].stack = net->d_levels;
+    spec[0].levels = net->levels;
+    cp_mac_batch b;
+    CP_TRY(mac_start(net->e, spec, var_heuristic, time_limit_ms, &b));
+    CP_TRY(cp_mac_batch_wait(&b, res));
+    return cp_mac_batch_solution(&b, 0, solution);
+  }
   DeviceMAC mac(net, var_heuristic, val_heuristic);
   return mac.solve(time_limit_ms, res, solution);
+}
+
+int cp_engine_set_search_mode(cp_engine* e, int mode) {
+  if (!e) return fail(CP_E_ARG, "null engine");
+  if (mode != 0 && mode != 1) return fail(CP_E_ARG, "search mode must be 0 (device) or 1 (host-driven)");
+  e->search_mode = mode;
+  return CP_OK;
+}
+
+int cp_mac_batch_start(cp_engine* e, int k, cp_net* const* nets, const int* n_choice, const int* choice_var,
+                       const int* choice_val, int var_heuristic, int val_heuristic, int64_t time_limit_ms,
+                       cp_mac_batch** out) {
+  if (!e || !out || k < 1 || !nets) return fail(CP_E_ARG, "bad MAC batch arguments");
+  if (var_heuristic != 0 && var_heuristic != 1)
+    return fail(CP_E_UNSUPPORTED, "variable heuristic: 0 (VRH_LEX) or 1 (VRH_DOM_MIN)");
+  if (val_heuristic != 0) return fail(CP_E_UNSUPPORTED, "value heuristic: 0 (VLH_MIN)");
+  std::vector<MacSpec> spec(static_cast<size_t>(k));
+  int64_t c = 0;
+  for (int i = 0; i < k; ++i) {
+    cp_net* n = nets[i];
+    if (!n || n->e->device != e->device) return fail(CP_E_ARG, "MAC batch member on another device");
+    if (n->n >= 65536) return fail(CP_E_UNSUPPORTED, "MAC batch members need n < 65536");
+    spec[i].net = n;
+    spec[i].init = n->level_ptr(0);
+    spec[i].levels = n->n + 3;
+    const int nc = n_choice ? n_choice[i] : 0;
+    if (nc < 0 || (nc > 0 && (!choice_var || !choice_val))) return fail(CP_E_ARG, "bad choice list");
+    for (int j = 0; j < nc; ++j, ++c) {
+      CP_TRY(check_var_val(n, choice_var[c], choice_val[c]));
+      spec[i].choices.push_back(make_int2(choice_var[c], choice_val[c]));
+    }
+  }
+  auto b = std::make_unique<cp_mac_batch>();
+  CP_TRY(mac_start(e, spec, var_heuristic, time_limit_ms, b.get()));
+  *out = b.release();
+  return CP_OK;
+}
+
+int cp_mac_batch_poll(cp_mac_batch* b, uint8_t* done, cp_search_result* res, int* n_done) {
+  if (!b || !done || !res) return fail(CP_E_ARG, "null argument");
+  const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - b->t0).count();
+  int nd = 0;
+  for (int i = 0; i < b->k; ++i) {
+    if (!b->reported[i]) {
+      const volatile int* flag = &b->outs[i].done;
+      if (*flag) {
+        std::atomic_thread_fence(std::memory_order_acquire);
+        const MacOut& o = b->outs[i];
+        if (o.status < 0) return fail(o.status, "device MAC search failed (level stack or round limit)");
+        cp_search_result r{};
+        r.status = o.status;
+        r.num_positive = o.npos;
+        r.num_negative = o.nneg;
+        r.propagations = o.props;
+        r.solve_ms = ms;
+        b->res[i] = r;
+        b->reported[i] = 1;
+      }
+    }
+    done[i] = b->reported[i];
+    if (b->reported[i]) {
+      res[i] = b->res[i];
+      ++nd;
+    }
+  }
+  if (nd < b->k) {
+    const cudaError_t q = cudaEventQuery(b->ev);
+    if (q != cudaSuccess && q != cudaErrorNotReady) return fail(CP_E_CUDA, std::string("MAC batch: ") + cudaGetErrorString(q));
+    if (q == cudaSuccess) {
+      // The launch has ended: results written meanwhile are collected, and
+      // searches suspended at the end of their slice are resumed.
+      bool again = false;
+      for (int i = 0; i < b->k; ++i)
+        if (!b->reported[i] && *reinterpret_cast<volatile int*>(&b->outs[i].done)) again = true;
+      if (again) return cp_mac_batch_poll(b, done, res, n_done);
+      CP_TRY(b->launch());
+    }
+  }
+  if (n_done) *n_done = nd;
+  return CP_OK;
+}
+
+int cp_mac_batch_wait(cp_mac_batch* b, cp_search_result* res) {
+  if (!b) return fail(CP_E_ARG, "null batch");
+  std::vector<uint8_t> done(b->k);
+  std::vector<cp_search_result> tmp(b->k);
+  int nd = 0;
+  for (;;) {
+    CP_CUDA(cudaEventSynchronize(b->ev));
+    CP_TRY(cp_mac_batch_poll(b, done.data(), tmp.data(), &nd));  // relaunches suspended searches
+    if (nd == b->k) break;
+  }
+  if (res)
+    for (int i = 0; i < b->k; ++i) res[i] = tmp[i];
+  return CP_OK;
+}
+
+int cp_mac_batch_solution(cp_mac_batch* b, int i, int* out) {
+  if (!b || !out || i < 0 || i >= b->k) return fail(CP_E_ARG, "bad solution request");
+  if (!b->reported[i]) return fail(CP_E_STATE, "search not finished");
+  std::memcpy(out, b->sols + b->sol_off[i], static_cast<size_t>(b->n_of[i]) * sizeof(int));
+  return CP_OK;
+}
+
+int cp_mac_batch_destroy(cp_mac_batch* b) {
+  if (!b) return CP_OK;
+  delete b;
+  return CP_OK;
 }
 
 int cp_gsolver_solve(cp_net* net, int64_t time_limit_ms, cp_search_result* res, int* solution) {

@@ -103,6 +103,39 @@ struct SacScratch {
 
 enum NodeOp { kOpRoot = 0, kOpAssign = 1, kOpRefute = 2, kOpSingleton = 3, kOpEvents = 4 };
 
+// One device-resident MAC search (k_mac): the whole depth-first search of one
+// network runs in one CTA.
+// Where a search stands between launches: searches run in time slices, and
+// a slice that ends mid-search leaves its state here for the next launch.
+struct MacState {
+  int phase;             // 0 not started, 1 suspended, 2 finished
+  int p, top;            // path depth, highest level with live flags
+  int pad;
+  long long npos, nneg, props, t_start;
+};
+
+struct MacJob {
+  MacState* state;       // device memory, zeroed before the first launch
+  int net;               // index into the launch's network array
+  int levels;            // depth of the level stack
+  int varh;              // 1: dom/min, 0: lex
+  int n_choice;
+  const u64* init;       // n*W words: domains before the choices
+  u64* stack_dom;        // levels * n * W words
+  uint8_t* assigned;     // levels * n flags
+  int2* path;            // n + 1 decisions (variable, value)
+  const int2* choices;   // n_choice (variable, value): D(var) reduced to {value} before the root
+  int* solution;         // n values (host-visible memory)
+  long long limit_ns;    // time limit from the start of the job (0: none)
+};
+
+// Result of one k_mac job, in host-visible memory; `done` is written last.
+struct MacOut {
+  int status;            // 1 solution, 0 unsatisfiable, 2 time limit, < 0 error code
+  int done;
+  long long npos, nneg, props;
+};
+
 // A multi-instance batch: networks of one internal domain width, processed
 // together by one launch per phase. Work pairs and tiles carry the instance in
 // the high 16 bits of their variable field (instance < 32768, n < 65536).
@@ -151,6 +184,11 @@ cudaError_t launch_batch_commit(int W, const BatchDev& B, KStats* st, cudaStream
 cudaError_t launch_batch_select(const BatchDev& B, bool initial, cudaStream_t s);
 // Copies level (batch level + delta) onto the batch level for every member.
 cudaError_t launch_batch_copy(int W, const BatchDev& B, int src_level, cudaStream_t s);
+// MAC searches (any widths and network kinds in one launch); CTA state in
+// shared memory (smem bytes) or per-CTA global scratch (gscratch, gstride).
+cudaError_t launch_mac(const DevNet* nets, const MacJob* jobs, int njobs, int* cursor, MacOut* outs, int block,
+                       int grid, size_t smem, void* gscratch, size_t gstride, long long slice_ns, cudaStream_t s);
+int mac_blocks_per_sm(int block, size_t smem);
 cudaError_t launch_batch_edit(int W, const BatchDev& B, int n_edit, const int* member, const int* var, const int* val,
                               cudaStream_t s);
 cudaError_t launch_batch_gather(int W, const BatchDev& B, u64* out, cudaStream_t s);

@@ -509,6 +509,270 @@ __global__ void __launch_bounds__(512) k_node(DevNet N, u64* levels, int src, in
 }
 
 // ---------------------------------------------------------------------------
+// k_mac: the MAC search of MAC::enforce (src/MAC.cpp:100-165) run by one CTA,
+// with the per-level "assigned" flags of IntVar (src/Network.cpp:112-118,
+// 235-256) and AssignedStack (src/Solver.cpp:36-56, 114-116) that decide the
+// dom/min variable order (src/MAC.cpp:357-368). The CTA's shared-memory
+// domains always hold the current search level; levels live in a global
+// stack. Persistent CTAs take jobs from a cursor.
+// ---------------------------------------------------------------------------
+struct MacShared {
+  int qlen[3], failed[2], failvar, err, job, val, stop;
+  unsigned long long wmin[32];
+};
+
+// One fixpoint on the CTA domains after op (root: every variable seeded;
+// assign: D(var) := {val}; refute: val removed from D(var)). Returns true if
+// consistent.
+template <int WT, bool kTab>
+__device__ bool mac_fix(const DevNet& N, const Fix& F, char* base, const CtaLayout& L, MacShared& sh, int op, int var,
+                        int val, Cnt& cn) {
+  block_zero(reinterpret_cast<u32*>(base + L.fb0), (L.ts - L.fb0) / 4);
+  if (N.nt) block_zero(reinterpret_cast<u32*>(F.tstamp), N.nt);
+  if (threadIdx.x == 0) {
+    sh.qlen[0] = sh.qlen[1] = sh.qlen[2] = 0;
+    sh.failed[0] = sh.failed[1] = 0;
+  }
+  __syncthreads();
+  if (op == kOpRoot) {
+    for (int z = threadIdx.x; z < N.n; z += blockDim.x) seed_var<WT>(N, F, z);
+  } else if (threadIdx.x == 0) {
+    u64* dv = F.D + static_cast<size_t>(var) * WT;
+    if (op == kOpAssign) {
+      for (int w = 0; w < WT; ++w) dv[w] = (w == (val >> 6)) ? (1ull << (val & 63)) : 0ull;
+    } else {
+      dv[val >> 6] &= ~(1ull << (val & 63));
+    }
+    seed_var<WT>(N, F, var);
+  }
+  __syncthreads();
+  cta_fixpoint<WT, kTab>(N, F, cn, &sh.err);
+  return (vloadi(&sh.failed[0]) | vloadi(&sh.failed[1])) == 0;
+}
+
+// First value of D(x) (VLH_MIN, src/MAC.cpp:338-340).
+template <int WT>
+__device__ __forceinline__ int dom_head(const u64* D, int x) {
+#pragma unroll
+  for (int w = 0; w < WT; ++w) {
+    const u64 v = D[static_cast<size_t>(x) * WT + w];
+    if (v) return w * 64 + __ffsll(static_cast<long long>(v)) - 1;
+  }
+  return -1;
+}
+
+// VRH_DOM_MIN: the first unassigned variable of strictly smaller domain size
+// (smallest size, ties to the smallest index). Block-wide.
+template <int WT>
+__device__ int mac_select(const u64* D, const uint8_t* A_p, int n, MacShared& sh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  unsigned long long best = ~0ull;
+  for (int v = threadIdx.x; v < n; v += blockDim.x) {
+    if (A_p[v]) continue;
+    int sz = 0;
+#pragma unroll
+    for (int w = 0; w < WT; ++w) sz += __popcll(D[static_cast<size_t>(v) * WT + w]);
+    const unsigned long long key = (static_cast<unsigned long long>(sz) << 32) | static_cast<unsigned>(v);
+    best = key < best ? key : best;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long other = __shfl_xor_sync(kFull, best, o);
+    best = other < best ? other : best;
+  }
+  if (lane == 0) sh.wmin[warp] = best;
+  __syncthreads();
+  if (warp == 0) {
+    unsigned long long b = lane < nwarps ? sh.wmin[lane] : ~0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long other = __shfl_xor_sync(kFull, b, o);
+      b = other < b ? other : b;
+    }
+    if (lane == 0) sh.wmin[0] = b;
+  }
+  __syncthreads();
+  const unsigned long long b = sh.wmin[0];
+  __syncthreads();
+  return b == ~0ull ? -1 : static_cast<int>(b & 0xffffffffu);
+}
+
+// Runs job J for at most slice_ns of this launch (checked between nodes);
+// a search still open then is suspended in J.state for the next launch.
+template <int WT, bool kTab>
+__device__ void mac_one(const DevNet& N, const MacJob& J, MacOut* out, char* base, MacShared& sh, long long slice_ns) {
+  MacState& S = *J.state;
+  if (S.phase == 2) return;
+  Fix F = make_cta_fix(N, base, sh.qlen, sh.failed, &sh.failvar);
+  const CtaLayout L = cta_layout(N);
+  const int n = N.n;
+  const size_t words = static_cast<size_t>(n) * WT;
+  uint8_t* A = J.assigned;
+  const long long t_enter = globaltimer_ns();
+  if (threadIdx.x == 0) sh.err = 0;
+  Cnt cn;
+  long long npos = 0, nneg = 0, props = 0, t0 = t_enter;
+  int status = -1, p = 0, top = 0;
+  bool ok = true;
+  if (S.phase == 0) {
+    block_copy(F.D, J.init, words);
+    for (size_t i = threadIdx.x; i < static_cast<size_t>(J.levels) * n; i += blockDim.x) A[i] = 0;
+    __syncthreads();
+    if (threadIdx.x == 0)
+      for (int c = 0; c < J.n_choice; ++c) {
+        const int2 ch = J.choices[c];
+        u64* dv = F.D + static_cast<size_t>(ch.x) * WT;
+        for (int w = 0; w < WT; ++w) dv[w] &= (w == (ch.y >> 6)) ? (1ull << (ch.y & 63)) : 0ull;
+      }
+    __syncthreads();
+    props = 1;
+    ok = mac_fix<WT, kTab>(N, F, base, L, sh, kOpRoot, 0, 0, cn);
+    block_copy(J.stack_dom, F.D, words);
+    if (!ok) status = 0;
+  } else {
+    p = S.p;
+    top = S.top;
+    npos = S.npos;
+    nneg = S.nneg;
+    props = S.props;
+    t0 = S.t_start;
+    block_copy(F.D, J.stack_dom + static_cast<size_t>(p) * words, words);
+    __syncthreads();
+  }
+  bool suspended = false;
+  while (status < 0) {
+    if (threadIdx.x == 0) {
+      const long long now = globaltimer_ns();
+      sh.stop = (J.limit_ns > 0 && now - t0 > J.limit_ns) ? 1 : (slice_ns > 0 && now - t_enter > slice_ns ? 2 : 0);
+    }
+    __syncthreads();
+    const int stop = sh.stop, err = sh.err;
+    __syncthreads();
+    if (err) {
+      status = err;
+      break;
+    }
+    if (stop == 1) {
+      status = 2;
+      break;
+    }
+    if (stop == 2) {
+      suspended = true;
+      break;
+    }
+    if (p + 1 >= J.levels) {
+      status = -1;  // level stack too shallow
+      break;
+    }
+    const int var = J.varh == 0 ? (p + 1 < n ? p + 1 : -1) : mac_select<WT>(F.D, A + static_cast<size_t>(p) * n, n, sh);
+    if (var < 0) {
+      status = -6;  // no variable to branch on
+      break;
+    }
+    if (threadIdx.x == 0) sh.val = dom_head<WT>(F.D, var);
+    // new_level(p): the flags of level p carry to level p + 1.
+    for (int v = threadIdx.x; v < n; v += blockDim.x)
+      A[static_cast<size_t>(p + 1) * n + v] = A[static_cast<size_t>(p) * n + v];
+    top = p;
+    __syncthreads();
+    const int val = sh.val;
+    if (threadIdx.x == 0) {
+      J.path[p] = make_int2(var, val);
+      A[static_cast<size_t>(p + 1) * n + var] = 1;
+    }
+    ++p;
+    ++npos;
+    ok = mac_fix<WT, kTab>(N, F, base, L, sh, kOpAssign, var, val, cn);
+    ++props;
+    block_copy(J.stack_dom + static_cast<size_t>(p) * words, F.D, words);
+    if (ok && p == n) {
+      for (int x = threadIdx.x; x < n; x += blockDim.x) J.solution[x] = dom_head<WT>(F.D, x);
+      status = 1;
+      break;
+    }
+    while (!ok && p > 0) {
+      __syncthreads();
+      const int2 va = J.path[p - 1];
+      --p;
+      // back_to(p): flags of levels p..top cleared.
+      for (size_t i = static_cast<size_t>(p) * n + threadIdx.x; i < static_cast<size_t>(top + 1) * n; i += blockDim.x)
+        A[i] = 0;
+      top = p;
+      ++nneg;
+      block_copy(F.D, J.stack_dom + static_cast<size_t>(p) * words, words);
+      ok = mac_fix<WT, kTab>(N, F, base, L, sh, kOpRefute, va.x, va.y, cn);
+      ++props;
+      block_copy(J.stack_dom + static_cast<size_t>(p) * words, F.D, words);
+      // update_model_assigned: the decisions still on the path.
+      for (int i = threadIdx.x; i < p; i += blockDim.x) A[static_cast<size_t>(p) * n + J.path[i].x] = 1;
+      __syncthreads();
+    }
+    if (!ok) status = 0;
+  }
+  __syncthreads();
+  if (suspended) {
+    if (threadIdx.x == 0) {
+      S.phase = 1;
+      S.p = p;
+      S.top = top;
+      S.npos = npos;
+      S.nneg = nneg;
+      S.props = props;
+      S.t_start = t0;
+    }
+    return;
+  }
+  __threadfence_system();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    S.phase = 2;
+    out->status = status;
+    out->npos = npos;
+    out->nneg = nneg;
+    out->props = props;
+    __threadfence_system();
+    *reinterpret_cast<volatile int*>(&out->done) = 1;
+  }
+}
+
+// Jobs of any domain width and network kind in one launch: each job runs the
+// body instantiated for its width and table flag.
+__global__ void __launch_bounds__(256) k_mac(const DevNet* nets, const MacJob* jobs, int njobs, int* cursor,
+                                              MacOut* outs, char* gscratch, size_t gstride, long long slice_ns) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ MacShared sh;
+  __shared__ DevNet sN;
+  char* base = gscratch ? gscratch + blockIdx.x * gstride : reinterpret_cast<char*>(smem_raw);
+  for (;;) {
+    if (threadIdx.x == 0) {
+      sh.job = atomicAdd(cursor, 1);
+      if (sh.job < njobs) sN = nets[jobs[sh.job].net];
+    }
+    __syncthreads();
+    const int j = sh.job;
+    if (j >= njobs) break;
+    const MacJob& J = jobs[j];
+    MacOut* o = outs + j;
+    const bool tab = sN.nt > 0;
+    switch (sN.W) {
+      case 1:
+        tab ? mac_one<1, true>(sN, J, o, base, sh, slice_ns) : mac_one<1, false>(sN, J, o, base, sh, slice_ns);
+        break;
+      case 2:
+        tab ? mac_one<2, true>(sN, J, o, base, sh, slice_ns) : mac_one<2, false>(sN, J, o, base, sh, slice_ns);
+        break;
+      case 4:
+        tab ? mac_one<4, true>(sN, J, o, base, sh, slice_ns) : mac_one<4, false>(sN, J, o, base, sh, slice_ns);
+        break;
+      default:
+        mac_one<8, false>(sN, J, o, base, sh, slice_ns);
+        break;
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
 // k_sac: persistent CTAs over the SAC branch work list.
 // ---------------------------------------------------------------------------
 template <int WT, bool kTab>
@@ -1299,6 +1563,30 @@ cudaError_t launch_node(const DevNet& N, u64* levels, int src, int dst, int op, 
   });
 }
 
+template <typename F>
+cudaError_t dispatch_wtab(int W, bool tables, F&& f) {
+  DevNet probe;
+  probe.W = W;
+  probe.nt = tables ? 1 : 0;
+  return dispatch_wt(probe, f);
+}
+
+int mac_blocks_per_sm(int block, size_t smem) {
+  int per_sm = 0;
+  if (allow_smem(k_mac, smem) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mac, block, smem) != cudaSuccess) return 0;
+  return per_sm;
+}
+
+cudaError_t launch_mac(const DevNet* nets, const MacJob* jobs, int njobs, int* cursor, MacOut* outs, int block,
+                       int grid, size_t smem, void* gscratch, size_t gstride, long long slice_ns, cudaStream_t s) {
+  const size_t dyn = gscratch ? 0 : smem;
+  cudaError_t e = allow_smem(k_mac, dyn);
+  if (e != cudaSuccess) return e;
+  k_mac<<<grid, block, dyn, s>>>(nets, jobs, njobs, cursor, outs, static_cast<char*>(gscratch), gstride, slice_ns);
+  return cudaGetLastError();
+}
+
 int ac_grid_max_blocks(const DevNet& N, int block, int sm_count) {
   int per_sm = 0;
   cudaError_t e = dispatch_wt(N, [&](auto wt, auto tab) -> cudaError_t {
@@ -1431,13 +1719,6 @@ cudaError_t launch_gen_rows(const DevNet& N, u64* rel, const int* bx, const int*
 }
 
 // ---- batches ----
-template <typename F>
-cudaError_t dispatch_wtab(int W, bool tables, F&& f) {
-  DevNet probe;
-  probe.W = W;
-  probe.nt = tables ? 1 : 0;
-  return dispatch_wt(probe, f);
-}
 
 int batch_node_blocks_per_sm(int W, bool tables, int block, size_t smem) {
   int per_sm = 0;

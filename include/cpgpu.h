@@ -270,6 +270,30 @@ typedef struct cp_search_result {
 } cp_search_result;
 int cp_mac_solve(cp_net* net, int var_heuristic, int val_heuristic, int64_t time_limit_ms,
                  cp_search_result* res, int* solution);
+/* Search placement: 0 (default) runs the whole MAC search of cp_mac_solve on
+ * the device, in one CTA, where the network's propagation state fits one CTA
+ * (node counts and solutions are those of the host-driven search); 1 drives
+ * every node from the host. */
+int cp_engine_set_search_mode(cp_engine* e, int mode);
+/* Many MAC searches in one launch (one CTA per search, CTAs take searches
+ * from a queue). Search i runs on nets[i] from its level 0 with the next
+ * n_choice[i] (choice_var, choice_val) pairs reduced to single values (n_choice
+ * may be NULL), in its own level stack, so one network may appear several
+ * times. Networks may live on other engines of the device. The time limit
+ * counts from the start of each search. Returns at once. */
+typedef struct cp_mac_batch cp_mac_batch;
+int cp_mac_batch_start(cp_engine* e, int k, cp_net* const* nets, const int* n_choice, const int* choice_var,
+                       const int* choice_val, int var_heuristic, int val_heuristic, int64_t time_limit_ms,
+                       cp_mac_batch** out);
+/* Non-blocking: done[i] = 1 and res[i] filled for the searches that have
+ * ended (results are written by the device into host-mapped memory as each
+ * search ends); *n_done = their number. */
+int cp_mac_batch_poll(cp_mac_batch* b, uint8_t* done, cp_search_result* res, int* n_done);
+/* Blocks until every search has ended; res may be NULL. */
+int cp_mac_batch_wait(cp_mac_batch* b, cp_search_result* res);
+/* The solution of an ended search i (n_i values; meaningful if status 1). */
+int cp_mac_batch_solution(cp_mac_batch* b, int i, int* out);
+int cp_mac_batch_destroy(cp_mac_batch* b);
 /* GModelSolver::Solve (src/GModelSolver.cu:31-102): d-way search, min-domain
  * variable among those with more than one value, all values in order. */
 int cp_gsolver_solve(cp_net* net, int64_t time_limit_ms, cp_search_result* res, int* solution);

@@ -45,20 +45,23 @@ def test_sac1_matches_reference(engine, golden):
         net.close()
 
 
-def test_mac_matches_reference(engine, golden):
+@pytest.mark.parametrize("mode", [0, 1], ids=["device-search", "host-driven"])
+def test_mac_matches_reference(golden, mode):
     cases = _cases(golden, "mac")
     assert cases
-    for c in cases:
-        inst = make_engine_instance(c["args"])
-        net = engine.upload(inst)
-        m = net.mac_solve(time_limit_ms=60000)
-        r = c["result"]
-        assert m["num_positive"] == r["num_positive"], c["args"]
-        assert m["num_negative"] == r["num_negative"], c["args"]
-        assert (m["status"] == 1) == (r["num_sol"] == 1), c["args"]
-        if m["status"] == 1:
-            assert m["solution"] == r["solution"], c["args"]
-        net.close()
+    with cp.Engine(0) as engine:
+        engine.set_search_mode(mode)
+        for c in cases:
+            inst = make_engine_instance(c["args"])
+            net = engine.upload(inst)
+            m = net.mac_solve(time_limit_ms=60000)
+            r = c["result"]
+            assert m["num_positive"] == r["num_positive"], c["args"]
+            assert m["num_negative"] == r["num_negative"], c["args"]
+            assert (m["status"] == 1) == (r["num_sol"] == 1), c["args"]
+            if m["status"] == 1:
+                assert m["solution"] == r["solution"], c["args"]
+            net.close()
 
 
 @pytest.mark.parametrize("args", [(60, 8, 150, 0.2, 0.4, 20, 300, 0.1), (60, 16, 200, 0.2, 0.4, 30, 2000, 0.1),

@@ -1,0 +1,112 @@
+"""GPU tests of the device-resident MAC search (k_mac): a whole search per
+CTA must give the host-driven search's node counts and solutions, alone and
+batched, with and without variable choices."""
+import numpy as np
+import pytest
+
+import cpim_gb300 as cp
+from tests.golden_cases import make_engine_instance
+
+pytestmark = pytest.mark.gpu
+
+
+def _host_driven(inst, choices, var_h=cp.VarHeuristic.VRH_DOM_MIN):
+    with cp.Engine(0) as e:
+        e.set_search_mode(1)
+        net = e.upload(inst)
+        for x, a in choices:
+            net.reduce_to(0, x, a)
+        r = net.mac_solve(var_h, cp.ValHeuristic.VLH_MIN, time_limit_ms=120000)
+        net.close()
+    return r
+
+
+def _same(a, b, tag):
+    assert a["status"] == b["status"], tag
+    assert (a["num_positive"], a["num_negative"]) == (b["num_positive"], b["num_negative"]), tag
+    if a["status"] == 1:
+        assert a["solution"] == b["solution"], tag
+
+
+def _choices(inst, rng, k):
+    out = []
+    for _ in range(k):
+        x = int(rng.integers(0, inst.n))
+        out.append((x, int(rng.integers(0, int(inst.dom[x])))))
+    # keep the first choice per variable (the server answers conflicting ones
+    # without a search)
+    seen, keep = set(), []
+    for x, a in out:
+        if x not in seen:
+            seen.add(x)
+            keep.append((x, a))
+    return keep
+
+
+def test_mac_batch_matches_host_driven(golden):
+    rng = np.random.default_rng(3)
+    insts = [make_engine_instance(c["args"]) for c in golden if c["op"] == "mac"][:10]
+    insts += [cp.gen_uneven(700 + i, 12, 40, 64) for i in range(8)]
+    insts += [cp.gen_mixed(30, 8, 60, 0.3, 0.5, 40, 60, 0.2, s) for s in (1, 2)]
+    with cp.Engine(0) as up, cp.Engine(0) as eng:
+        nets = [up.upload(i) for i in insts]
+        jobs, refs = [], []
+        for inst, net in zip(insts, nets):
+            for rep in range(2):
+                ch = _choices(inst, rng, rep * 2)
+                jobs.append((net, ch))
+                refs.append(_host_driven(inst, ch))
+        mb = cp.MacBatch(eng, jobs, time_limit_ms=120000)
+        got = mb.wait()
+        for k, (g, r) in enumerate(zip(got, refs)):
+            _same(g, r, k)
+        mb.close()
+        for n in nets:
+            n.close()
+
+
+def test_mac_batch_poll_reports_each_search_once():
+    insts = [cp.gen_uneven(800 + i, 12, 30, 16) for i in range(12)]
+    with cp.Engine(0) as eng:
+        nets = [eng.upload(i) for i in insts]
+        mb = cp.MacBatch(eng, [(n, []) for n in nets], time_limit_ms=120000)
+        seen = {}
+        for _ in range(200000):
+            done, res = mb.poll()
+            for i, r in enumerate(res):
+                if r is not None and i not in seen:
+                    seen[i] = r
+            if done.all():
+                break
+        assert len(seen) == len(nets)
+        final = mb.wait()
+        for i, r in enumerate(final):
+            _same(r, seen[i], i)
+        mb.close()
+        for n in nets:
+            n.close()
+
+
+def _lex(inst, mode):
+    with cp.Engine(0) as eng:
+        eng.set_search_mode(mode)
+        net = eng.upload(inst)
+        try:
+            return net.mac_solve(cp.VarHeuristic.VRH_LEX, cp.ValHeuristic.VLH_MIN)
+        except cp.CPError as ex:
+            return {"error": ex.code}
+        finally:
+            net.close()
+
+
+@pytest.mark.parametrize("p", [0.3, 0.55])
+def test_mac_lex_order_device_equals_host(p):
+    """VRH_LEX takes vars[|I| + 1] (src/MAC.cpp:366-368): it never branches on
+    variable 0 and runs off the end once |I| + 1 = n, which both paths report
+    as an error; an unsatisfiable network is refuted with equal counts."""
+    inst = cp.gen_binary(20, 8, 60, p, p, 0.0, 9)
+    d, h = _lex(inst, 0), _lex(inst, 1)
+    if "error" in h:
+        assert d.get("error") == h["error"]
+    else:
+        _same(d, h, "lex")
