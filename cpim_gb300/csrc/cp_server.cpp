@@ -19,9 +19,9 @@
 //   - SAC lane: the same for SAC requests, on a default-priority stream whose
 //     sweep CTAs retire after a few tiles, so that the propagate and solve
 //     lanes get SMs during long sweeps instead of waiting behind them;
-//   - solve lane(s): MAC solves, whose host-driven search is latency-bound,
-//     one per thread (high-priority streams); a solver keeps its own copy of
-//     each resident network it has used.
+//   - solve lane(s): MAC solves, run whole on the device, one CTA per search,
+//     everything queued when a solver is free in one launch; each request
+//     finishes as soon as its own search ends (high-priority streams).
 // Requests that arrive while a lane is busy join its next batch. Without
 // batching one lane runs every propagate and SAC request alone, in order: the
 // one-request-per-launch path. Built only on the public C ABI.
@@ -58,7 +58,6 @@ struct Resident {
   std::vector<int> free_slots;
   int64_t footprint = 0;
   int refs = 0;               // queued or running requests on it
-  bool dead = false;          // unregistered (the object stays for solver caches)
 };
 
 struct Req {
@@ -102,6 +101,12 @@ int64_t net_footprint(const cpgen::Instance& I, int levels) {
 // Device bytes a request adds to a batch (work lists, tiles, descriptors).
 int64_t batch_share(const cpgen::Instance& I) {
   return total_values(I) * 16 + int64_t(I.n) * (32 + 16 * internal_w(I.W)) + 4096;
+}
+
+// Device bytes of one device MAC search: its level stack, assigned flags and
+// path.
+int64_t search_share(const cpgen::Instance& I) {
+  return int64_t(I.n + 3) * I.n * (internal_w(I.W) * 8 + 1) + int64_t(I.n) * 8 + 4096;
 }
 
 int upload(cp_engine* e, const cpgen::Instance& I, int levels, cp_net** out) {
@@ -360,97 +365,96 @@ struct cp_server {
     }
   }
 
-  // One MAC solve on the solver's engine: resident networks from the
-  // solver's cached copy (domains reset to the initial ones), others
-  // uploaded for the request.
-  void solve_one(Req* r, cp_engine* eng, std::unordered_map<int64_t, cp_net*>& cache) {
-    cp_net* net = nullptr;
-    bool owned = false;
-    int rc = CP_OK;
-    if (r->res) {
-      auto it = cache.find(r->res->id);
-      if (it == cache.end()) {
-        rc = upload(eng, *r->inst, 0, &net);
-        if (rc == CP_OK) {
-          cache[r->res->id] = net;
-          std::lock_guard<std::mutex> lk(mu);
-          account(cp_net_device_bytes(net));
-        }
+  // MAC solves: everything queued when a solver is free runs as one batch of
+  // device searches (one CTA per search; resident networks are read in place
+  // from their pristine level 0, each search in its own level stack), and
+  // each request finishes as soon as its own search ends.
+  void solve_batch(std::vector<Req*>& rq, cp_engine* eng) {
+    std::vector<cp_net*> nets, owned;
+    std::vector<int> nch, cv, ca;
+    std::vector<Req*> live;
+    for (Req* r : rq) {
+      cp_net* net = nullptr;
+      if (r->res) {
+        net = r->res->net;
       } else {
-        net = it->second;
-        rc = cp_dom_set(net, 0, r->inst->init.data());
+        const int rc = upload(eng, *r->inst, 2, &net);
+        if (rc != CP_OK) {
+          fail_req(r, rc);
+          finish(r);
+          continue;
+        }
+        owned.push_back(net);
       }
-    } else {
-      rc = upload(eng, *r->inst, 0, &net);
-      owned = rc == CP_OK;
+      live.push_back(r);
+      nets.push_back(net);
+      nch.push_back(static_cast<int>(r->cvar.size()));
+      cv.insert(cv.end(), r->cvar.begin(), r->cvar.end());
+      ca.insert(ca.end(), r->cval.begin(), r->cval.end());
     }
-    for (size_t j = 0; rc == CP_OK && j < r->cvar.size(); ++j) rc = cp_reduce_to(net, 0, r->cvar[j], r->cval[j]);
-    if (rc == CP_OK) {
-      cp_search_result res{};
-      r->sol.assign(r->inst->n, -1);
+    const int k = static_cast<int>(live.size());
+    if (k > 0) {
       int64_t limit;
       {
         std::lock_guard<std::mutex> lk(mu);
         limit = solve_limit_ms;
       }
-      rc = cp_mac_solve(net, 1, 0, limit, &res, r->sol.data());
-      if (rc == CP_OK) {
-        if (res.status == 2) {
-          std::lock_guard<std::mutex> lk(mu);
-          ++mac_timeouts;
+      cp_mac_batch* b = nullptr;
+      int rc = cp_mac_batch_start(eng, k, nets.data(), nch.data(), cv.data(), ca.data(), 1, 0, limit, &b);
+      std::vector<uint8_t> done(k, 0), fin(k, 0);
+      std::vector<cp_search_result> res(k);
+      int left = k;
+      while (rc == CP_OK && left > 0) {
+        int nd = 0;
+        rc = cp_mac_batch_poll(b, done.data(), res.data(), &nd);
+        for (int i = 0; rc == CP_OK && i < k; ++i) {
+          if (!done[i] || fin[i]) continue;
+          Req* r = live[i];
+          r->mac_status = res[i].status;
+          r->npos = res[i].num_positive;
+          r->nneg = res[i].num_negative;
+          r->inconsistent = res[i].status == 0;
+          r->sol.assign(r->inst->n, -1);
+          if (res[i].status == 1) cp_mac_batch_solution(b, i, r->sol.data());
+          if (res[i].status == 2) {
+            std::lock_guard<std::mutex> lk(mu);
+            ++mac_timeouts;
+          }
+          finish(r);
+          fin[i] = 1;
+          --left;
         }
-        r->mac_status = res.status;
-        r->npos = res.num_positive;
-        r->nneg = res.num_negative;
-        r->inconsistent = res.status == 0;
+        if (rc == CP_OK && left > 0) std::this_thread::sleep_for(std::chrono::microseconds(20));
       }
+      for (int i = 0; i < k; ++i)
+        if (!fin[i]) {
+          fail_req(live[i], rc != CP_OK ? rc : CP_E_STATE);
+          finish(live[i]);
+        }
+      if (b) cp_mac_batch_destroy(b);
     }
-    if (rc != CP_OK) fail_req(r, rc);
-    if (owned) cp_net_destroy(net);
+    for (cp_net* n : owned) cp_net_destroy(n);
   }
 
   void solve_loop(cp_engine* eng) {
     cudaSetDevice(cp_engine_device(eng));
-    std::unordered_map<int64_t, cp_net*> cache;  // resident id -> this solver's copy
     std::unique_lock<std::mutex> lk(mu);
     while (!stop) {
-      // Copies of unregistered networks go first.
-      std::vector<cp_net*> drop;
-      for (auto it = cache.begin(); it != cache.end();) {
-        auto rit = residents.find(it->first);
-        if (rit == residents.end() || rit->second->dead) {
-          in_use -= cp_net_device_bytes(it->second);
-          drop.push_back(it->second);
-          it = cache.erase(it);
-        } else {
-          ++it;
-        }
-      }
-      if (!drop.empty()) {
-        lk.unlock();
-        for (cp_net* n : drop) cp_net_destroy(n);
-        lk.lock();
-        continue;
-      }
       if (solve_q.empty()) {
         cv_solve.wait_for(lk, std::chrono::milliseconds(2));
         continue;
       }
-      Req* r = solve_q.front();
-      solve_q.pop_front();
+      std::vector<Req*> rq;
+      while (!solve_q.empty() && static_cast<int>(rq.size()) < max_batch) {
+        rq.push_back(solve_q.front());
+        solve_q.pop_front();
+      }
       lk.unlock();
       const auto t0 = Clock::now();
-      solve_one(r, eng, cache);
+      solve_batch(rq, eng);
       const double dt = std::chrono::duration<double>(Clock::now() - t0).count();
-      finish(r);
       lk.lock();
       solve_busy_s += dt;
-    }
-    for (auto& kv : cache) {
-      in_use -= cp_net_device_bytes(kv.second);
-      lk.unlock();
-      cp_net_destroy(kv.second);
-      lk.lock();
     }
   }
 
@@ -465,7 +469,7 @@ struct cp_server {
     std::lock_guard<std::mutex> lk(mu);
     if (q->net_id != 0) {
       auto it = residents.find(q->net_id);
-      if (it == residents.end() || it->second->dead) return CP_E_ARG;
+      if (it == residents.end()) return CP_E_ARG;
       r->res = it->second.get();
       r->inst = &r->res->I;
     } else {
@@ -475,10 +479,8 @@ struct cp_server {
     const cpgen::Instance& I = *r->inst;
     for (int j = 0; j < q->n_choice; ++j)
       if (r->cvar[j] < 0 || r->cvar[j] >= I.n || r->cval[j] < 0 || r->cval[j] >= I.dom[r->cvar[j]]) return CP_E_ARG;
-    if (r->res)
-      r->footprint = r->type == 2 ? net_footprint(I, I.n + 3) : batch_share(I);
-    else
-      r->footprint = net_footprint(I, r->type == 2 ? I.n + 3 : 2) + (r->type == 2 ? 0 : batch_share(I));
+    const int64_t share = r->type == 2 ? search_share(I) : batch_share(I);
+    r->footprint = r->res ? share : net_footprint(I, 2) + share;
     r->t_submit = Clock::now();
     r->id = next_id++;
     if (r->res) ++r->res->refs;
@@ -609,21 +611,18 @@ int cp_server_register(cp_server* s, const cp_instance* inst, int slots, int64_t
 
 int cp_server_unregister(cp_server* s, int64_t net_id) {
   if (!s) return CP_E_ARG;
-  cp_net* net = nullptr;
+  std::unique_ptr<Resident> gone;
   {
     std::lock_guard<std::mutex> lk(s->mu);
     auto it = s->residents.find(net_id);
-    if (it == s->residents.end() || it->second->dead) return CP_E_ARG;
-    Resident* r = it->second.get();
-    if (r->refs > 0) return CP_E_STATE;  // requests still queued or running on it
-    r->dead = true;
-    net = r->net;
-    r->net = nullptr;
-    s->in_use -= r->footprint;
-    r->I = cpgen::Instance();
+    if (it == s->residents.end()) return CP_E_ARG;
+    if (it->second->refs > 0) return CP_E_STATE;  // requests still queued or running on it
+    gone = std::move(it->second);
+    s->residents.erase(it);
+    s->in_use -= gone->footprint;
   }
   std::lock_guard<std::mutex> eg(s->eng_mu);
-  cp_net_destroy(net);
+  cp_net_destroy(gone->net);
   return CP_OK;
 }
 
