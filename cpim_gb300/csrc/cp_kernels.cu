@@ -1049,36 +1049,47 @@ __device__ __forceinline__ void tile_one(const DevNet& N, const u64* root, int x
             uc[w] = warp_or64(mine ? dy[w] : 0ull);
             acc[w] = 0;
           }
-          bool still = mine;
+          // Rows of the values of y that some open lane still has, 32 values
+          // per chunk, 8 rows between coverage tests; a lane ORs the rows of
+          // its own values (a predicated OR per row: the row address and the
+          // skip test are warp-uniform). Stops once every open lane's
+          // accumulated support covers its D(z).
           bool go = true;
           int loaded = 0;
 #pragma unroll
-          for (int w = 0; w < WT; ++w) {
-            u64 m = go ? uc[w] : 0ull;
-            while (m) {
-              const int c0 = pop_low<WT>(m, w), c1 = pop_low<WT>(m, w), c2 = pop_low<WT>(m, w), c3 = pop_low<WT>(m, w);
-              u64 r0[WT], r1[WT], r2[WT], r3[WT];
-              load_row<WT>(N.rel, A.yz + static_cast<size_t>(c0) * WT, r0);
-              if (c1 >= 0) load_row<WT>(N.rel, A.yz + static_cast<size_t>(c1) * WT, r1);
-              if (c2 >= 0) load_row<WT>(N.rel, A.yz + static_cast<size_t>(c2) * WT, r2);
-              if (c3 >= 0) load_row<WT>(N.rel, A.yz + static_cast<size_t>(c3) * WT, r3);
-              loaded += 1 + (c1 >= 0) + (c2 >= 0) + (c3 >= 0);
-              const bool h0 = (sel<WT>(dy, c0 >> 6) >> (c0 & 63)) & 1ull;
-              const bool h1 = c1 >= 0 && ((sel<WT>(dy, c1 >> 6) >> (c1 & 63)) & 1ull);
-              const bool h2 = c2 >= 0 && ((sel<WT>(dy, c2 >> 6) >> (c2 & 63)) & 1ull);
-              const bool h3 = c3 >= 0 && ((sel<WT>(dy, c3 >> 6) >> (c3 & 63)) & 1ull);
+          for (int h = 0; h < 2 * WT; ++h) {
+            const u32 ucw = static_cast<u32>(sel<WT>(uc, h >> 1) >> ((h & 1) * 32));
+            const u32 myb = mine ? static_cast<u32>(sel<WT>(dy, h >> 1) >> ((h & 1) * 32)) : 0u;
+            if (ucw == 0) continue;
+            const u64* rc = N.rel + A.yz + static_cast<size_t>(h) * 32 * WT;
+#pragma unroll
+            for (int j0 = 0; j0 < 32; j0 += 8) {
+              const u32 chunk = (ucw >> j0) & 0xffu;
+              if (!go || chunk == 0) continue;
+#pragma unroll
+              for (int jj = 0; jj < 8; ++jj) {
+                if ((chunk >> jj) & 1u) {
+                  u64 r[WT];
+                  load_row<WT>(rc, static_cast<size_t>(j0 + jj) * WT, r);
+                  ++loaded;
+                  if ((myb >> (j0 + jj)) & 1u) {
+#pragma unroll
+                    for (int q = 0; q < WT; ++q) acc[q] |= r[q];
+                  }
+                }
+              }
               u64 gap = 0;
 #pragma unroll
-              for (int q = 0; q < WT; ++q) {
-                acc[q] |= (h0 ? r0[q] : 0ull) | (h1 ? r1[q] : 0ull) | (h2 ? r2[q] : 0ull) | (h3 ? r3[q] : 0ull);
-                gap |= cur[q] & ~acc[q];
-              }
-              still = still && gap != 0;
-              if (__ballot_sync(kFull, still) == 0) {
-                m = 0;
-                go = false;  // every open lane is covered: no change in round two
-              }
+              for (int q = 0; q < WT; ++q) gap |= cur[q] & ~acc[q];
+              if (__ballot_sync(kFull, mine && gap != 0) == 0) go = false;  // every open lane covered
             }
+          }
+          bool still = false;
+          if (go) {
+            u64 gap = 0;
+#pragma unroll
+            for (int q = 0; q < WT; ++q) gap |= cur[q] & ~acc[q];
+            still = mine && gap != 0;
           }
           if (lane == 0) {
             ++c_rev;
@@ -1128,7 +1139,7 @@ __device__ __forceinline__ void flush_tile_counts(KStats* st, u64 c_rev, u64 c_r
 }
 
 template <int WT>
-__global__ void __launch_bounds__(256) k_sac_tile(DevNet N, const u64* root, const int4* tiles, const int* ntiles,
+__global__ void __launch_bounds__(256, WT <= 2 ? 4 : 1) k_sac_tile(DevNet N, const u64* root, const int4* tiles, const int* ntiles,
                                                   int* tcursor, uint8_t* ok, int* deep, int* ndeep, int slot_cap,
                                                   KStats* st) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1335,7 +1346,7 @@ __global__ void k_batch_build(BatchDev B, int with_tiles) {
 template <int WT>
 // quota > 0: a CTA takes at most quota tiles and retires (the grid then
 // covers every tile), so that CTAs of other streams get SMs between tiles.
-__global__ void __launch_bounds__(256) k_batch_tile(BatchDev B, int slot_cap, int max_n, KStats* st, int quota) {
+__global__ void __launch_bounds__(256, WT <= 2 ? 4 : 1) k_batch_tile(BatchDev B, int slot_cap, int max_n, KStats* st, int quota) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   u64* T = reinterpret_cast<u64*>(smem_raw);
   int* slot_of = reinterpret_cast<int*>(smem_raw + static_cast<size_t>(slot_cap) * 32 * WT * 8);
