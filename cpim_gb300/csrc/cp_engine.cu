@@ -662,6 +662,8 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   CP_TRY(net->alloc(&S.tcursor, 4));
   CP_TRY(net->alloc(&S.deep, total_values));
   CP_TRY(net->alloc(&S.ndeep, 4));
+  S.weak = nullptr;
+  if (n_tab == 0 && n_bin > 0) CP_TRY(net->alloc(&S.weak, static_cast<size_t>(2) * n_bin * (kWeakK + 1)));
   CP_TRY(net->alloc(&net->d_stats, 1));
   CP_TRY(net->alloc(&net->d_evt, n));
   CP_TRY(net->alloc(&net->d_sizes, n));
@@ -916,7 +918,13 @@ int cp_enforce_sac1(cp_net* net, int level, cp_stats* st) {
     CP_CUDA(cudaEventRecord(e->evk0, s));
     if (tiled) {
       // Two-round branches resolved by the tiled kernel, the rest (the deep
-      // list) by the general kernel.
+      // list) by the general kernel; the weak-support lists are rebuilt for
+      // this sweep's domains first.
+      if (S.weak) {
+        CP_CUDA(launch_weak(net->dn, net->level_ptr(level), S.weak, s));
+        launches += 1;
+        e->launches += 1;
+      }
       CP_CUDA(launch_sac_tile(net->dn, net->level_ptr(level), S, S.ok, net->slot_cap, net->d_stats, 256,
                               net->tile_grid, s));
       CP_CUDA(launch_sac_branches(net->dn, net->level_ptr(level), S.work, S.nwork, S.cursor, S.ok, net->d_stats,

@@ -28,6 +28,10 @@ using u64 = unsigned long long;
 using u32 = unsigned int;
 
 constexpr int kMaxArity = 4;
+// Weak-support lists of the tiled SAC sweep: per directional arc, the kWeakK
+// values of the revised variable with the fewest supports, then the count of
+// the next one.
+constexpr int kWeakK = 16;
 constexpr int kItemVarShift = 12;             // work item = (var << 12) | chunk
 constexpr int kMaxChunksPerVar = 1 << kItemVarShift;
 constexpr int kMaxVars = 1 << (32 - kItemVarShift);
@@ -99,6 +103,7 @@ struct SacScratch {
   int* tcursor;       // [1]
   int* deep;          // work indices the tiled kernel hands to the general one
   int* ndeep;         // [1]
+  u32* weak;          // [2*nb][kWeakK + 1] weak-support lists (null: not built)
 };
 
 enum NodeOp { kOpRoot = 0, kOpAssign = 1, kOpRefute = 2, kOpSingleton = 3, kOpEvents = 4 };
@@ -218,6 +223,8 @@ int sac_blocks_per_sm(const DevNet& N, int block, bool smem_state);
 // S.deep for the general kernel. slot_cap: neighbours held in shared memory.
 cudaError_t launch_sac_tile(const DevNet& N, const u64* root, SacScratch S, uint8_t* ok, int slot_cap, KStats* st,
                             int block, int grid, cudaStream_t s);
+// Weak-support lists of every arc for the domains at root (into S.weak).
+cudaError_t launch_weak(const DevNet& N, const u64* root, u32* weak, cudaStream_t s);
 size_t sac_tile_smem(const DevNet& N, int slot_cap);
 int sac_tile_blocks_per_sm(const DevNet& N, int slot_cap, int block);
 // Builds the list of live (x, a) pairs of a level (warp ballot + prefix);

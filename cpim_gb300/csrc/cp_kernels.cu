@@ -976,9 +976,10 @@ __device__ __forceinline__ int pop_low(u64& m, int word) {
 // s_fail / s_deep must be zero and visible to the whole CTA on entry. Ends
 // with the CTA synchronised.
 template <int WT>
-__device__ __forceinline__ void tile_one(const DevNet& N, const u64* root, int x, int base, int b0, u32 live,
-                                         uint8_t* ok, int* deep, int* ndeep, int slot_cap, u64* T, int* slot_of,
-                                         u32& s_fail, u32& s_deep, u64& c_rev, u64& c_rows, u64& c_done) {
+__device__ __forceinline__ void tile_one(const DevNet& N, const u64* root, const u32* weak, int x, int base, int b0,
+                                         u32 live, uint8_t* ok, int* deep, int* ndeep, int slot_cap, u64* T,
+                                         int* slot_of, u32& s_fail, u32& s_deep, u64& c_rev, u64& c_rows,
+                                         u64& c_done) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   {
     const int a0 = N.arc_start[x], deg = N.arc_start[x + 1] - a0;
@@ -1021,8 +1022,18 @@ __device__ __forceinline__ void tile_one(const DevNet& N, const u64* root, int x
         const int y = N.arcs[a0 + s].z;
         if (slot_of[y] != s) continue;
         u64 dy[WT];
+        int removed = 0;  // values of y this lane's round one removed
 #pragma unroll
-        for (int w = 0; w < WT; ++w) dy[w] = T[(static_cast<size_t>(s) * 32 + lane) * WT + w];
+        for (int w = 0; w < WT; ++w) {
+          dy[w] = T[(static_cast<size_t>(s) * 32 + lane) * WT + w];
+          removed += __popcll(__ldg(root + static_cast<size_t>(y) * WT + w)) - __popcll(dy[w]);
+        }
+        // Above thr every value of z keeps a support in any lane's D(y)
+        // (pigeonhole over the removed values): only the listed weak values
+        // need a row test.
+        int thr = ((live >> lane) & 1u) ? removed : 0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) thr = max(thr, __shfl_xor_sync(kFull, thr, o));
         const int y0 = N.arc_start[y], y1 = N.arc_start[y + 1];
         for (int j = y0; j < y1; ++j) {
           // Lanes still open (live, not failed, not handed over), warp-uniform.
@@ -1043,64 +1054,92 @@ __device__ __forceinline__ void tile_one(const DevNet& N, const u64* root, int x
             for (int w = 0; w < WT; ++w) cur[w] = __ldg(root + static_cast<size_t>(z) * WT + w);
           }
           const bool mine = (open >> lane) & 1u;
-          u64 uc[WT], acc[WT];
-#pragma unroll
-          for (int w = 0; w < WT; ++w) {
-            uc[w] = warp_or64(mine ? dy[w] : 0ull);
-            acc[w] = 0;
-          }
-          // Rows of the values of y that some open lane still has, 32 values
-          // per chunk, 8 rows between coverage tests; a lane ORs the rows of
-          // its own values (a predicated OR per row: the row address and the
-          // skip test are warp-uniform). Stops once every open lane's
-          // accumulated support covers its D(z).
-          bool go = true;
+          bool still = false, left = false;
           int loaded = 0;
+          const u32* wl = weak ? weak + static_cast<size_t>(j) * (kWeakK + 1) : nullptr;
+          if (wl && static_cast<int>(__ldg(wl + kWeakK) >> 16) > thr) {
+            // Weak values only: v loses all supports iff its row misses D(y).
+            int unsup = 0;
+            for (int k = 0; k < kWeakK; ++k) {
+              const u32 e = __ldg(wl + k);
+              const int cnt = static_cast<int>(e >> 16);
+              if (cnt > thr) break;
+              const int v = static_cast<int>(e & 0xffffu);
+              const bool need =
+                  mine && removed >= cnt && ((sel<WT>(cur, v >> 6) >> (v & 63)) & 1ull);
+              if (__ballot_sync(kFull, need) == 0) continue;
+              u64 r[WT];
+              load_row<WT>(N.rel, A.zy + static_cast<size_t>(v) * WT, r);
+              ++loaded;
+              u64 hit = 0;
 #pragma unroll
-          for (int h = 0; h < 2 * WT; ++h) {
-            const u32 ucw = static_cast<u32>(sel<WT>(uc, h >> 1) >> ((h & 1) * 32));
-            const u32 myb = mine ? static_cast<u32>(sel<WT>(dy, h >> 1) >> ((h & 1) * 32)) : 0u;
-            if (ucw == 0) continue;
-            const u64* rc = N.rel + A.yz + static_cast<size_t>(h) * 32 * WT;
+              for (int q = 0; q < WT; ++q) hit |= r[q] & dy[q];
+              if (need && hit == 0) ++unsup;
+            }
+            if (unsup) {
+              int size = 0;
 #pragma unroll
-            for (int j0 = 0; j0 < 32; j0 += 8) {
-              const u32 chunk = (ucw >> j0) & 0xffu;
-              if (!go || chunk == 0) continue;
+              for (int q = 0; q < WT; ++q) size += __popcll(cur[q]);
+              still = true;
+              left = unsup < size;
+            }
+          } else {
+            u64 uc[WT], acc[WT];
 #pragma unroll
-              for (int jj = 0; jj < 8; ++jj) {
-                if ((chunk >> jj) & 1u) {
-                  u64 r[WT];
-                  load_row<WT>(rc, static_cast<size_t>(j0 + jj) * WT, r);
-                  ++loaded;
-                  if ((myb >> (j0 + jj)) & 1u) {
+            for (int w = 0; w < WT; ++w) {
+              uc[w] = warp_or64(mine ? dy[w] : 0ull);
+              acc[w] = 0;
+            }
+            // Rows of the values of y that some open lane still has, 32 values
+            // per chunk, 8 rows between coverage tests; a lane ORs the rows of
+            // its own values (a predicated OR per row: the row address and the
+            // skip test are warp-uniform). Stops once every open lane's
+            // accumulated support covers its D(z).
+            bool go = true;
 #pragma unroll
-                    for (int q = 0; q < WT; ++q) acc[q] |= r[q];
+            for (int h = 0; h < 2 * WT; ++h) {
+              const u32 ucw = static_cast<u32>(sel<WT>(uc, h >> 1) >> ((h & 1) * 32));
+              const u32 myb = mine ? static_cast<u32>(sel<WT>(dy, h >> 1) >> ((h & 1) * 32)) : 0u;
+              if (ucw == 0) continue;
+              const u64* rc = N.rel + A.yz + static_cast<size_t>(h) * 32 * WT;
+#pragma unroll
+              for (int j0 = 0; j0 < 32; j0 += 8) {
+                const u32 chunk = (ucw >> j0) & 0xffu;
+                if (!go || chunk == 0) continue;
+#pragma unroll
+                for (int jj = 0; jj < 8; ++jj) {
+                  if ((chunk >> jj) & 1u) {
+                    u64 r[WT];
+                    load_row<WT>(rc, static_cast<size_t>(j0 + jj) * WT, r);
+                    ++loaded;
+                    if ((myb >> (j0 + jj)) & 1u) {
+#pragma unroll
+                      for (int q = 0; q < WT; ++q) acc[q] |= r[q];
+                    }
                   }
                 }
+                u64 gap = 0;
+#pragma unroll
+                for (int q = 0; q < WT; ++q) gap |= cur[q] & ~acc[q];
+                if (__ballot_sync(kFull, mine && gap != 0) == 0) go = false;  // every open lane covered
               }
-              u64 gap = 0;
-#pragma unroll
-              for (int q = 0; q < WT; ++q) gap |= cur[q] & ~acc[q];
-              if (__ballot_sync(kFull, mine && gap != 0) == 0) go = false;  // every open lane covered
             }
-          }
-          bool still = false;
-          if (go) {
-            u64 gap = 0;
+            if (go) {
+              u64 gap = 0, kept = 0;
 #pragma unroll
-            for (int q = 0; q < WT; ++q) gap |= cur[q] & ~acc[q];
-            still = mine && gap != 0;
+              for (int q = 0; q < WT; ++q) {
+                gap |= cur[q] & ~acc[q];
+                kept |= cur[q] & acc[q];
+              }
+              still = mine && gap != 0;
+              left = kept != 0;
+            }
           }
           if (lane == 0) {
             ++c_rev;
             c_rows += loaded;
           }
-          if (still) {
-            u64 left = 0;
-#pragma unroll
-            for (int q = 0; q < WT; ++q) left |= cur[q] & acc[q];
-            atomicOr(left ? &s_deep : &s_fail, 1u << lane);
-          }
+          if (still) atomicOr(left ? &s_deep : &s_fail, 1u << lane);
         }
       }
       __syncthreads();
@@ -1126,6 +1165,58 @@ __device__ __forceinline__ void tile_one(const DevNet& N, const u64* root, int x
   }
 }
 
+// Weak-support lists for the root domains: per directional arc j (revise z
+// against y), the kWeakK values v of D(z) with the fewest supports
+// |row_zy(v) & D(y)| in increasing (count, v) order as count << 16 | v, then
+// the next count << 16 (0xffff: none). One warp per source variable y; the
+// smallest keys are taken by repeated warp minima.
+template <int WT>
+__global__ void k_weak(DevNet N, const u64* root, u32* weak) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int y = gw; y < N.n; y += nw) {
+    u64 dy[WT];
+    load_dom_uniform<WT>(root + static_cast<size_t>(y) * WT, dy);
+    for (int j = N.arc_start[y]; j < N.arc_start[y + 1]; ++j) {
+      const Arc A = N.arcs[j];
+      const int z = A.z, dz = N.dsize[z];
+      u64 d0z[WT];
+      load_dom_uniform<WT>(root + static_cast<size_t>(z) * WT, d0z);
+      u32 key[2 * WT];
+#pragma unroll
+      for (int t = 0; t < 2 * WT; ++t) {
+        const int v = t * 32 + lane;
+        key[t] = 0xffffffffu;
+        if (v < dz && ((sel<WT>(d0z, v >> 6) >> (v & 63)) & 1ull)) {
+          u64 r[WT];
+          load_row<WT>(N.rel, A.zy + static_cast<size_t>(v) * WT, r);
+          int c = 0;
+#pragma unroll
+          for (int w = 0; w < WT; ++w) c += __popcll(r[w] & dy[w]);
+          key[t] = (static_cast<u32>(c) << 16) | static_cast<u32>(v);
+        }
+      }
+      u32* out = weak + static_cast<size_t>(j) * (kWeakK + 1);
+      for (int k = 0; k <= kWeakK; ++k) {
+        u32 m = key[0];
+#pragma unroll
+        for (int t = 1; t < 2 * WT; ++t) m = min(m, key[t]);
+        m = __reduce_min_sync(kFull, m);
+        if (lane == 0) out[k] = k < kWeakK ? m : (m | 0xffffu);
+        if (m == 0xffffffffu) {
+          if (lane == 0)
+            for (int r = k + 1; r <= kWeakK; ++r) out[r] = 0xffffffffu;
+          break;
+        }
+#pragma unroll
+        for (int t = 0; t < 2 * WT; ++t)
+          if (key[t] == m) key[t] = 0xffffffffu;
+      }
+    }
+  }
+}
+
 __device__ __forceinline__ void flush_tile_counts(KStats* st, u64 c_rev, u64 c_rows, u64 c_done) {
   Cnt cn;
   cn.rev = c_rev;
@@ -1141,7 +1232,7 @@ __device__ __forceinline__ void flush_tile_counts(KStats* st, u64 c_rev, u64 c_r
 template <int WT>
 __global__ void __launch_bounds__(256, WT <= 2 ? 4 : 1) k_sac_tile(DevNet N, const u64* root, const int4* tiles, const int* ntiles,
                                                   int* tcursor, uint8_t* ok, int* deep, int* ndeep, int slot_cap,
-                                                  KStats* st) {
+                                                  KStats* st, const u32* weak) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   u64* T = reinterpret_cast<u64*>(smem_raw);  // [slot_cap][32][WT]
   int* slot_of = reinterpret_cast<int*>(smem_raw + static_cast<size_t>(slot_cap) * 32 * WT * 8);  // [n]
@@ -1160,7 +1251,7 @@ __global__ void __launch_bounds__(256, WT <= 2 ? 4 : 1) k_sac_tile(DevNet N, con
     const int t = s_t;
     if (t >= total) break;
     const int4 tl = tiles[t];
-    tile_one<WT>(N, root, tl.x, tl.y, tl.z, static_cast<u32>(tl.w), ok, deep, ndeep, slot_cap, T, slot_of, s_fail,
+    tile_one<WT>(N, root, weak, tl.x, tl.y, tl.z, static_cast<u32>(tl.w), ok, deep, ndeep, slot_cap, T, slot_of, s_fail,
                  s_deep, c_rev, c_rows, c_done);
   }
   flush_tile_counts(st, c_rev, c_rows, c_done);
@@ -1368,7 +1459,7 @@ __global__ void __launch_bounds__(256, WT <= 2 ? 4 : 1) k_batch_tile(BatchDev B,
     if (t >= total) break;
     const int4 tl = B.tiles[t];
     const int inst = tl.x >> 16;
-    tile_one<WT>(sN, B.roots[inst], tl.x & 0xffff, tl.y, tl.z, static_cast<u32>(tl.w), B.ok, B.deep, B.ndeep,
+    tile_one<WT>(sN, B.roots[inst], nullptr, tl.x & 0xffff, tl.y, tl.z, static_cast<u32>(tl.w), B.ok, B.deep, B.ndeep,
                  slot_cap, T, slot_of, s_fail, s_deep, c_rev, c_rows, c_done);
   }
   flush_tile_counts(st, c_rev, c_rows, c_done);
@@ -1674,7 +1765,16 @@ cudaError_t launch_sac_tile(const DevNet& N, const u64* root, SacScratch S, uint
     cudaError_t e = allow_smem(k_sac_tile<WT>, smem);
     if (e != cudaSuccess) return e;
     k_sac_tile<WT><<<grid, block, smem, s>>>(N, root, S.tiles, S.ntiles, S.tcursor, ok, S.deep, S.ndeep, slot_cap,
-                                             st);
+                                             st, S.weak);
+    return cudaGetLastError();
+  });
+}
+
+cudaError_t launch_weak(const DevNet& N, const u64* root, u32* weak, cudaStream_t s) {
+  return dispatch_w(N.W, [&](auto wt) -> cudaError_t {
+    constexpr int WT = decltype(wt)::value;
+    const int blocks = std::max(1, std::min(4096, (N.n * 32 + 255) / 256));
+    k_weak<WT><<<blocks, 256, 0, s>>>(N, root, weak);
     return cudaGetLastError();
   });
 }

@@ -96,7 +96,9 @@ def test_sac_mixed_matches_oracle(engine, args):
 @pytest.mark.parametrize("args", [(30, 8, 120, 0.35, 0.35, 0.1, 1), (30, 8, 120, 0.35, 0.35, 0.1, 4),
                                   (30, 8, 120, 0.45, 0.45, 0.1, 3), (40, 100, 160, 0.8, 0.8, 0.2, 3),
                                   (24, 256, 60, 0.9, 0.9, 0.3, 3), (60, 64, 600, 0.55, 0.55, 0.1, 5),
-                                  (100, 128, 1000, 0.4, 0.4, 0.0, 7), (150, 16, 3000, 0.3, 0.3, 0.05, 2)])
+                                  (100, 128, 1000, 0.4, 0.4, 0.0, 7), (150, 16, 3000, 0.3, 0.3, 0.05, 2),
+                                  (60, 300, 500, 0.5, 0.5, 0.0, 4), (120, 64, 2000, 0.5, 0.5, 0.0, 8),
+                                  (80, 128, 1500, 0.55, 0.55, 0.0, 6), (40, 70, 200, 0.88, 0.88, 0.0, 4)])
 def test_sac_tiled_equals_general(args):
     # The tiled sweep (two-round test, deeper branches handed to the general
     # kernel) and the general per-branch kernel give the same SAC closure,
