@@ -1917,8 +1917,9 @@ int batch_group_setup(cp_batch* b, BatchGroup& g) {
   const int kg = static_cast<int>(g.members.size());
   std::vector<DevNet> nets(kg);
   std::vector<u64*> roots(kg), bases(kg);
-  std::vector<int64_t> offs(kg);
+  std::vector<int64_t> offs(kg), woff(kg);
   std::vector<int> wuser(kg);
+  int64_t weak_words = 0;
   std::vector<int> var_base(kg + 1, 0);
   int max_deg = 1;
   g.cta_bytes = 0;
@@ -1930,6 +1931,8 @@ int batch_group_setup(cp_batch* b, BatchGroup& g) {
     bases[i] = n->d_levels;
     offs[i] = b->out_off[g.members[i]];
     wuser[i] = n->W_user;
+    woff[i] = weak_words;
+    weak_words += static_cast<int64_t>(2) * n->nb * (kWeakK + 1);
     var_base[i + 1] = var_base[i] + n->n;
     g.max_n = std::max(g.max_n, n->n);
     g.cta_bytes = std::max(g.cta_bytes, cta_state_bytes(n->dn));
@@ -1949,12 +1952,14 @@ int batch_group_setup(cp_batch* b, BatchGroup& g) {
   u64** d_roots;
   u64** d_bases;
   int64_t* d_offs;
+  int64_t* d_woff;
   int *d_vb, *d_vi, *d_wu;
   MetaPack mp;
   mp.add(&d_nets, nets.data(), kg);
   mp.add(&d_roots, roots.data(), kg);
   mp.add(&d_bases, bases.data(), kg);
   mp.add(&d_offs, offs.data(), kg);
+  mp.add(&d_woff, woff.data(), kg);
   mp.add(&d_wu, wuser.data(), kg);
   mp.add(&d_vb, var_base.data(), kg + 1);
   mp.add(&d_vi, var_inst.data(), tv);
@@ -1971,6 +1976,9 @@ int batch_group_setup(cp_batch* b, BatchGroup& g) {
   B.roots = d_roots;
   B.bases = d_bases;
   B.out_off = d_offs;
+  B.weak_off = d_woff;
+  B.weak = nullptr;
+  if (!g.tables && weak_words > 0) CP_TRY(b->alloc(&B.weak, static_cast<size_t>(weak_words)));
   B.wuser = d_wu;
   B.var_base = d_vb;
   B.var_inst = d_vi;
@@ -2067,6 +2075,10 @@ int batch_sweep_launches(cp_batch* b, BatchGroup& g, bool with_commit) {
     return q > 0 ? static_cast<int>(std::min<int64_t>((units + q - 1) / q, int64_t(1) << 30)) : persistent;
   };
   if (g.tiled) {
+    if (B.weak) {
+      CP_CUDA(launch_batch_weak(g.W, B, s));
+      e->launches += 1;
+    }
     CP_CUDA(launch_batch_tile(g.W, B, g.slot_cap, g.max_n, b->d_stats, cover(g.tiles_upper, g.tile_grid), q, s));
     CP_CUDA(launch_batch_sac(g.W, g.tables, B, true, b->d_stats, g.sac_block, cover(g.total_values, g.sac_grid), smem,
                              g.gscratch, g.gstride, q, s));

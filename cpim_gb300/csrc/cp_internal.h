@@ -171,6 +171,8 @@ struct BatchDev {
   int* tcursor = nullptr;
   int* deep = nullptr;
   int* ndeep = nullptr;
+  u32* weak = nullptr;             // weak-support lists of all members (null: none)
+  const int64_t* weak_off = nullptr;  // [k] first list word of each member
 };
 
 // Batch launch wrappers (cp_kernels.cu). W / tables select the template.
@@ -189,6 +191,7 @@ cudaError_t launch_batch_commit(int W, const BatchDev& B, KStats* st, cudaStream
 cudaError_t launch_batch_select(const BatchDev& B, bool initial, cudaStream_t s);
 // Copies level (batch level + delta) onto the batch level for every member.
 cudaError_t launch_batch_copy(int W, const BatchDev& B, int src_level, cudaStream_t s);
+cudaError_t launch_batch_weak(int W, const BatchDev& B, cudaStream_t s);
 // MAC searches (any widths and network kinds in one launch); CTA state in
 // shared memory (smem bytes) or per-CTA global scratch (gscratch, gstride).
 cudaError_t launch_mac(const DevNet* nets, const MacJob* jobs, int njobs, int* cursor, MacOut* outs, int block,

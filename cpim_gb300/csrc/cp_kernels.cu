@@ -1171,50 +1171,58 @@ __device__ __forceinline__ void tile_one(const DevNet& N, const u64* root, const
 // the next count << 16 (0xffff: none). One warp per source variable y; the
 // smallest keys are taken by repeated warp minima.
 template <int WT>
-__global__ void k_weak(DevNet N, const u64* root, u32* weak) {
+__device__ void weak_lists_of(const DevNet& N, const u64* root, int y, u32* weak) {
   const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nw = (gridDim.x * blockDim.x) >> 5;
-  for (int y = gw; y < N.n; y += nw) {
-    u64 dy[WT];
-    load_dom_uniform<WT>(root + static_cast<size_t>(y) * WT, dy);
-    for (int j = N.arc_start[y]; j < N.arc_start[y + 1]; ++j) {
-      const Arc A = N.arcs[j];
-      const int z = A.z, dz = N.dsize[z];
-      u64 d0z[WT];
-      load_dom_uniform<WT>(root + static_cast<size_t>(z) * WT, d0z);
-      u32 key[2 * WT];
+  u64 dy[WT];
+  load_dom_uniform<WT>(root + static_cast<size_t>(y) * WT, dy);
+  for (int j = N.arc_start[y]; j < N.arc_start[y + 1]; ++j) {
+    const Arc A = N.arcs[j];
+    const int z = A.z, dz = N.dsize[z];
+    u64 d0z[WT];
+    load_dom_uniform<WT>(root + static_cast<size_t>(z) * WT, d0z);
+    u32 key[2 * WT];
 #pragma unroll
-      for (int t = 0; t < 2 * WT; ++t) {
-        const int v = t * 32 + lane;
-        key[t] = 0xffffffffu;
-        if (v < dz && ((sel<WT>(d0z, v >> 6) >> (v & 63)) & 1ull)) {
-          u64 r[WT];
-          load_row<WT>(N.rel, A.zy + static_cast<size_t>(v) * WT, r);
-          int c = 0;
+    for (int t = 0; t < 2 * WT; ++t) {
+      const int v = t * 32 + lane;
+      key[t] = 0xffffffffu;
+      if (v < dz && ((sel<WT>(d0z, v >> 6) >> (v & 63)) & 1ull)) {
+        u64 r[WT];
+        load_row<WT>(N.rel, A.zy + static_cast<size_t>(v) * WT, r);
+        int c = 0;
 #pragma unroll
-          for (int w = 0; w < WT; ++w) c += __popcll(r[w] & dy[w]);
-          key[t] = (static_cast<u32>(c) << 16) | static_cast<u32>(v);
-        }
-      }
-      u32* out = weak + static_cast<size_t>(j) * (kWeakK + 1);
-      for (int k = 0; k <= kWeakK; ++k) {
-        u32 m = key[0];
-#pragma unroll
-        for (int t = 1; t < 2 * WT; ++t) m = min(m, key[t]);
-        m = __reduce_min_sync(kFull, m);
-        if (lane == 0) out[k] = k < kWeakK ? m : (m | 0xffffu);
-        if (m == 0xffffffffu) {
-          if (lane == 0)
-            for (int r = k + 1; r <= kWeakK; ++r) out[r] = 0xffffffffu;
-          break;
-        }
-#pragma unroll
-        for (int t = 0; t < 2 * WT; ++t)
-          if (key[t] == m) key[t] = 0xffffffffu;
+        for (int w = 0; w < WT; ++w) c += __popcll(r[w] & dy[w]);
+        key[t] = (static_cast<u32>(c) << 16) | static_cast<u32>(v);
       }
     }
+    u32* out = weak + static_cast<size_t>(j) * (kWeakK + 1);
+    for (int k = 0; k <= kWeakK; ++k) {
+      u32 m = key[0];
+#pragma unroll
+      for (int t = 1; t < 2 * WT; ++t) m = min(m, key[t]);
+      m = __reduce_min_sync(kFull, m);
+      if (lane == 0) out[k] = k < kWeakK ? m : (m | 0xffffu);
+      if (m == 0xffffffffu) {
+        if (lane == 0)
+          for (int r = k + 1; r <= kWeakK; ++r) out[r] = 0xffffffffu;
+        break;
+      }
+#pragma unroll
+      for (int t = 0; t < 2 * WT; ++t)
+        if (key[t] == m) key[t] = 0xffffffffu;
+    }
   }
+}
+
+// Weak-support lists for the root domains: per directional arc j (revise z
+// against y), the kWeakK values v of D(z) with the fewest supports
+// |row_zy(v) & D(y)| in increasing (count, v) order as count << 16 | v, then
+// the next count << 16 (0xffff: none). One warp per source variable y; the
+// smallest keys are taken by repeated warp minima.
+template <int WT>
+__global__ void k_weak(DevNet N, const u64* root, u32* weak) {
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int y = gw; y < N.n; y += nw) weak_lists_of<WT>(N, root, y, weak);
 }
 
 __device__ __forceinline__ void flush_tile_counts(KStats* st, u64 c_rev, u64 c_rows, u64 c_done) {
@@ -1434,6 +1442,19 @@ __global__ void k_batch_build(BatchDev B, int with_tiles) {
   }
 }
 
+// The same lists for every active instance of a batch (instance i's lists at
+// weak + weak_off[i]), one warp per variable.
+template <int WT>
+__global__ void k_batch_weak(BatchDev B) {
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int g = gw; g < B.total_vars; g += nw) {
+    const int inst = B.var_inst[g];
+    if (!B.act[inst] || B.inc[inst]) continue;
+    weak_lists_of<WT>(B.nets[inst], B.roots[inst], g - B.var_base[inst], B.weak + B.weak_off[inst]);
+  }
+}
+
 template <int WT>
 // quota > 0: a CTA takes at most quota tiles and retires (the grid then
 // covers every tile), so that CTAs of other streams get SMs between tiles.
@@ -1459,7 +1480,7 @@ __global__ void __launch_bounds__(256, WT <= 2 ? 4 : 1) k_batch_tile(BatchDev B,
     if (t >= total) break;
     const int4 tl = B.tiles[t];
     const int inst = tl.x >> 16;
-    tile_one<WT>(sN, B.roots[inst], nullptr, tl.x & 0xffff, tl.y, tl.z, static_cast<u32>(tl.w), B.ok, B.deep, B.ndeep,
+    tile_one<WT>(sN, B.roots[inst], B.weak ? B.weak + B.weak_off[inst] : nullptr, tl.x & 0xffff, tl.y, tl.z, static_cast<u32>(tl.w), B.ok, B.deep, B.ndeep,
                  slot_cap, T, slot_of, s_fail, s_deep, c_rev, c_rows, c_done);
   }
   flush_tile_counts(st, c_rev, c_rows, c_done);
@@ -1860,6 +1881,15 @@ cudaError_t launch_batch_build(int W, const BatchDev& B, bool with_tiles, cudaSt
     constexpr int WT = decltype(wt)::value;
     const int blocks = std::max(1, std::min(8192, (B.total_vars * 32 + 255) / 256));
     k_batch_build<WT><<<blocks, 256, 0, s>>>(B, with_tiles ? 1 : 0);
+    return cudaGetLastError();
+  });
+}
+
+cudaError_t launch_batch_weak(int W, const BatchDev& B, cudaStream_t s) {
+  return dispatch_w(W, [&](auto wt) -> cudaError_t {
+    constexpr int WT = decltype(wt)::value;
+    const int blocks = std::max(1, std::min(8192, (B.total_vars * 32 + 255) / 256));
+    k_batch_weak<WT><<<blocks, 256, 0, s>>>(B);
     return cudaGetLastError();
   });
 }
