@@ -45,17 +45,24 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """dram bytes per launch of the batched branch kernel from the committed
-    ncu summary (line 'traffic_bytes_per_launch: N'), or None."""
-    path = os.path.join(ROOT, "profiles", "k_sac_cfg3_sweep.md")
+def profile_field(name):
+    """A 'name: value' line of the committed ncu summary of the SAC sweep
+    kernels (profiles/k_sac_tile_cfg3_sweep.md), or None."""
+    path = os.path.join(ROOT, "profiles", "k_sac_tile_cfg3_sweep.md")
     try:
         for line in open(path):
-            if line.startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":", 1)[1].split()[0])
+            if line.startswith(name + ":"):
+                return line.split(":", 1)[1].strip()
     except OSError:
         pass
     return None
+
+
+def profile_traffic():
+    """DRAM bytes (read + write) per sweep of the SAC sweep kernels, from the
+    committed ncu summary, or None."""
+    v = profile_field("traffic_bytes_per_launch")
+    return float(v.split()[0]) if v else None
 
 
 class ClockSampler:
@@ -301,10 +308,11 @@ def run_ours(args):
         "gpu_launches": int(gpu_launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "kernel": "k_sac (batched singleton fixpoints)",
+                     "kernel": "SAC sweep kernels (k_weak + k_sac_tile + k_sac on the deep list), per sweep",
                      "kernel_ms_per_launch": kern_ms / max(1, launches_k),
                      "alg_bytes_per_launch": kern_bytes / max(1, launches_k),
-                     "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"},
+                     "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                     "limiter": profile_field("limiter")},
         "cpu_baseline": {k2: base[k2] for k2 in ("value", "unit", "cores", "kind", "sample")},
         "plain_single_instance": {"value": plain_rate, "unit": UNIT,
                                   "sample": "%d singleton tests, one single-CTA launch each" % k,
@@ -403,7 +411,7 @@ def run_uneven(args):
 
 
 SERVING_WORKLOAD = ("serving: Poisson arrivals, requests propagate:SAC:MAC-solve = 70:20:10 on {r} resident networks "
-                    "(random binary CSPs, n~U[20,400], d in {{8..256}}, density~U[0.05,0.3], tightness~U[0.2,0.6], "
+                    "(random binary CSPs, n~U[20,400], d in {{8..128}}, density~U[0.05,0.3], tightness~U[0.2,0.6], "
                     "seeds 5*1000003+i), 0-3 random variable choices per request, HBM budget 150 GB")
 
 
@@ -434,8 +442,9 @@ def run_serving(args):
     R = args.networks
     seeds = [5 * 1000003 + i for i in range(R)]
     t0 = time.time()
-    hs = [cp.InstanceHandle.uneven(sd, 20, 400, 256) for sd in seeds]
-    shapes = [cp._uneven_shape(sd, 20, 400, 256) for sd in seeds]
+    # Config 4's size distribution capped at config 3's shape (d <= 128).
+    hs = [cp.InstanceHandle.uneven(sd, 20, 400, 128) for sd in seeds]
+    shapes = [cp._uneven_shape(sd, 20, 400, 128) for sd in seeds]
     gen_s = time.time() - t0
     rates = [float(x) for x in args.rates.split(",")]
     modes = [("batched", True), ("plain", False)]
