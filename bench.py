@@ -79,7 +79,7 @@ class ClockSampler:
              "clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -158,7 +158,7 @@ def run_reference(args):
     vals = []
     # Each step is a bounded sample sized so the whole run stays near 90 s of
     # wall time on the host's cores.
-    per_step_wall = max(0.25, 90.0 / max(1, args.warmup + args.steps))
+    per_step_wall = max(0.05, 90.0 / max(1, args.warmup + args.steps))
     for i in range(args.warmup + args.steps):
         r = cpu_baseline_port(inst, threads, budget_s=per_step_wall * threads)
         if i >= args.warmup:
@@ -505,7 +505,7 @@ def run_serving(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="timed steps only (for profiling)")
