@@ -1035,111 +1035,127 @@ __device__ __forceinline__ void tile_one(const DevNet& N, const u64* root, const
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) thr = max(thr, __shfl_xor_sync(kFull, thr, o));
         const int y0 = N.arc_start[y], y1 = N.arc_start[y + 1];
-        for (int j = y0; j < y1; ++j) {
+        for (int jb = y0; jb < y1; jb += 32) {
           // Lanes still open (live, not failed, not handed over), warp-uniform.
           const u32 done_m = __shfl_sync(kFull, *reinterpret_cast<volatile u32*>(&s_fail) |
                                                     *reinterpret_cast<volatile u32*>(&s_deep), 0);
           const u32 open = live & ~done_m;
           if (!open) break;
-          const Arc A = N.arcs[j];
-          const int z = A.z;
-          if (z == x) continue;
-          const int sz = slot_of[z];
-          u64 cur[WT];
-          if (sz >= 0) {
-#pragma unroll
-            for (int w = 0; w < WT; ++w) cur[w] = T[(static_cast<size_t>(sz) * 32 + lane) * WT + w];
-          } else {
-#pragma unroll
-            for (int w = 0; w < WT; ++w) cur[w] = __ldg(root + static_cast<size_t>(z) * WT + w);
+          // 32 arcs classified at once (lane l: arc jb + l), so their loads
+          // overlap: an arc whose weakest value of z has more supports than
+          // any lane's D(y) lost can remove nothing and needs no test.
+          const int jl = jb + lane;
+          bool arc_in = false, act = false;
+          if (jl < y1) {
+            arc_in = N.arcs[jl].z != x;
+            const u32 e0 = weak ? __ldg(weak + static_cast<size_t>(jl) * (kWeakK + 1)) : 0u;
+            act = arc_in && static_cast<int>(e0 >> 16) <= thr;
           }
-          const bool mine = (open >> lane) & 1u;
-          bool still = false, left = false;
-          int loaded = 0;
-          const u32* wl = weak ? weak + static_cast<size_t>(j) * (kWeakK + 1) : nullptr;
-          if (wl && static_cast<int>(__ldg(wl + kWeakK) >> 16) > thr) {
-            // Weak values only: v loses all supports iff its row misses D(y).
-            int unsup = 0;
-            for (int k = 0; k < kWeakK; ++k) {
-              const u32 e = __ldg(wl + k);
-              const int cnt = static_cast<int>(e >> 16);
-              if (cnt > thr) break;
-              const int v = static_cast<int>(e & 0xffffu);
-              const bool need =
-                  mine && removed >= cnt && ((sel<WT>(cur, v >> 6) >> (v & 63)) & 1ull);
-              if (__ballot_sync(kFull, need) == 0) continue;
-              u64 r[WT];
-              load_row<WT>(N.rel, A.zy + static_cast<size_t>(v) * WT, r);
-              ++loaded;
-              u64 hit = 0;
+          const u32 arcs_m = __ballot_sync(kFull, arc_in);
+          u32 todo = __ballot_sync(kFull, act);
+          if (lane == 0) c_rev += __popc(arcs_m & ~todo);
+          while (todo) {
+            const int j = jb + __ffs(todo) - 1;
+            todo &= todo - 1;
+            const Arc A = N.arcs[j];
+            const int z = A.z;
+            const int sz = slot_of[z];
+            u64 cur[WT];
+            if (sz >= 0) {
 #pragma unroll
-              for (int q = 0; q < WT; ++q) hit |= r[q] & dy[q];
-              if (need && hit == 0) ++unsup;
+              for (int w = 0; w < WT; ++w) cur[w] = T[(static_cast<size_t>(sz) * 32 + lane) * WT + w];
+            } else {
+#pragma unroll
+              for (int w = 0; w < WT; ++w) cur[w] = __ldg(root + static_cast<size_t>(z) * WT + w);
             }
-            if (unsup) {
-              int size = 0;
+            const bool mine = (open >> lane) & 1u;
+            bool still = false, left = false;
+            int loaded = 0;
+            const u32* wl = weak ? weak + static_cast<size_t>(j) * (kWeakK + 1) : nullptr;
+            if (wl && static_cast<int>(__ldg(wl + kWeakK) >> 16) > thr) {
+              // Weak values only: v loses all supports iff its row misses D(y).
+              int unsup = 0;
+              for (int k = 0; k < kWeakK; ++k) {
+                const u32 e = __ldg(wl + k);
+                const int cnt = static_cast<int>(e >> 16);
+                if (cnt > thr) break;
+                const int v = static_cast<int>(e & 0xffffu);
+                const bool need =
+                    mine && removed >= cnt && ((sel<WT>(cur, v >> 6) >> (v & 63)) & 1ull);
+                if (__ballot_sync(kFull, need) == 0) continue;
+                u64 r[WT];
+                load_row<WT>(N.rel, A.zy + static_cast<size_t>(v) * WT, r);
+                ++loaded;
+                u64 hit = 0;
 #pragma unroll
-              for (int q = 0; q < WT; ++q) size += __popcll(cur[q]);
-              still = true;
-              left = unsup < size;
-            }
-          } else {
-            u64 uc[WT], acc[WT];
+                for (int q = 0; q < WT; ++q) hit |= r[q] & dy[q];
+                if (need && hit == 0) ++unsup;
+              }
+              if (unsup) {
+                int size = 0;
 #pragma unroll
-            for (int w = 0; w < WT; ++w) {
-              uc[w] = warp_or64(mine ? dy[w] : 0ull);
-              acc[w] = 0;
-            }
-            // Rows of the values of y that some open lane still has, 32 values
-            // per chunk, 8 rows between coverage tests; a lane ORs the rows of
-            // its own values (a predicated OR per row: the row address and the
-            // skip test are warp-uniform). Stops once every open lane's
-            // accumulated support covers its D(z).
-            bool go = true;
+                for (int q = 0; q < WT; ++q) size += __popcll(cur[q]);
+                still = true;
+                left = unsup < size;
+              }
+            } else {
+              u64 uc[WT], acc[WT];
 #pragma unroll
-            for (int h = 0; h < 2 * WT; ++h) {
-              const u32 ucw = static_cast<u32>(sel<WT>(uc, h >> 1) >> ((h & 1) * 32));
-              const u32 myb = mine ? static_cast<u32>(sel<WT>(dy, h >> 1) >> ((h & 1) * 32)) : 0u;
-              if (ucw == 0) continue;
-              const u64* rc = N.rel + A.yz + static_cast<size_t>(h) * 32 * WT;
+              for (int w = 0; w < WT; ++w) {
+                uc[w] = warp_or64(mine ? dy[w] : 0ull);
+                acc[w] = 0;
+              }
+              // Rows of the values of y that some open lane still has, 32 values
+              // per chunk, 8 rows between coverage tests; a lane ORs the rows of
+              // its own values (a predicated OR per row: the row address and the
+              // skip test are warp-uniform). Stops once every open lane's
+              // accumulated support covers its D(z).
+              bool go = true;
 #pragma unroll
-              for (int j0 = 0; j0 < 32; j0 += 8) {
-                const u32 chunk = (ucw >> j0) & 0xffu;
-                if (!go || chunk == 0) continue;
+              for (int h = 0; h < 2 * WT; ++h) {
+                const u32 ucw = static_cast<u32>(sel<WT>(uc, h >> 1) >> ((h & 1) * 32));
+                const u32 myb = mine ? static_cast<u32>(sel<WT>(dy, h >> 1) >> ((h & 1) * 32)) : 0u;
+                if (ucw == 0) continue;
+                const u64* rc = N.rel + A.yz + static_cast<size_t>(h) * 32 * WT;
 #pragma unroll
-                for (int jj = 0; jj < 8; ++jj) {
-                  if ((chunk >> jj) & 1u) {
-                    u64 r[WT];
-                    load_row<WT>(rc, static_cast<size_t>(j0 + jj) * WT, r);
-                    ++loaded;
-                    if ((myb >> (j0 + jj)) & 1u) {
+                for (int j0 = 0; j0 < 32; j0 += 8) {
+                  const u32 chunk = (ucw >> j0) & 0xffu;
+                  if (!go || chunk == 0) continue;
 #pragma unroll
-                      for (int q = 0; q < WT; ++q) acc[q] |= r[q];
+                  for (int jj = 0; jj < 8; ++jj) {
+                    if ((chunk >> jj) & 1u) {
+                      u64 r[WT];
+                      load_row<WT>(rc, static_cast<size_t>(j0 + jj) * WT, r);
+                      ++loaded;
+                      if ((myb >> (j0 + jj)) & 1u) {
+#pragma unroll
+                        for (int q = 0; q < WT; ++q) acc[q] |= r[q];
+                      }
                     }
                   }
+                  u64 gap = 0;
+#pragma unroll
+                  for (int q = 0; q < WT; ++q) gap |= cur[q] & ~acc[q];
+                  if (__ballot_sync(kFull, mine && gap != 0) == 0) go = false;  // every open lane covered
                 }
-                u64 gap = 0;
+              }
+              if (go) {
+                u64 gap = 0, kept = 0;
 #pragma unroll
-                for (int q = 0; q < WT; ++q) gap |= cur[q] & ~acc[q];
-                if (__ballot_sync(kFull, mine && gap != 0) == 0) go = false;  // every open lane covered
+                for (int q = 0; q < WT; ++q) {
+                  gap |= cur[q] & ~acc[q];
+                  kept |= cur[q] & acc[q];
+                }
+                still = mine && gap != 0;
+                left = kept != 0;
               }
             }
-            if (go) {
-              u64 gap = 0, kept = 0;
-#pragma unroll
-              for (int q = 0; q < WT; ++q) {
-                gap |= cur[q] & ~acc[q];
-                kept |= cur[q] & acc[q];
-              }
-              still = mine && gap != 0;
-              left = kept != 0;
+            if (lane == 0) {
+              ++c_rev;
+              c_rows += loaded;
             }
+            if (still) atomicOr(left ? &s_deep : &s_fail, 1u << lane);
           }
-          if (lane == 0) {
-            ++c_rev;
-            c_rows += loaded;
-          }
-          if (still) atomicOr(left ? &s_deep : &s_fail, 1u << lane);
         }
       }
       __syncthreads();
