@@ -59,6 +59,12 @@ __device__ __forceinline__ u64 warp_or64(u64 x) {
   return (static_cast<u64>(hi) << 32) | lo;
 }
 
+__device__ __forceinline__ u64 shfl64(u64 x, int src) {
+  const u32 lo = __shfl_sync(kFull, static_cast<u32>(x), src);
+  const u32 hi = __shfl_sync(kFull, static_cast<u32>(x >> 32), src);
+  return (static_cast<u64>(hi) << 32) | lo;
+}
+
 // Support rows are read-only during a launch: non-coherent 128-bit loads.
 template <int WT>
 __device__ __forceinline__ void load_row(const u64* rel, size_t off, u64 (&r)[WT]) {
@@ -1071,24 +1077,31 @@ __device__ __forceinline__ void tile_one(const DevNet& N, const u64* root, const
             const bool mine = (open >> lane) & 1u;
             bool still = false, left = false;
             int loaded = 0;
+            // Lane k < kWeakK holds list entry k, lane kWeakK the next count;
+            // the lanes of candidate entries load their rows at once.
             const u32* wl = weak ? weak + static_cast<size_t>(j) * (kWeakK + 1) : nullptr;
-            if (wl && static_cast<int>(__ldg(wl + kWeakK) >> 16) > thr) {
+            const u32 ent = (wl && lane <= kWeakK) ? __ldg(wl + lane) : 0xffffffffu;
+            const int next_cnt = static_cast<int>(__shfl_sync(kFull, ent, kWeakK) >> 16);
+            if (wl && next_cnt > thr) {
               // Weak values only: v loses all supports iff its row misses D(y).
+              const bool cand = lane < kWeakK && static_cast<int>(ent >> 16) <= thr;
+              u64 row[WT];
+#pragma unroll
+              for (int q = 0; q < WT; ++q) row[q] = 0;
+              if (cand) load_row<WT>(N.rel, A.zy + static_cast<size_t>(ent & 0xffffu) * WT, row);
+              u32 cm = __ballot_sync(kFull, cand);
+              loaded = __popc(cm);
               int unsup = 0;
-              for (int k = 0; k < kWeakK; ++k) {
-                const u32 e = __ldg(wl + k);
+              while (cm) {
+                const int k = __ffs(cm) - 1;
+                cm &= cm - 1;
+                const u32 e = __shfl_sync(kFull, ent, k);
                 const int cnt = static_cast<int>(e >> 16);
-                if (cnt > thr) break;
                 const int v = static_cast<int>(e & 0xffffu);
-                const bool need =
-                    mine && removed >= cnt && ((sel<WT>(cur, v >> 6) >> (v & 63)) & 1ull);
-                if (__ballot_sync(kFull, need) == 0) continue;
-                u64 r[WT];
-                load_row<WT>(N.rel, A.zy + static_cast<size_t>(v) * WT, r);
-                ++loaded;
                 u64 hit = 0;
 #pragma unroll
-                for (int q = 0; q < WT; ++q) hit |= r[q] & dy[q];
+                for (int q = 0; q < WT; ++q) hit |= shfl64(row[q], k) & dy[q];
+                const bool need = mine && removed >= cnt && ((sel<WT>(cur, v >> 6) >> (v & 63)) & 1ull);
                 if (need && hit == 0) ++unsup;
               }
               if (unsup) {
