@@ -1197,61 +1197,71 @@ __device__ __forceinline__ void tile_one(const DevNet& N, const u64* root, const
 // Weak-support lists for the root domains: per directional arc j (revise z
 // against y), the kWeakK values v of D(z) with the fewest supports
 // |row_zy(v) & D(y)| in increasing (count, v) order as count << 16 | v, then
-// the next count << 16 (0xffff: none). One warp per source variable y; the
-// smallest keys are taken by repeated warp minima.
+// the next count << 16 (0xffff: none). One warp per arc; the smallest keys are
+// taken by repeated warp minima.
 template <int WT>
-__device__ void weak_lists_of(const DevNet& N, const u64* root, int y, u32* weak) {
+__device__ void weak_list_arc(const DevNet& N, const u64* root, const u64 (&dy)[WT], int j, u32* weak) {
   const int lane = threadIdx.x & 31;
-  u64 dy[WT];
-  load_dom_uniform<WT>(root + static_cast<size_t>(y) * WT, dy);
-  for (int j = N.arc_start[y]; j < N.arc_start[y + 1]; ++j) {
-    const Arc A = N.arcs[j];
-    const int z = A.z, dz = N.dsize[z];
-    u64 d0z[WT];
-    load_dom_uniform<WT>(root + static_cast<size_t>(z) * WT, d0z);
-    u32 key[2 * WT];
+  const Arc A = N.arcs[j];
+  const int z = A.z, dz = N.dsize[z];
+  u64 d0z[WT];
+  load_dom_uniform<WT>(root + static_cast<size_t>(z) * WT, d0z);
+  u32 key[2 * WT];
 #pragma unroll
-    for (int t = 0; t < 2 * WT; ++t) {
-      const int v = t * 32 + lane;
-      key[t] = 0xffffffffu;
-      if (v < dz && ((sel<WT>(d0z, v >> 6) >> (v & 63)) & 1ull)) {
-        u64 r[WT];
-        load_row<WT>(N.rel, A.zy + static_cast<size_t>(v) * WT, r);
-        int c = 0;
+  for (int t = 0; t < 2 * WT; ++t) {
+    const int v = t * 32 + lane;
+    key[t] = 0xffffffffu;
+    if (v < dz && ((sel<WT>(d0z, v >> 6) >> (v & 63)) & 1ull)) {
+      u64 r[WT];
+      load_row<WT>(N.rel, A.zy + static_cast<size_t>(v) * WT, r);
+      int c = 0;
 #pragma unroll
-        for (int w = 0; w < WT; ++w) c += __popcll(r[w] & dy[w]);
-        key[t] = (static_cast<u32>(c) << 16) | static_cast<u32>(v);
-      }
+      for (int w = 0; w < WT; ++w) c += __popcll(r[w] & dy[w]);
+      key[t] = (static_cast<u32>(c) << 16) | static_cast<u32>(v);
     }
-    u32* out = weak + static_cast<size_t>(j) * (kWeakK + 1);
-    for (int k = 0; k <= kWeakK; ++k) {
-      u32 m = key[0];
+  }
+  u32* out = weak + static_cast<size_t>(j) * (kWeakK + 1);
+  for (int k = 0; k <= kWeakK; ++k) {
+    u32 m = key[0];
 #pragma unroll
-      for (int t = 1; t < 2 * WT; ++t) m = min(m, key[t]);
-      m = __reduce_min_sync(kFull, m);
-      if (lane == 0) out[k] = k < kWeakK ? m : (m | 0xffffu);
-      if (m == 0xffffffffu) {
-        if (lane == 0)
-          for (int r = k + 1; r <= kWeakK; ++r) out[r] = 0xffffffffu;
-        break;
-      }
-#pragma unroll
-      for (int t = 0; t < 2 * WT; ++t)
-        if (key[t] == m) key[t] = 0xffffffffu;
+    for (int t = 1; t < 2 * WT; ++t) m = min(m, key[t]);
+    m = __reduce_min_sync(kFull, m);
+    if (lane == 0) out[k] = k < kWeakK ? m : (m | 0xffffu);
+    if (m == 0xffffffffu) {
+      if (lane == 0)
+        for (int r = k + 1; r <= kWeakK; ++r) out[r] = 0xffffffffu;
+      break;
     }
+#pragma unroll
+    for (int t = 0; t < 2 * WT; ++t)
+      if (key[t] == m) key[t] = 0xffffffffu;
   }
 }
 
-// Weak-support lists for the root domains: per directional arc j (revise z
-// against y), the kWeakK values v of D(z) with the fewest supports
-// |row_zy(v) & D(y)| in increasing (count, v) order as count << 16 | v, then
-// the next count << 16 (0xffff: none). One warp per source variable y; the
-// smallest keys are taken by repeated warp minima.
+// Lists of all arcs of source variable y (one warp).
+template <int WT>
+__device__ void weak_lists_of(const DevNet& N, const u64* root, int y, u32* weak) {
+  u64 dy[WT];
+  load_dom_uniform<WT>(root + static_cast<size_t>(y) * WT, dy);
+  for (int j = N.arc_start[y]; j < N.arc_start[y + 1]; ++j) weak_list_arc<WT>(N, root, dy, j, weak);
+}
+
 template <int WT>
 __global__ void k_weak(DevNet N, const u64* root, u32* weak) {
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nw = (gridDim.x * blockDim.x) >> 5;
-  for (int y = gw; y < N.n; y += nw) weak_lists_of<WT>(N, root, y, weak);
+  const int narcs = N.arc_start[N.n];
+  for (int j = gw; j < narcs; j += nw) {
+    // Source variable of arc j: the last y with arc_start[y] <= j.
+    int lo = 0, hi = N.n - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (N.arc_start[mid] <= j) lo = mid; else hi = mid - 1;
+    }
+    u64 dy[WT];
+    load_dom_uniform<WT>(root + static_cast<size_t>(lo) * WT, dy);
+    weak_list_arc<WT>(N, root, dy, j, weak);
+  }
 }
 
 __device__ __forceinline__ void flush_tile_counts(KStats* st, u64 c_rev, u64 c_rows, u64 c_done) {
@@ -1823,7 +1833,7 @@ cudaError_t launch_sac_tile(const DevNet& N, const u64* root, SacScratch S, uint
 cudaError_t launch_weak(const DevNet& N, const u64* root, u32* weak, cudaStream_t s) {
   return dispatch_w(N.W, [&](auto wt) -> cudaError_t {
     constexpr int WT = decltype(wt)::value;
-    const int blocks = std::max(1, std::min(4096, (N.n * 32 + 255) / 256));
+    const int blocks = std::max(1, std::min(8192, (2 * N.nb * 32 + 255) / 256));
     k_weak<WT><<<blocks, 256, 0, s>>>(N, root, weak);
     return cudaGetLastError();
   });
