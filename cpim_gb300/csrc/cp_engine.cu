@@ -22,6 +22,9 @@
 
 using namespace cpgpu;
 
+// Threads per CTA of the tiled SAC sweep (one tile of 32 branches per CTA).
+constexpr int kTileBlock = 256;
+
 namespace {
 
 thread_local std::string g_last_error;
@@ -715,7 +718,7 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
     if (static_cast<size_t>(n) * 4 + per_slot * 8 <= budget) {
       const size_t fit = (budget - static_cast<size_t>(n) * 4) / per_slot;
       net->slot_cap = static_cast<int>(std::min<size_t>(static_cast<size_t>(cap), fit));
-      const int per_sm_t = sac_tile_blocks_per_sm(D, net->slot_cap, 256);
+      const int per_sm_t = sac_tile_blocks_per_sm(D, net->slot_cap, kTileBlock);
       net->tile_grid = per_sm_t > 0 ? per_sm_t * e->sm_count : 0;
     }
   }
@@ -925,7 +928,7 @@ int cp_enforce_sac1(cp_net* net, int level, cp_stats* st) {
         launches += 1;
         e->launches += 1;
       }
-      CP_CUDA(launch_sac_tile(net->dn, net->level_ptr(level), S, S.ok, net->slot_cap, net->d_stats, 256,
+      CP_CUDA(launch_sac_tile(net->dn, net->level_ptr(level), S, S.ok, net->slot_cap, net->d_stats, kTileBlock,
                               net->tile_grid, s));
       CP_CUDA(launch_sac_branches(net->dn, net->level_ptr(level), S.work, S.nwork, S.cursor, S.ok, net->d_stats,
                                   e->block_sac, net->sac_grid, net->d_sac_scratch, net->sac_stride, s, S.deep,
