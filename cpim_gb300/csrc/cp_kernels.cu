@@ -984,7 +984,7 @@ __device__ __forceinline__ int pop_low(u64& m, int word) {
 template <int WT>
 __device__ __forceinline__ void tile_one(const DevNet& N, const u64* root, const u32* weak, int x, int base, int b0,
                                          u32 live, uint8_t* ok, int* deep, int* ndeep, int slot_cap, u64* T,
-                                         int* slot_of, u32& s_fail, u32& s_deep, u64& c_rev, u64& c_rows,
+                                         int* slot_of, u32& s_fail, u32& s_deep, int& s_next, u64& c_rev, u64& c_rows,
                                          u64& c_done) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   {
@@ -1022,9 +1022,15 @@ __device__ __forceinline__ void tile_one(const DevNet& N, const u64* root, const
         for (int w = 0; w < WT; ++w) any |= T[(static_cast<size_t>(i) * 32 + l) * WT + w];
         if (!any) atomicOr(&s_fail, 1u << l);
       }
+      if (threadIdx.x == 0) s_next = 0;
       __syncthreads();
-      // Round two, tested only.
-      for (int s = warp; s < deg; s += nwarps) {
+      // Round two, tested only; warps take neighbours y dynamically (their
+      // costs differ), so fewer wait at the barrier that ends the tile.
+      for (;;) {
+        int s = 0;
+        if (lane == 0) s = atomicAdd(&s_next, 1);
+        s = __shfl_sync(kFull, s, 0);
+        if (s >= deg) break;
         const int y = N.arcs[a0 + s].z;
         if (slot_of[y] != s) continue;
         u64 dy[WT];
@@ -1285,6 +1291,7 @@ __global__ void __launch_bounds__(256, WT <= 2 ? 4 : 1) k_sac_tile(DevNet N, con
   int* slot_of = reinterpret_cast<int*>(smem_raw + static_cast<size_t>(slot_cap) * 32 * WT * 8);  // [n]
   __shared__ int s_t;
   __shared__ u32 s_fail, s_deep;
+  __shared__ int s_next;
   const int total = *ntiles;
   for (int i = threadIdx.x; i < N.n; i += blockDim.x) slot_of[i] = -1;
   u64 c_rev = 0, c_rows = 0, c_done = 0;
@@ -1299,7 +1306,7 @@ __global__ void __launch_bounds__(256, WT <= 2 ? 4 : 1) k_sac_tile(DevNet N, con
     if (t >= total) break;
     const int4 tl = tiles[t];
     tile_one<WT>(N, root, weak, tl.x, tl.y, tl.z, static_cast<u32>(tl.w), ok, deep, ndeep, slot_cap, T, slot_of, s_fail,
-                 s_deep, c_rev, c_rows, c_done);
+                 s_deep, s_next, c_rev, c_rows, c_done);
   }
   flush_tile_counts(st, c_rev, c_rows, c_done);
 }
@@ -1503,6 +1510,7 @@ __global__ void __launch_bounds__(256, WT <= 2 ? 4 : 1) k_batch_tile(BatchDev B,
   int* slot_of = reinterpret_cast<int*>(smem_raw + static_cast<size_t>(slot_cap) * 32 * WT * 8);
   __shared__ int s_t;
   __shared__ u32 s_fail, s_deep;
+  __shared__ int s_next;
   __shared__ DevNet sN;
   const int total = *B.ntiles;
   for (int i = threadIdx.x; i < max_n; i += blockDim.x) slot_of[i] = -1;
@@ -1520,7 +1528,7 @@ __global__ void __launch_bounds__(256, WT <= 2 ? 4 : 1) k_batch_tile(BatchDev B,
     const int4 tl = B.tiles[t];
     const int inst = tl.x >> 16;
     tile_one<WT>(sN, B.roots[inst], B.weak ? B.weak + B.weak_off[inst] : nullptr, tl.x & 0xffff, tl.y, tl.z, static_cast<u32>(tl.w), B.ok, B.deep, B.ndeep,
-                 slot_cap, T, slot_of, s_fail, s_deep, c_rev, c_rows, c_done);
+                 slot_cap, T, slot_of, s_fail, s_deep, s_next, c_rev, c_rows, c_done);
   }
   flush_tile_counts(st, c_rev, c_rows, c_done);
 }
