@@ -1027,9 +1027,10 @@ __device__ __forceinline__ void tile_one(const DevNet& N, const u64* root, const
       // Round two, tested only; warps take neighbours y dynamically (their
       // costs differ), so fewer wait at the barrier that ends the tile.
       for (;;) {
-        int s = 0;
-        if (lane == 0) s = atomicAdd(&s_next, 1);
-        s = __shfl_sync(kFull, s, 0);
+        int item = 0;
+        if (lane == 0) item = atomicAdd(&s_next, 1);
+        item = __shfl_sync(kFull, item, 0);
+        const int s = item >> 1, half = item & 1;  // two items per neighbour: alternate 32-arc chunks
         if (s >= deg) break;
         const int y = N.arcs[a0 + s].z;
         if (slot_of[y] != s) continue;
@@ -1047,7 +1048,7 @@ __device__ __forceinline__ void tile_one(const DevNet& N, const u64* root, const
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) thr = max(thr, __shfl_xor_sync(kFull, thr, o));
         const int y0 = N.arc_start[y], y1 = N.arc_start[y + 1];
-        for (int jb = y0; jb < y1; jb += 32) {
+        for (int jb = y0 + 32 * half; jb < y1; jb += 64) {
           // Lanes still open (live, not failed, not handed over), warp-uniform.
           const u32 done_m = __shfl_sync(kFull, *reinterpret_cast<volatile u32*>(&s_fail) |
                                                     *reinterpret_cast<volatile u32*>(&s_deep), 0);
