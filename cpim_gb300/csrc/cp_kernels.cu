@@ -1284,7 +1284,7 @@ __device__ __forceinline__ void flush_tile_counts(KStats* st, u64 c_rev, u64 c_r
 }
 
 template <int WT>
-__global__ void __launch_bounds__(256, WT <= 2 ? 4 : 1) k_sac_tile(DevNet N, const u64* root, const int4* tiles, const int* ntiles,
+__global__ void __launch_bounds__(256, WT <= 2 ? 5 : 1) k_sac_tile(DevNet N, const u64* root, const int4* tiles, const int* ntiles,
                                                   int* tcursor, uint8_t* ok, int* deep, int* ndeep, int slot_cap,
                                                   KStats* st, const u32* weak) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
