@@ -994,26 +994,39 @@ __device__ __forceinline__ void tile_one(const DevNet& N, const u64* root, const
       // Round one: slots for the distinct neighbours, D_a(y) = D0(y) & rows.
       for (int i = threadIdx.x; i < deg; i += blockDim.x) atomicCAS(&slot_of[N.arcs[a0 + i].z], -1, i);
       __syncthreads();
-      for (int k = threadIdx.x; k < deg * 32; k += blockDim.x) {
-        const int i = k >> 5, l = k & 31;
-        const int z = N.arcs[a0 + i].z;
-        if (slot_of[z] == i) {
-#pragma unroll
-          for (int w = 0; w < WT; ++w) T[(static_cast<size_t>(i) * 32 + l) * WT + w] = root[static_cast<size_t>(z) * WT + w];
-        }
-      }
-      __syncthreads();
+      // The first arc to each neighbour z writes D_a(z) = D0(z) & row(x = a)
+      // (lanes without a branch keep D0(z)); further constraints on the same
+      // pair, if any, AND their rows in afterwards.
+      bool dup = false;
       for (int i = warp; i < deg; i += nwarps) {
         const Arc A = N.arcs[a0 + i];
-        const int s = slot_of[A.z];
+        if (slot_of[A.z] != i) {
+          dup = true;
+          continue;
+        }
+        u64 d[WT], r[WT];
+#pragma unroll
+        for (int w = 0; w < WT; ++w) d[w] = root[static_cast<size_t>(A.z) * WT + w];
         if ((live >> lane) & 1u) {
+          load_row<WT>(N.rel, A.yz + static_cast<size_t>(base + lane) * WT, r);
+#pragma unroll
+          for (int w = 0; w < WT; ++w) d[w] &= r[w];
+        }
+#pragma unroll
+        for (int w = 0; w < WT; ++w) T[(static_cast<size_t>(i) * 32 + lane) * WT + w] = d[w];
+      }
+      if (__syncthreads_or(dup)) {
+        for (int i = warp; i < deg; i += nwarps) {
+          const Arc A = N.arcs[a0 + i];
+          const int s = slot_of[A.z];
+          if (s == i || !((live >> lane) & 1u)) continue;
           u64 r[WT];
           load_row<WT>(N.rel, A.yz + static_cast<size_t>(base + lane) * WT, r);
 #pragma unroll
           for (int w = 0; w < WT; ++w) atomicAnd(&T[(static_cast<size_t>(s) * 32 + lane) * WT + w], r[w]);
         }
+        __syncthreads();
       }
-      __syncthreads();
       for (int k = threadIdx.x; k < deg * 32; k += blockDim.x) {
         const int i = k >> 5, l = k & 31;
         if (slot_of[N.arcs[a0 + i].z] != i || !((live >> l) & 1u)) continue;
