@@ -231,3 +231,32 @@ def test_level_ops_round_trip(engine):
     net.dom_set(2, d0)
     assert np.array_equal(net.dom_get(2), d0)
     net.close()
+
+
+@pytest.mark.parametrize("p", [0.5, 0.6])
+def test_sac_tiled_with_repeated_pairs(p):
+    # Two constraints on the same variable pair (the union of two networks
+    # over the same variables): the tiled sweep ANDs both rows into one
+    # neighbour slot, and must still give the oracle's SAC closure (0.5:
+    # consistent, 0.6: SAC wipe-out).
+    a = cp.gen_binary(30, 64, 200, p, p, 0.0, 11)
+    b = cp.gen_binary(30, 64, 200, p, p, 0.0, 12)
+    pairs_a = {tuple(sorted(p)) for p in a.bin_scope.reshape(-1, 2).tolist()}
+    pairs_b = {tuple(sorted(p)) for p in b.bin_scope.reshape(-1, 2).tolist()}
+    assert pairs_a & pairs_b  # the union repeats some pairs
+    inst = cp.Instance(n=a.n, W=a.W, dom=a.dom, init=a.init,
+                       bin_scope=np.concatenate([a.bin_scope, b.bin_scope]),
+                       bin_rows=np.concatenate([a.bin_rows, b.bin_rows]),
+                       tab_arity=a.tab_arity, tab_scope=a.tab_scope, tab_ntup=a.tab_ntup,
+                       tab_tuples=a.tab_tuples)
+    ok_o, d_o, dels_o = O.sac1(oracle_view_of(inst))
+    for mode in (0, 1):
+        with cp.Engine(0) as eng:
+            eng.set_sac_mode(mode)
+            net = eng.upload(inst)
+            st = net.enforce_sac1(0)
+            assert bool(st.inconsistent) == (not ok_o), mode
+            if ok_o:
+                assert np.array_equal(net.dom_get(0), d_o), mode
+                assert st.deletions == dels_o, mode
+            net.close()
