@@ -502,6 +502,124 @@ def run_serving(args):
     return 0
 
 
+def run_gac(args):
+    """Config-2 measurement: one GAC fixpoint of the large mixed network
+    (binary rows + ternary positive tables, 20% of values removed) on the
+    grid-wide persistent kernel; revisions/s and algorithmic GB/s. The
+    published shape (500 tuples per table) has an empty GAC closure, so a
+    second shape with 1200 tuples per table gives a full fixpoint."""
+    import torch
+    import cpim_gb300 as cp
+    from oracle import pyoracle as O
+
+    torch.cuda.set_device(0)
+    peak, peak_kind = measured_peaks()
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    eng = cp.Engine(0)
+    out = []
+    for ntup in (500, 1200):
+        inst = cp.gen_mixed(2000, 64, 30000, 0.2, 0.5, 5000, ntup, 0.2, 1)
+        net = eng.upload(inst, max_levels=2)
+        sts = []
+        for i in range(args.warmup + args.steps):
+            net.dom_set(0, inst.init)
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            st = net.enforce_ac(0)
+            if i >= args.warmup:
+                sts.append(st)
+        ms = statistics.median(s.device_ms for s in sts)
+        st = sts[-1]
+        t0 = time.perf_counter()
+        ok, _, dels = O.gac(O.Instance(n=inst.n, W=inst.W, dom=inst.dom, init=inst.init,
+                                       bx=inst.bin_scope[0::2].copy(), by=inst.bin_scope[1::2].copy(),
+                                       brows=inst.bin_rows, tarity=inst.tab_arity, tscope=inst.tab_scope,
+                                       tntup=inst.tab_ntup, ttup=inst.tab_tuples))
+        cpu_s = time.perf_counter() - t0
+        assert ok == (not st.inconsistent)
+        if ok:
+            assert dels == st.deletions
+        ach = st.alg_bytes / (ms / 1e3) / 1e9
+        out.append({"tuples_per_table": ntup, "inconsistent": bool(st.inconsistent), "ms": ms,
+                    "revisions": int(st.revisions), "revisions_per_s": st.revisions / (ms / 1e3),
+                    "deletions": int(st.deletions), "rounds": int(st.rounds),
+                    "alg_gb_per_s": ach, "frac_of_hbm_peak": ach / peak,
+                    "cpu_oracle_ms": cpu_s * 1e3, "cpu_oracle_cores": 1})
+        net.close()
+    eng.close()
+    line = {"metric": "GAC revisions/s (single large mixed network, bit-exact)", "value": out[0]["revisions_per_s"],
+            "unit": "revisions/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": out[0]["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u64", "data": "synthetic (seeded generator)",
+            "config": {"workload": "GAC fixpoint: n=2000 d=64, 30000 binary (p~U[0.2,0.5]) + 5000 ternary positive "
+                                   "tables, 20% of values removed, seed 1; L2 flushed before each step",
+                       "peak_source": peak_kind},
+            "shapes": out}
+    print(json.dumps(line))
+    return 0
+
+
+def run_mac(args):
+    """Config-1 measurement: MAC (dom/min, min value) to the first solution on
+    the plain CPU-runnable shape, seeds 1..10: the device search (one CTA per
+    search), the host-driven search (one launch per node), a batch of all
+    searches in one launch, and the oracle's CPU MAC."""
+    import cpim_gb300 as cp
+    from oracle import pyoracle as O
+
+    insts = [cp.gen_binary(50, 16, 250, 0.30, 0.30, 0.0, s) for s in range(1, 11)]
+    res = {}
+    nodes = None
+    for mode, name in ((0, "device_search"), (1, "host_driven")):
+        with cp.Engine(0) as eng:
+            eng.set_search_mode(mode)
+            nets = [eng.upload(i) for i in insts]
+            for n in nets[:2]:
+                n.mac_solve()
+            t0 = time.perf_counter()
+            rs = [n.mac_solve() for n in nets]
+            wall = time.perf_counter() - t0
+            nn = sum(r["num_positive"] + r["num_negative"] for r in rs)
+            nodes = nn if nodes is None else nodes
+            assert nn == nodes
+            res[name] = {"ms_per_solve": wall * 1e3 / len(nets), "nodes_per_s": nn / wall}
+            for n in nets:
+                n.close()
+    with cp.Engine(0) as eng:
+        nets = [eng.upload(i) for i in insts]
+        reps = 64
+        jobs = [(n, []) for n in nets] * reps
+        mb = cp.MacBatch(eng, jobs[:10])
+        mb.wait()
+        mb.close()
+        t0 = time.perf_counter()
+        mb = cp.MacBatch(eng, jobs)
+        rs = mb.wait()
+        wall = time.perf_counter() - t0
+        mb.close()
+        nn = sum(r["num_positive"] + r["num_negative"] for r in rs)
+        res["device_batch"] = {"searches": len(jobs), "ms_total": wall * 1e3, "solves_per_s": len(jobs) / wall,
+                               "nodes_per_s": nn / wall}
+        for n in nets:
+            n.close()
+    t0 = time.perf_counter()
+    for i in insts:
+        O.mac(O.Instance(n=i.n, W=i.W, dom=i.dom, init=i.init, bx=i.bin_scope[0::2].copy(),
+                         by=i.bin_scope[1::2].copy(), brows=i.bin_rows, tarity=i.tab_arity, tscope=i.tab_scope,
+                         tntup=i.tab_ntup, ttup=i.tab_tuples))
+    cpu = time.perf_counter() - t0
+    res["cpu_oracle_1core"] = {"ms_per_solve": cpu * 1e3 / len(insts), "nodes_per_s": nodes / cpu}
+    line = {"metric": "MAC first-solution solves/s (cfg1, node counts bit-exact)",
+            "value": res["device_batch"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (seeded generator)",
+            "config": {"workload": "MAC(AC_3bit, dom/min, min): n=50 d=16 e=250 p=0.30, seeds 1..10",
+                       "nodes_total_10_seeds": nodes},
+            "modes": res}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -509,9 +627,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="timed steps only (for profiling)")
-    ap.add_argument("--workload", default="sac", choices=["sac", "uneven", "serving"],
+    ap.add_argument("--workload", default="sac", choices=["sac", "uneven", "serving", "gac", "mac"],
                     help="sac: the batched SAC sweep (headline); uneven: the uneven multi-instance batch; "
-                         "serving: the request server under Poisson load")
+                         "serving: the request server under Poisson load; gac: the large GAC fixpoint; "
+                         "mac: MAC searches on the plain shape")
     ap.add_argument("--instances", type=int, default=4096, help="uneven workload: instances")
     ap.add_argument("--per-instance-sample", type=int, default=256, help="uneven workload: one-by-one sample")
     ap.add_argument("--networks", type=int, default=64, help="serving: resident networks")
@@ -529,6 +648,10 @@ def main():
         return run_uneven(args)
     if args.workload == "serving":
         return run_serving(args)
+    if args.workload == "gac":
+        return run_gac(args)
+    if args.workload == "mac":
+        return run_mac(args)
     return run_ours(args)
 
 
