@@ -667,6 +667,7 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   CP_TRY(net->alloc(&S.ndeep, 4));
   S.weak = nullptr;
   if (n_tab == 0 && n_bin > 0) CP_TRY(net->alloc(&S.weak, static_cast<size_t>(2) * n_bin * (kWeakK + 1)));
+  CP_TRY(net->alloc(&S.snap, static_cast<size_t>(n) * Wi));
   CP_TRY(net->alloc(&net->d_stats, 1));
   CP_TRY(net->alloc(&net->d_evt, n));
   CP_TRY(net->alloc(&net->d_sizes, n));
@@ -919,12 +920,19 @@ int cp_enforce_sac1(cp_net* net, int level, cp_stats* st) {
     }
     CP_CUDA(launch_build_work(net->dn, net->level_ptr(level), S, s));
     CP_CUDA(cudaEventRecord(e->evk0, s));
+    // Mode 0: failed branches remove their value from the level at once
+    // (later branches of the sweep start without it; the closure is the
+    // same, since a wipe-out on a larger domain implies one on a smaller);
+    // mode 1 keeps the plain Jacobi sweep as the reference path.
+    u64* gs_root = e->sac_mode == 0 ? net->level_ptr(level) : nullptr;
     if (tiled) {
       // Two-round branches resolved by the tiled kernel, the rest (the deep
-      // list) by the general kernel; the weak-support lists are rebuilt for
-      // this sweep's domains first.
+      // list) by the general kernel; the sweep-start domains and the
+      // weak-support lists counted against them come first.
+      CP_CUDA(cudaMemcpyAsync(S.snap, net->level_ptr(level), static_cast<size_t>(net->n) * net->W * 8,
+                              cudaMemcpyDeviceToDevice, s));
       if (S.weak) {
-        CP_CUDA(launch_weak(net->dn, net->level_ptr(level), S.weak, s));
+        CP_CUDA(launch_weak(net->dn, S.snap, S.weak, s));
         launches += 1;
         e->launches += 1;
       }
@@ -932,12 +940,13 @@ int cp_enforce_sac1(cp_net* net, int level, cp_stats* st) {
                               net->tile_grid, s));
       CP_CUDA(launch_sac_branches(net->dn, net->level_ptr(level), S.work, S.nwork, S.cursor, S.ok, net->d_stats,
                                   e->block_sac, net->sac_grid, net->d_sac_scratch, net->sac_stride, s, S.deep,
-                                  S.ndeep));
+                                  S.ndeep, gs_root));
       launches += 1;
       e->launches += 1;
     } else {
       CP_CUDA(launch_sac_branches(net->dn, net->level_ptr(level), S.work, S.nwork, S.cursor, S.ok, net->d_stats,
-                                  e->block_sac, net->sac_grid, net->d_sac_scratch, net->sac_stride, s));
+                                  e->block_sac, net->sac_grid, net->d_sac_scratch, net->sac_stride, s, nullptr,
+                                  nullptr, gs_root));
     }
     CP_CUDA(cudaEventRecord(e->evk1, s));
     CP_CUDA(launch_commit(net->dn, net->level_ptr(level), S, net->d_stats, s));
@@ -1981,7 +1990,11 @@ int batch_group_setup(cp_batch* b, BatchGroup& g) {
   B.out_off = d_offs;
   B.weak_off = d_woff;
   B.weak = nullptr;
-  if (!g.tables && weak_words > 0) CP_TRY(b->alloc(&B.weak, static_cast<size_t>(weak_words)));
+  B.snap = nullptr;
+  if (!g.tables && weak_words > 0) {
+    CP_TRY(b->alloc(&B.weak, static_cast<size_t>(weak_words)));
+    CP_TRY(b->alloc(&B.snap, static_cast<size_t>(tv) * g.W));
+  }
   B.wuser = d_wu;
   B.var_base = d_vb;
   B.var_inst = d_vi;
@@ -2077,6 +2090,11 @@ int batch_sweep_launches(cp_batch* b, BatchGroup& g, bool with_commit) {
   auto cover = [&](int64_t units, int persistent) {
     return q > 0 ? static_cast<int>(std::min<int64_t>((units + q - 1) / q, int64_t(1) << 30)) : persistent;
   };
+  if (B.snap) {
+    // Sweep-start domains (early removals then change only the roots).
+    CP_CUDA(launch_batch_snap(g.W, B, s));
+    e->launches += 1;
+  }
   if (g.tiled) {
     if (B.weak) {
       CP_CUDA(launch_batch_weak(g.W, B, s));
@@ -2320,6 +2338,9 @@ int cp_batch_tune(cp_batch* b) {
   for (auto& g : b->groups) {
     CP_TRY(batch_stats_begin(b));
     CP_TRY(batch_root(b, g));
+    // Trial sweeps only test: no early removals from the members' domains.
+    u64* snap = g.B.snap;
+    g.B.snap = nullptr;
     const bool can_tile = g.tile_grid > 0;
     struct Cand {
       bool tiled;
@@ -2347,6 +2368,7 @@ int cp_batch_tune(cp_batch* b) {
         pick = c;
       }
     }
+    g.B.snap = snap;
     g.tiled = pick.tiled;
     g.sac_block = pick.block;
     if (g.exec) {

@@ -104,6 +104,7 @@ struct SacScratch {
   int* deep;          // work indices the tiled kernel hands to the general one
   int* ndeep;         // [1]
   u32* weak;          // [2*nb][kWeakK + 1] weak-support lists (null: not built)
+  u64* snap;          // [n*W] the level's domains at the start of the sweep
 };
 
 enum NodeOp { kOpRoot = 0, kOpAssign = 1, kOpRefute = 2, kOpSingleton = 3, kOpEvents = 4 };
@@ -172,6 +173,7 @@ struct BatchDev {
   int* deep = nullptr;
   int* ndeep = nullptr;
   u32* weak = nullptr;             // weak-support lists of all members (null: none)
+  u64* snap = nullptr;             // [total_vars*W] members' domains at the sweep start (null: no early removal)
   const int64_t* weak_off = nullptr;  // [k] first list word of each member
 };
 
@@ -219,13 +221,15 @@ int ac_grid_max_blocks(const DevNet& N, int block, int sm_count);
 // With idx != nullptr the tests are work[idx[i]] for i < *nidx.
 cudaError_t launch_sac_branches(const DevNet& N, const u64* root, const int2* work, const int* nwork, int* cursor,
                                 uint8_t* ok, KStats* st, int block, int grid, void* gscratch, size_t gstride,
-                                cudaStream_t s, const int* idx = nullptr, const int* nidx = nullptr);
+                                cudaStream_t s, const int* idx = nullptr, const int* nidx = nullptr,
+                                u64* gs_root = nullptr);
 int sac_blocks_per_sm(const DevNet& N, int block, bool smem_state);
 // Tiled singleton tests (binary networks): 32 branches of one variable per
 // tile; branches that need more than two propagation rounds are appended to
 // S.deep for the general kernel. slot_cap: neighbours held in shared memory.
-cudaError_t launch_sac_tile(const DevNet& N, const u64* root, SacScratch S, uint8_t* ok, int slot_cap, KStats* st,
+cudaError_t launch_sac_tile(const DevNet& N, u64* root, SacScratch S, uint8_t* ok, int slot_cap, KStats* st,
                             int block, int grid, cudaStream_t s);
+cudaError_t launch_batch_snap(int W, const BatchDev& B, cudaStream_t s);
 // Weak-support lists of every arc for the domains at root (into S.weak).
 cudaError_t launch_weak(const DevNet& N, const u64* root, u32* weak, cudaStream_t s);
 size_t sac_tile_smem(const DevNet& N, int slot_cap);

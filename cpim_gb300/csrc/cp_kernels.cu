@@ -781,10 +781,12 @@ __global__ void __launch_bounds__(256) k_mac(const DevNet* nets, const MacJob* j
 // ---------------------------------------------------------------------------
 // k_sac: persistent CTAs over the SAC branch work list.
 // ---------------------------------------------------------------------------
+// gs_root (optional): a failed branch also removes its value from that
+// level at once, so branches that start later in the sweep see it.
 template <int WT, bool kTab>
 __global__ void __launch_bounds__(256) k_sac(DevNet N, const u64* root, const int2* work, const int* nwork,
                                              int* cursor, uint8_t* ok, KStats* st, char* gscratch, size_t gstride,
-                                             const int* idx) {
+                                             const int* idx, u64* gs_root) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_qlen[3], s_failed[2], s_failvar, s_err, s_b;
   char* base = gscratch ? gscratch + blockIdx.x * gstride : reinterpret_cast<char*>(smem_raw);
@@ -819,7 +821,11 @@ __global__ void __launch_bounds__(256) k_sac(DevNet N, const u64* root, const in
     __syncthreads();
     const int rounds = cta_fixpoint<WT, kTab>(N, F, cn, &s_err);
     rounds_max = max(rounds_max, rounds);
-    if (threadIdx.x == 0) ok[b] = (s_failed[0] | s_failed[1]) ? 0 : 1;
+    if (threadIdx.x == 0) {
+      const bool failed = (s_failed[0] | s_failed[1]) != 0;
+      ok[b] = failed ? 0 : 1;
+      if (failed && gs_root) atomicAnd(gs_root + static_cast<size_t>(xa.x) * WT + (xa.y >> 6), ~(1ull << (xa.y & 63)));
+    }
     ++done;
     __syncthreads();
   }
@@ -982,7 +988,8 @@ __device__ __forceinline__ int pop_low(u64& m, int word) {
 // s_fail / s_deep must be zero and visible to the whole CTA on entry. Ends
 // with the CTA synchronised.
 template <int WT>
-__device__ __forceinline__ void tile_one(const DevNet& N, const u64* root, const u32* weak, int x, int base, int b0,
+__device__ __forceinline__ void tile_one(const DevNet& N, u64* root, const u64* snap, const u32* weak, bool gs, int x,
+                                         int base, int b0,
                                          u32 live, uint8_t* ok, int* deep, int* ndeep, int slot_cap, u64* T,
                                          int* slot_of, u32& s_fail, u32& s_deep, int& s_next, u64& c_rev, u64& c_rows,
                                          u64& c_done) {
@@ -1052,7 +1059,7 @@ __device__ __forceinline__ void tile_one(const DevNet& N, const u64* root, const
 #pragma unroll
         for (int w = 0; w < WT; ++w) {
           dy[w] = T[(static_cast<size_t>(s) * 32 + lane) * WT + w];
-          removed += __popcll(__ldg(root + static_cast<size_t>(y) * WT + w)) - __popcll(dy[w]);
+          removed += __popcll(__ldg(snap + static_cast<size_t>(y) * WT + w)) - __popcll(dy[w]);
         }
         // Above thr every value of z keeps a support in any lane's D(y)
         // (pigeonhole over the removed values): only the listed weak values
@@ -1092,7 +1099,7 @@ __device__ __forceinline__ void tile_one(const DevNet& N, const u64* root, const
               for (int w = 0; w < WT; ++w) cur[w] = T[(static_cast<size_t>(sz) * 32 + lane) * WT + w];
             } else {
 #pragma unroll
-              for (int w = 0; w < WT; ++w) cur[w] = __ldg(root + static_cast<size_t>(z) * WT + w);
+              for (int w = 0; w < WT; ++w) cur[w] = root[static_cast<size_t>(z) * WT + w];
             }
             const bool mine = (open >> lane) & 1u;
             bool still = false, left = false;
@@ -1200,6 +1207,8 @@ __device__ __forceinline__ void tile_one(const DevNet& N, const u64* root, const
       const u32 failm = *reinterpret_cast<volatile u32*>(&s_fail);
       const u32 deepm = fits ? *reinterpret_cast<volatile u32*>(&s_deep) : live;
       const bool f = is_live && ((failm >> lane) & 1u);
+      if (gs && f)  // early removal at the level: later branches of the sweep start without it
+        atomicAnd(root + static_cast<size_t>(x) * WT + ((base + lane) >> 6), ~(1ull << ((base + lane) & 63)));
       const bool d = is_live && !f && ((deepm >> lane) & 1u);
       const int b = b0 + __popc(live & ((1u << lane) - 1u));
       const u32 dm = __ballot_sync(kFull, d);
@@ -1297,9 +1306,10 @@ __device__ __forceinline__ void flush_tile_counts(KStats* st, u64 c_rev, u64 c_r
 }
 
 template <int WT>
-__global__ void __launch_bounds__(256, WT <= 2 ? 5 : 1) k_sac_tile(DevNet N, const u64* root, const int4* tiles, const int* ntiles,
-                                                  int* tcursor, uint8_t* ok, int* deep, int* ndeep, int slot_cap,
-                                                  KStats* st, const u32* weak) {
+__global__ void __launch_bounds__(256, WT <= 2 ? 5 : 1) k_sac_tile(DevNet N, u64* root, const u64* snap,
+                                                                   const int4* tiles, const int* ntiles, int* tcursor,
+                                                                   uint8_t* ok, int* deep, int* ndeep, int slot_cap,
+                                                                   KStats* st, const u32* weak) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   u64* T = reinterpret_cast<u64*>(smem_raw);  // [slot_cap][32][WT]
   int* slot_of = reinterpret_cast<int*>(smem_raw + static_cast<size_t>(slot_cap) * 32 * WT * 8);  // [n]
@@ -1319,8 +1329,8 @@ __global__ void __launch_bounds__(256, WT <= 2 ? 5 : 1) k_sac_tile(DevNet N, con
     const int t = s_t;
     if (t >= total) break;
     const int4 tl = tiles[t];
-    tile_one<WT>(N, root, weak, tl.x, tl.y, tl.z, static_cast<u32>(tl.w), ok, deep, ndeep, slot_cap, T, slot_of, s_fail,
-                 s_deep, s_next, c_rev, c_rows, c_done);
+    tile_one<WT>(N, root, snap ? snap : root, weak, snap != nullptr, tl.x, tl.y, tl.z, static_cast<u32>(tl.w), ok,
+                 deep, ndeep, slot_cap, T, slot_of, s_fail, s_deep, s_next, c_rev, c_rows, c_done);
   }
   flush_tile_counts(st, c_rev, c_rows, c_done);
 }
@@ -1541,7 +1551,8 @@ __global__ void __launch_bounds__(256, WT <= 2 ? 4 : 1) k_batch_tile(BatchDev B,
     if (t >= total) break;
     const int4 tl = B.tiles[t];
     const int inst = tl.x >> 16;
-    tile_one<WT>(sN, B.roots[inst], B.weak ? B.weak + B.weak_off[inst] : nullptr, tl.x & 0xffff, tl.y, tl.z, static_cast<u32>(tl.w), B.ok, B.deep, B.ndeep,
+    tile_one<WT>(sN, B.roots[inst], B.snap ? B.snap + static_cast<size_t>(B.var_base[inst]) * WT : B.roots[inst],
+                 B.weak ? B.weak + B.weak_off[inst] : nullptr, B.snap != nullptr, tl.x & 0xffff, tl.y, tl.z, static_cast<u32>(tl.w), B.ok, B.deep, B.ndeep,
                  slot_cap, T, slot_of, s_fail, s_deep, s_next, c_rev, c_rows, c_done);
   }
   flush_tile_counts(st, c_rev, c_rows, c_done);
@@ -1594,7 +1605,12 @@ __global__ void __launch_bounds__(256) k_batch_sac(BatchDev B, int deep_only, KS
     __syncthreads();
     const int rounds = cta_fixpoint<WT, kTab>(N, F, cn, &s_err);
     rounds_max = max(rounds_max, rounds);
-    if (threadIdx.x == 0) B.ok[b] = (s_failed[0] | s_failed[1]) ? 0 : 1;
+    if (threadIdx.x == 0) {
+      const bool failed = (s_failed[0] | s_failed[1]) != 0;
+      B.ok[b] = failed ? 0 : 1;
+      if (failed && B.snap)  // early removal, as in k_sac
+        atomicAnd(B.roots[inst] + static_cast<size_t>(x) * WT + (a >> 6), ~(1ull << (a & 63)));
+    }
     ++done;
     __syncthreads();
   }
@@ -1628,6 +1644,17 @@ __global__ void k_batch_commit(BatchDev B, int W, KStats* st) {
   if (removed) {
     atomicAdd(&st->removed, removed);
     atomicAdd(&st->deletions, removed);
+  }
+}
+
+// Sweep-start copy of every active member's working domains into B.snap.
+__global__ void k_batch_snap(BatchDev B, int W) {
+  for (int i = blockIdx.x; i < B.k; i += gridDim.x) {
+    if (!B.act[i] || B.inc[i]) continue;
+    const size_t words = static_cast<size_t>(B.nets[i].n) * W;
+    const u64* src = B.roots[i];
+    u64* dst = B.snap + static_cast<size_t>(B.var_base[i]) * W;
+    for (size_t j = threadIdx.x; j < words; j += blockDim.x) dst[j] = src[j];
   }
 }
 
@@ -1809,7 +1836,7 @@ int sac_blocks_per_sm(const DevNet& N, int block, bool smem_state) {
 
 cudaError_t launch_sac_branches(const DevNet& N, const u64* root, const int2* work, const int* nwork, int* cursor,
                                 uint8_t* ok, KStats* st, int block, int grid, void* gscratch, size_t gstride,
-                                cudaStream_t s, const int* idx, const int* nidx) {
+                                cudaStream_t s, const int* idx, const int* nidx, u64* gs_root) {
   const size_t smem = gscratch ? 0 : cta_state_bytes(N);
   const int* count = idx ? nidx : nwork;
   return dispatch_wt(N, [&](auto wt, auto tab) -> cudaError_t {
@@ -1818,7 +1845,7 @@ cudaError_t launch_sac_branches(const DevNet& N, const u64* root, const int2* wo
     cudaError_t e = allow_smem(k_sac<WT, TB>, smem);
     if (e != cudaSuccess) return e;
     k_sac<WT, TB><<<grid, block, smem, s>>>(N, root, work, count, cursor, ok, st, static_cast<char*>(gscratch),
-                                            gstride, idx);
+                                            gstride, idx, gs_root);
     return cudaGetLastError();
   });
 }
@@ -1839,15 +1866,15 @@ int sac_tile_blocks_per_sm(const DevNet& N, int slot_cap, int block) {
   return e == cudaSuccess ? per_sm : 0;
 }
 
-cudaError_t launch_sac_tile(const DevNet& N, const u64* root, SacScratch S, uint8_t* ok, int slot_cap, KStats* st,
+cudaError_t launch_sac_tile(const DevNet& N, u64* root, SacScratch S, uint8_t* ok, int slot_cap, KStats* st,
                             int block, int grid, cudaStream_t s) {
   const size_t smem = sac_tile_smem(N, slot_cap);
   return dispatch_w(N.W, [&](auto wt) -> cudaError_t {
     constexpr int WT = decltype(wt)::value;
     cudaError_t e = allow_smem(k_sac_tile<WT>, smem);
     if (e != cudaSuccess) return e;
-    k_sac_tile<WT><<<grid, block, smem, s>>>(N, root, S.tiles, S.ntiles, S.tcursor, ok, S.deep, S.ndeep, slot_cap,
-                                             st, S.weak);
+    k_sac_tile<WT><<<grid, block, smem, s>>>(N, root, S.snap, S.tiles, S.ntiles, S.tcursor, ok, S.deep, S.ndeep,
+                                             slot_cap, st, S.weak);
     return cudaGetLastError();
   });
 }
@@ -1944,6 +1971,11 @@ cudaError_t launch_batch_build(int W, const BatchDev& B, bool with_tiles, cudaSt
     k_batch_build<WT><<<blocks, 256, 0, s>>>(B, with_tiles ? 1 : 0);
     return cudaGetLastError();
   });
+}
+
+cudaError_t launch_batch_snap(int W, const BatchDev& B, cudaStream_t s) {
+  k_batch_snap<<<std::max(1, std::min(B.k, 4096)), 256, 0, s>>>(B, W);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_batch_weak(int W, const BatchDev& B, cudaStream_t s) {
