@@ -236,7 +236,9 @@ def test_batch_cta_quota_and_priority_keep_results(quota):
         for k in range(len(nets)):
             if not ip[k]:
                 assert np.array_equal(dq[k], dp[k]), k
-        assert sq.branches == sp.branches
+        # (Branch counts may differ: failed branches remove their value at
+        # once, so how many branches a sweep still tests depends on timing.)
+        assert sq.deletions == sp.deletions
         bq.close()
         bp.close()
         for n in nets:
