@@ -236,9 +236,10 @@ def test_batch_cta_quota_and_priority_keep_results(quota):
         for k in range(len(nets)):
             if not ip[k]:
                 assert np.array_equal(dq[k], dp[k]), k
-        # (Branch counts may differ: failed branches remove their value at
-        # once, so how many branches a sweep still tests depends on timing.)
-        assert sq.deletions == sp.deletions
+        # Branch and deletion totals are not compared: failed branches remove
+        # their value at once, so how many branches a sweep still tests, and
+        # how many values an inconsistent member loses before its wipe-out is
+        # seen, depend on timing. The closures above are what must agree.
         bq.close()
         bp.close()
         for n in nets:
