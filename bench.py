@@ -230,13 +230,10 @@ def run_ours(args):
     gpu_launches = eng.launches - launches0
     dev_ms = [s.device_ms for s in sts]
     branches = sum(s.branches for s in sts)
-    total_ms = sum(dev_ms)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = branches * world / (total_ms / 1e3)
+    # Replicas: branches summed over ranks, the slowest rank's device time.
+    from cpim_gb300.replicas import job_rate
+    _, job_s, value = job_rate(branches, sum(dev_ms) / 1e3, device="cuda")
+    total_ms = job_s * 1e3
     # Parity of the timed result (deterministic closure): consistent, no test fails.
     final = net.dom_get(0)
     assert not sts[-1].inconsistent
@@ -275,7 +272,7 @@ def run_ours(args):
         e2e_br += st.branches
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
-    e2e_value = e2e_br * world / e2e_s
+    _, _, e2e_value = job_rate(e2e_br, e2e_s, device="cuda")
     assert np.array_equal(r, final)
 
     # Plain single-instance path: one launch per singleton test (sample).
