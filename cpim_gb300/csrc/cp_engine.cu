@@ -1442,7 +1442,13 @@ int mac_start(cp_engine* e, std::vector<MacSpec>& specs, int varh, int64_t time_
   }
   // CTA state: shared memory when the largest fits, else per-CTA scratch.
   const bool smem_mode = max_state + 2048 <= e->smem_optin;
-  const int block = std::min(e->block_node, 256);
+  // CTA size (measured on one GB300): many searches of small networks run
+  // best as many small CTAs (64 threads: 163 k cfg1 searches/s vs 120 k at
+  // 512); a few searches, or large networks, as wide CTAs (512 threads:
+  // 1.65x the node rate of 256 on networks of a few thousand arcs).
+  int max_inc = 0;
+  for (const MacSpec& sp : specs) max_inc = std::max(max_inc, 2 * sp.net->nb + sp.net->nt);
+  const int block = (max_inc <= 2048 && k >= 2 * e->sm_count) ? 64 : 512;
   const int per_sm = mac_blocks_per_sm(block, smem_mode ? max_state : 0);
   if (per_sm < 1) return fail(CP_E_UNSUPPORTED, "MAC kernel does not fit on an SM");
   const int grid = std::min(k, per_sm * e->sm_count);

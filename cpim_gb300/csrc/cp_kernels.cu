@@ -743,7 +743,7 @@ __device__ void mac_one(const DevNet& N, const MacJob& J, MacOut* out, char* bas
 
 // Jobs of any domain width and network kind in one launch: each job runs the
 // body instantiated for its width and table flag.
-__global__ void __launch_bounds__(256) k_mac(const DevNet* nets, const MacJob* jobs, int njobs, int* cursor,
+__global__ void __launch_bounds__(512) k_mac(const DevNet* nets, const MacJob* jobs, int njobs, int* cursor,
                                               MacOut* outs, char* gscratch, size_t gstride, long long slice_ns) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ MacShared sh;
