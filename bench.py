@@ -386,6 +386,33 @@ def run_uneven(args):
         sub_ms.append(s_st.device_ms)
     sub.close()
     sub_rate = M / (min(sub_ms) / 1e3)
+
+    # The same comparison on the smallest members (n*d <= 2048), where one
+    # instance alone leaves most of the GPU idle.
+    shapes = [cp._uneven_shape(7 * 1000003 + i, 20, 400, 256) for i in range(K)]
+    small = [i for i in range(K) if shapes[i][0] * shapes[i][1] <= 2048][:M]
+
+    def one_by_one(idx):
+        t = 0.0
+        for i in idx:
+            nets[i].level_copy(1, 0)
+            t += nets[i].enforce_sac1(0).device_ms
+        return len(idx) / (t / 1e3)
+
+    def batched(idx):
+        b2 = cp.Batch(eng, [nets[i] for i in idx], level=0)
+        best = 1e30
+        for _ in range(2):
+            b2.copy_level(1)
+            best = min(best, b2.sac1()[0].device_ms)
+        b2.close()
+        return len(idx) / (best / 1e3)
+
+    small_cmp = None
+    if small:
+        a, b_ = one_by_one(small), batched(small)
+        small_cmp = {"instances": len(small), "value_device": a, "batched_same_instances": b_,
+                     "batched_over_per_instance": b_ / a, "unit": "instances/s"}
     line = {"metric": "instance AC+SAC fixpoints/s (uneven batch, bit-exact)", "value": inst_rate,
             "unit": "instances/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": statistics.median(ms), "higher_is_better": True, "scaling": "weak",
@@ -398,6 +425,7 @@ def run_uneven(args):
             "per_instance_launches": {"instances": M, "value_device": per_inst, "value_wall": per_inst_wall,
                                       "unit": "instances/s", "batched_same_instances": sub_rate,
                                       "batched_over_per_instance": sub_rate / per_inst},
+            "small_members_n_times_d_le_2048": small_cmp,
             "gpu_launches": int(gpu_launches), "clocks": clk.summary()}
     print(json.dumps(line))
     batch.close()
