@@ -1638,6 +1638,18 @@ int cp_mac_batch_destroy(cp_mac_batch* b) {
 
 int cp_gsolver_solve(cp_net* net, int64_t time_limit_ms, cp_search_result* res, int* solution) {
   if (!net || !res || !solution) return fail(CP_E_ARG, "null argument");
+  if (net->e->search_mode == 0 && !net->prefer_grid) {
+    // The whole d-way search in one CTA, on the network's own level stack.
+    std::vector<MacSpec> spec(1);
+    spec[0].net = net;
+    spec[0].init = net->level_ptr(0);
+    spec[0].stack = net->d_levels;
+    spec[0].levels = net->levels;
+    cp_mac_batch b;
+    CP_TRY(mac_start(net->e, spec, 2, time_limit_ms, &b));
+    CP_TRY(cp_mac_batch_wait(&b, res));
+    return cp_mac_batch_solution(&b, 0, solution);
+  }
   DeviceGSolver g(net);
   return g.solve(time_limit_ms, res, solution);
 }

@@ -124,7 +124,7 @@ struct MacJob {
   MacState* state;       // device memory, zeroed before the first launch
   int net;               // index into the launch's network array
   int levels;            // depth of the level stack
-  int varh;              // 1: dom/min, 0: lex
+  int varh;              // MAC order 1: dom/min, 0: lex; 2: the d-way search of GModelSolver
   int n_choice;
   const u64* init;       // n*W words: domains before the choices
   u64* stack_dom;        // levels * n * W words

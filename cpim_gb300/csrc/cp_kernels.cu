@@ -568,16 +568,19 @@ __device__ __forceinline__ int dom_head(const u64* D, int x) {
 }
 
 // VRH_DOM_MIN: the first unassigned variable of strictly smaller domain size
-// (smallest size, ties to the smallest index). Block-wide.
+// (smallest size, ties to the smallest index). Block-wide. With A_p null the
+// candidates are the variables with more than one value instead
+// (GModel::GetMinDomainVar, src/GModel.cu:1553-1572).
 template <int WT>
 __device__ int mac_select(const u64* D, const uint8_t* A_p, int n, MacShared& sh) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   unsigned long long best = ~0ull;
   for (int v = threadIdx.x; v < n; v += blockDim.x) {
-    if (A_p[v]) continue;
+    if (A_p && A_p[v]) continue;
     int sz = 0;
 #pragma unroll
     for (int w = 0; w < WT; ++w) sz += __popcll(D[static_cast<size_t>(v) * WT + w]);
+    if (!A_p && sz <= 1) continue;
     const unsigned long long key = (static_cast<unsigned long long>(sz) << 32) | static_cast<unsigned>(v);
     best = key < best ? key : best;
   }
@@ -741,6 +744,169 @@ __device__ void mac_one(const DevNet& N, const MacJob& J, MacOut* out, char* bas
   }
 }
 
+// First value of D(x) above a (VLH_MIN order; a = -1: the first value).
+template <int WT>
+__device__ __forceinline__ int dom_next(const u64* D, int x, int a) {
+  const int from = a + 1;
+#pragma unroll
+  for (int w = 0; w < WT; ++w) {
+    if ((w + 1) * 64 <= from) continue;
+    u64 v = D[static_cast<size_t>(x) * WT + w];
+    if (from > w * 64) v &= ~0ull << (from - w * 64);
+    if (v) return w * 64 + __ffsll(static_cast<long long>(v)) - 1;
+  }
+  return -1;
+}
+
+// The d-way search of GModelSolver::Solve / Search (src/GModelSolver.cu:31-189)
+// run by one CTA: at each level the smallest domain of more than one value,
+// its values in increasing order, one fixpoint per child; a child that fails
+// counts as a negative node. Level p's domains live in the global stack; the
+// state a time slice leaves (depth, "entering level p") is resumed by the next
+// launch, as for mac_one.
+template <int WT, bool kTab>
+__device__ void dway_one(const DevNet& N, const MacJob& J, MacOut* out, char* base, MacShared& sh,
+                         long long slice_ns) {
+  MacState& S = *J.state;
+  if (S.phase == 2) return;
+  Fix F = make_cta_fix(N, base, sh.qlen, sh.failed, &sh.failvar);
+  const CtaLayout L = cta_layout(N);
+  const int n = N.n;
+  const size_t words = static_cast<size_t>(n) * WT;
+  const long long t_enter = globaltimer_ns();
+  if (threadIdx.x == 0) sh.err = 0;
+  Cnt cn;
+  long long npos = 0, nneg = 0, props = 0, t0 = t_enter;
+  int status = -1, p = 0;
+  bool fresh = true, dirty = false;
+  if (S.phase == 0) {
+    block_copy(F.D, J.init, words);
+    __syncthreads();
+    if (threadIdx.x == 0)
+      for (int c = 0; c < J.n_choice; ++c) {
+        const int2 ch = J.choices[c];
+        u64* dv = F.D + static_cast<size_t>(ch.x) * WT;
+        for (int w = 0; w < WT; ++w) dv[w] &= (w == (ch.y >> 6)) ? (1ull << (ch.y & 63)) : 0ull;
+      }
+    __syncthreads();
+    props = 1;
+    const bool ok = mac_fix<WT, kTab>(N, F, base, L, sh, kOpRoot, 0, 0, cn);
+    block_copy(J.stack_dom, F.D, words);
+    if (!ok) status = 0;
+  } else {
+    p = S.p;
+    fresh = S.top != 0;
+    npos = S.npos;
+    nneg = S.nneg;
+    props = S.props;
+    t0 = S.t_start;
+    dirty = true;
+  }
+  bool suspended = false;
+  while (status < 0) {
+    if (threadIdx.x == 0) {
+      const long long now = globaltimer_ns();
+      sh.stop = (fresh && J.limit_ns > 0 && now - t0 >= J.limit_ns) ? 1
+                                                                     : (slice_ns > 0 && now - t_enter > slice_ns ? 2 : 0);
+    }
+    __syncthreads();
+    const int stop = sh.stop, err = sh.err;
+    __syncthreads();
+    if (err) {
+      status = err;
+      break;
+    }
+    if (stop == 1) {
+      status = 2;
+      break;
+    }
+    if (stop == 2) {
+      suspended = true;
+      break;
+    }
+    if (dirty) {  // the CTA domains must hold level p
+      block_copy(F.D, J.stack_dom + static_cast<size_t>(p) * words, words);
+      __syncthreads();
+      dirty = false;
+    }
+    if (fresh) {
+      if (p + 1 >= J.levels) {
+        status = -1;  // level stack too shallow
+        break;
+      }
+      const int var = mac_select<WT>(F.D, nullptr, n, sh);
+      if (var < 0) {  // every domain a singleton: a solution
+        for (int x = threadIdx.x; x < n; x += blockDim.x) J.solution[x] = dom_head<WT>(F.D, x);
+        status = 1;
+        break;
+      }
+      if (threadIdx.x == 0) J.path[p] = make_int2(var, -1);
+      fresh = false;
+      __syncthreads();
+    }
+    const int2 pv = J.path[p];
+    if (threadIdx.x == 0) sh.val = dom_next<WT>(F.D, pv.x, pv.y);
+    __syncthreads();
+    const int val = sh.val;
+    __syncthreads();
+    if (val < 0) {  // values of this level exhausted
+      if (p == 0) {
+        status = 0;
+        break;
+      }
+      --p;
+      dirty = true;
+      continue;
+    }
+    if (threadIdx.x == 0) J.path[p].y = val;
+    ++npos;
+    const bool ok = mac_fix<WT, kTab>(N, F, base, L, sh, kOpAssign, pv.x, val, cn);
+    ++props;
+    if (!ok) {
+      ++nneg;
+      dirty = true;
+      continue;
+    }
+    block_copy(J.stack_dom + static_cast<size_t>(p + 1) * words, F.D, words);
+    ++p;
+    fresh = true;
+  }
+  __syncthreads();
+  if (suspended) {
+    if (threadIdx.x == 0) {
+      S.phase = 1;
+      S.p = p;
+      S.top = fresh ? 1 : 0;
+      S.npos = npos;
+      S.nneg = nneg;
+      S.props = props;
+      S.t_start = t0;
+    }
+    return;
+  }
+  __threadfence_system();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    S.phase = 2;
+    out->status = status;
+    out->npos = npos;
+    out->nneg = nneg;
+    out->props = props;
+    __threadfence_system();
+    *reinterpret_cast<volatile int*>(&out->done) = 1;
+  }
+}
+
+// A job runs the MAC search (varh 0 / 1) or the d-way search (varh 2).
+template <int WT, bool kTab>
+__device__ __forceinline__ void search_one(const DevNet& N, const MacJob& J, MacOut* out, char* base, MacShared& sh,
+                                           long long slice_ns) {
+  if (J.varh == 2)
+    dway_one<WT, kTab>(N, J, out, base, sh, slice_ns);
+  else
+    mac_one<WT, kTab>(N, J, out, base, sh, slice_ns);
+}
+
 // Jobs of any domain width and network kind in one launch: each job runs the
 // body instantiated for its width and table flag.
 __global__ void __launch_bounds__(512) k_mac(const DevNet* nets, const MacJob* jobs, int njobs, int* cursor,
@@ -762,16 +928,16 @@ __global__ void __launch_bounds__(512) k_mac(const DevNet* nets, const MacJob* j
     const bool tab = sN.nt > 0;
     switch (sN.W) {
       case 1:
-        tab ? mac_one<1, true>(sN, J, o, base, sh, slice_ns) : mac_one<1, false>(sN, J, o, base, sh, slice_ns);
+        tab ? search_one<1, true>(sN, J, o, base, sh, slice_ns) : search_one<1, false>(sN, J, o, base, sh, slice_ns);
         break;
       case 2:
-        tab ? mac_one<2, true>(sN, J, o, base, sh, slice_ns) : mac_one<2, false>(sN, J, o, base, sh, slice_ns);
+        tab ? search_one<2, true>(sN, J, o, base, sh, slice_ns) : search_one<2, false>(sN, J, o, base, sh, slice_ns);
         break;
       case 4:
-        tab ? mac_one<4, true>(sN, J, o, base, sh, slice_ns) : mac_one<4, false>(sN, J, o, base, sh, slice_ns);
+        tab ? search_one<4, true>(sN, J, o, base, sh, slice_ns) : search_one<4, false>(sN, J, o, base, sh, slice_ns);
         break;
       default:
-        mac_one<8, false>(sN, J, o, base, sh, slice_ns);
+        search_one<8, false>(sN, J, o, base, sh, slice_ns);
         break;
     }
     __syncthreads();

@@ -110,3 +110,28 @@ def test_mac_lex_order_device_equals_host(p):
         assert d.get("error") == h["error"]
     else:
         _same(d, h, "lex")
+
+
+def _gsolve(inst, mode):
+    with cp.Engine(0) as eng:
+        eng.set_search_mode(mode)
+        net = eng.upload(inst)
+        r = net.gsolver_solve(time_limit_ms=120000)
+        net.close()
+    return r
+
+
+@pytest.mark.parametrize("args", [("binary", 50, 16, 250, 0.3, 0.3, 0.0, 1), ("binary", 50, 16, 250, 0.3, 0.3, 0.0, 2),
+                                  ("binary", 24, 8, 110, 0.42, 0.42, 0.0, 5), ("binary", 30, 100, 60, 0.5, 0.5, 0.1, 3),
+                                  ("binary", 14, 200, 30, 0.6, 0.6, 0.0, 4),
+                                  ("mixed", 30, 8, 60, 0.3, 0.5, 40, 60, 0.2, 2)])
+def test_gsolver_device_equals_host_driven(args):
+    """The d-way search of GModelSolver run whole on the device gives the
+    host-driven search's node counts, verdict and solution."""
+    inst = cp.gen_binary(*args[1:]) if args[0] == "binary" else cp.gen_mixed(*args[1:])
+    d, h = _gsolve(inst, 0), _gsolve(inst, 1)
+    _same(d, h, args)
+    if d["status"] == 1:
+        from tests.golden_cases import oracle_view_of
+        from oracle import pyoracle as O
+        assert O.check_solution(oracle_view_of(inst), d["solution"])
