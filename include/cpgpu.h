@@ -270,10 +270,10 @@ typedef struct cp_search_result {
 } cp_search_result;
 int cp_mac_solve(cp_net* net, int var_heuristic, int val_heuristic, int64_t time_limit_ms,
                  cp_search_result* res, int* solution);
-/* Search placement: 0 (default) runs the whole MAC search of cp_mac_solve on
- * the device, in one CTA, where the network's propagation state fits one CTA
- * (node counts and solutions are those of the host-driven search); 1 drives
- * every node from the host. */
+/* Search placement: 0 (default) runs the whole search of cp_mac_solve and of
+ * cp_gsolver_solve on the device, in one CTA, for networks whose fixpoints run
+ * in one CTA (node counts and solutions are those of the host-driven search);
+ * 1 drives every node from the host. */
 int cp_engine_set_search_mode(cp_engine* e, int mode);
 /* Many MAC searches in one launch (one CTA per search, CTAs take searches
  * from a queue). Search i runs on nets[i] from its level 0 with the next
