@@ -56,7 +56,7 @@ typedef struct cp_stats {
   int64_t revisions;     /* arc / table revisions performed */
   int64_t rows;          /* support rows and tuples read by revisions */
   int64_t fixpoints;     /* AC closures computed (1, or the SAC branches + root ACs) */
-  int64_t branches;      /* SAC singleton tests run */
+  int64_t branches;      /* SAC singleton tests run (scheduling-dependent with early removals) */
   int32_t sweeps;        /* SAC sweeps */
   int32_t launches;      /* kernel launches issued by this call */
   double device_ms;      /* device time of the call (CUDA events) */
@@ -130,7 +130,10 @@ int cp_enforce_ac(cp_net* net, int level, int n_evt, const int* evt, cp_stats* s
 /* SAC closure at `level` (SAC1::enforce, src/SAC1.cpp:57-103): every live
  * (x, a) is tested by a singleton AC fixpoint, all tests of a sweep batched
  * in one persistent launch, failed values removed and AC re-run, until no
- * test fails. */
+ * test fails. In SAC mode 0 a failed test also removes its value from the
+ * level at once, so later tests of the same sweep start without it; the
+ * closure is the same (unique), while the number of tests run depends on
+ * scheduling. */
 int cp_enforce_sac1(cp_net* net, int level, cp_stats* st);
 /* Singleton tests of `count` pairs (vars[i], vals[i]) against the domains of
  * `level` without changing them: ok[i] = 1 if the AC fixpoint of the level
