@@ -131,6 +131,8 @@ def lib():
         "cp_engine_device": ([vp], i),
         "cp_engine_set_priority": ([vp, i], i),
         "cp_engine_set_search_mode": ([vp, i], i),
+        "cp_engine_set_wait_budget": ([vp, i64], i),
+        "cp_engine_inject_alloc_failure": ([vp, i64], i),
         "cp_mac_batch_start": ([vp, i, PV, PI, PI, PI, i, i, i64, PV], i),
         "cp_mac_batch_poll": ([vp, PU8, C.POINTER(SearchResult), PI], i),
         "cp_mac_batch_wait": ([vp, C.POINTER(SearchResult)], i),
@@ -262,6 +264,14 @@ class Engine:
     def set_priority(self, priority: int):
         """Stream priority: -1 low, 0 default, 1 high (before any upload)."""
         _check(lib().cp_engine_set_priority(self._h, int(priority)))
+
+    def set_wait_budget(self, ns: int):
+        """Longest grid-barrier wait of a CTA before the call returns a timeout."""
+        _check(lib().cp_engine_set_wait_budget(self._h, int(ns)))
+
+    def inject_alloc_failure(self, after: int):
+        """Test hook: the device allocation after `after` more fails (-1: off)."""
+        _check(lib().cp_engine_inject_alloc_failure(self._h, int(after)))
 
     def set_search_mode(self, mode: int):
         """0: MAC searches run whole on the device (one CTA); 1: host-driven."""

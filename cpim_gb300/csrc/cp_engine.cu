@@ -77,6 +77,8 @@ struct cp_engine {
   int sac_mode = 0;  // 0: tiled sweep where eligible, 1: general kernel only
   int cta_quota = 0;  // batch sweep CTAs retire after this many units (0: persistent)
   int search_mode = 0;  // 0: MAC searches run on the device where they fit one CTA; 1: host-driven nodes
+  long long wait_ns = 2000000000ll;  // longest grid-barrier wait of a block (then CP_E_TIMEOUT)
+  int64_t fail_alloc_after = -1;     // test hook: device allocations left before one fails (-1: off)
   std::multimap<size_t, void*> mapped_free;  // host-mapped pinned blocks (device-written results)
   int priority = 0;   // stream priority class: -1 low, 0 default, 1 high
   // Device memory of this engine's networks and batches comes from a
@@ -88,7 +90,12 @@ struct cp_engine {
   std::multimap<size_t, void*> pinned_free;
 
   int dev_alloc(void** p, size_t bytes) {
-    // 256 extra bytes let the caller align the block's start.
+    if (fail_alloc_after == 0) {
+      fail_alloc_after = -1;
+      return fail(CP_E_OOM, "device allocation of " + std::to_string(bytes) + " bytes: injected failure");
+    }
+    if (fail_alloc_after > 0) --fail_alloc_after;
+    // Callers ask for 256 extra bytes to align the block's start themselves.
     cudaError_t err = cudaMallocFromPoolAsync(p, bytes, pool, stream);
     if (err != cudaSuccess) {
       cudaGetLastError();
@@ -304,6 +311,7 @@ int run_ac(cp_net* net, int level, const int* evt_dev, int nevt, int& launches) 
     const size_t nw = (static_cast<size_t>(net->n) + 31) / 32;
     CP_CUDA(cudaMemsetAsync(net->G.fb[0], 0, nw * 4, s));
     CP_CUDA(cudaMemsetAsync(net->G.fb[1], 0, nw * 4, s));
+    net->G.wait_ns = e->wait_ns;
     CP_CUDA(launch_ac_grid(net->dn, net->level_ptr(level), evt_dev, nullptr, evt_dev ? nevt : 0, net->G,
                            net->d_stats, e->block_grid, net->grid_blocks, s));
   } else {
@@ -446,6 +454,20 @@ int cp_engine_set_priority(cp_engine* e, int priority) {
   CP_CUDA(cudaStreamDestroy(e->stream));
   e->stream = ns;
   e->priority = priority;
+  return CP_OK;
+}
+
+int cp_engine_set_wait_budget(cp_engine* e, int64_t ns) {
+  if (!e) return fail(CP_E_ARG, "null engine");
+  if (ns < 0) return fail(CP_E_ARG, "negative wait budget");
+  e->wait_ns = ns;
+  return CP_OK;
+}
+
+int cp_engine_inject_alloc_failure(cp_engine* e, int64_t after) {
+  if (!e) return fail(CP_E_ARG, "null engine");
+  if (after < -1) return fail(CP_E_ARG, "after must be -1 (off) or >= 0");
+  e->fail_alloc_after = after;
   return CP_OK;
 }
 

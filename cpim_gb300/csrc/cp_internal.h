@@ -87,6 +87,7 @@ struct GridScratch {
   int* epoch;         // [1] stamp base carried across calls
   int* failed;        // [1]
   unsigned* bar;      // [2] grid barrier: count, generation
+  long long wait_ns;  // longest wait of a block at the grid barrier
 };
 
 // SAC sweep buffers (one per network).

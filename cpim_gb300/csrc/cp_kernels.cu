@@ -32,7 +32,6 @@ namespace cpgpu {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr long long kBarrierTimeoutNs = 2000000000ll;  // 2 s
 
 __device__ __forceinline__ u64 vload(const u64* p) { return *reinterpret_cast<const volatile u64*>(p); }
 __device__ __forceinline__ int vloadi(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
@@ -1009,9 +1008,10 @@ __global__ void __launch_bounds__(256) k_sac(DevNet N, const u64* root, const in
 // ---------------------------------------------------------------------------
 // k_ac_grid: whole-grid fixpoint with a bounded grid barrier.
 // ---------------------------------------------------------------------------
-// Sense-free generation barrier; every block waits at most
-// kBarrierTimeoutNs, then reports CP_E_TIMEOUT through *err and returns false.
-__device__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* err) {
+// Sense-free generation barrier; every block waits at most wait_ns, then
+// reports CP_E_TIMEOUT through *err and returns false (a block that sees
+// another's error stops waiting too, so every block leaves).
+__device__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* err, long long wait_ns) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -1028,7 +1028,7 @@ __device__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* err) {
       const long long t0 = globaltimer_ns();
       unsigned sleep = 32;
       while (*vgen == gen) {
-        if (vloadi(err) != 0 || globaltimer_ns() - t0 > kBarrierTimeoutNs) {
+        if (vloadi(err) != 0 || globaltimer_ns() - t0 > wait_ns) {
           atomicExch(err, -4);
           ok = 0;
           break;
@@ -1067,7 +1067,7 @@ __global__ void __launch_bounds__(512) k_ac_grid(DevNet N, u64* D, const int* ev
   Cnt cn;
   const long long max_rounds = N.total_values + 2;
   int r = 0;
-  bool ok = grid_barrier(G.bar, nblocks, err);
+  bool ok = grid_barrier(G.bar, nblocks, err, G.wait_ns);
   const int gwarp = gtid >> 5, nwarps = gthreads >> 5;
   for (; ok; ++r) {
     const int cur = r & 1;
@@ -1086,7 +1086,7 @@ __global__ void __launch_bounds__(512) k_ac_grid(DevNet N, u64* D, const int* ev
     int* qlenn = F.qlen + (r + 1) % 3;
     for (int j = gwarp; j < len; j += nwarps)
       process_item<WT, kTab, true>(N, F, qc[j], fbc, qn, fbn, qlenn, cur ^ 1, F.stamp_base + r + 1, cn);
-    ok = grid_barrier(G.bar, nblocks, err);
+    ok = grid_barrier(G.bar, nblocks, err, G.wait_ns);
   }
   flush_counts(st, cn);
   if (gtid == 0) {

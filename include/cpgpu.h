@@ -91,6 +91,13 @@ int cp_engine_set_priority(cp_engine* e, int priority);
  * higher-priority work on other streams gets SMs during long sweeps. Results
  * are unchanged. Applies to batches created afterwards. */
 int cp_engine_set_cta_quota(cp_engine* e, int quota);
+/* Longest wait of a CTA at the grid-wide barrier of the persistent fixpoint
+ * kernel (default 2 s); past it the kernel stops and the call returns
+ * CP_E_TIMEOUT, leaving the context usable. Failure handling and its tests. */
+int cp_engine_set_wait_budget(cp_engine* e, int64_t ns);
+/* Test hook: after `after` more device allocations of this engine succeed,
+ * the next one fails as out of memory (CP_E_OOM); -1 turns it off. */
+int cp_engine_inject_alloc_failure(cp_engine* e, int64_t after);
 
 /* ---- networks ------------------------------------------------------------ */
 /* Uploads a network; replaces GModelAdapter::Build
