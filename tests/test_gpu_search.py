@@ -135,3 +135,30 @@ def test_gsolver_device_equals_host_driven(args):
         from tests.golden_cases import oracle_view_of
         from oracle import pyoracle as O
         assert O.check_solution(oracle_view_of(inst), d["solution"])
+
+
+@pytest.mark.parametrize("which", ["queens8", "mixed"])
+def test_xcsp_instances_on_the_device(which):
+    """Networks read from XCSP text: device GAC and MAC equal the oracle's."""
+    from cpim_gb300.xcsp import read_xcsp
+    from oracle import pyoracle as O
+    from tests.golden_cases import oracle_view_of
+    from tests.test_xcsp import MIXED, _queens_xml
+    m = read_xcsp(_queens_xml(8) if which == "queens8" else MIXED)
+    ov = oracle_view_of(m.inst)
+    ok, d, _ = O.gac(ov)
+    ref = O.mac(ov)
+    with cp.Engine(0) as eng:
+        net = eng.upload(m.inst)
+        st = net.enforce_ac(0)
+        assert bool(st.inconsistent) == (not ok)
+        if ok:
+            assert np.array_equal(net.dom_get(0), d)
+        net.close()
+        net = eng.upload(m.inst)
+        r = net.mac_solve()
+        net.close()
+    assert r["status"] == ref["status"]
+    assert (r["num_positive"], r["num_negative"]) == (ref["num_positive"], ref["num_negative"])
+    if r["status"] == 1:
+        assert r["solution"] == ref["solution"]
