@@ -267,6 +267,26 @@ int stats_begin(cp_net* net) {
   return CP_OK;
 }
 
+// Both stats slots: zeroed together, fetched together (one sync).
+int stats_begin2(cp_net* net) {
+  KStats z{};
+  z.fail_var = -1;
+  net->h_stats[0] = z;
+  net->h_stats[1] = z;
+  CP_CUDA(cudaMemcpyAsync(net->d_stats, net->h_stats, 2 * sizeof(KStats), cudaMemcpyHostToDevice, net->e->stream));
+  return CP_OK;
+}
+
+int stats_fetch2(cp_net* net) {
+  CP_CUDA(cudaMemcpyAsync(net->h_stats, net->d_stats, 2 * sizeof(KStats), cudaMemcpyDeviceToHost, net->e->stream));
+  CP_CUDA(cudaStreamSynchronize(net->e->stream));
+  for (int i = 0; i < 2; ++i) {
+    if (net->h_stats[i].grid_err) return fail(CP_E_TIMEOUT, "device grid barrier wait ran out");
+    if (net->h_stats[i].error) return fail(net->h_stats[i].error, "device-side check failed (round limit)");
+  }
+  return CP_OK;
+}
+
 int stats_fetch(cp_net* net) {
   CP_CUDA(cudaMemcpyAsync(net->h_stats, net->d_stats, sizeof(KStats), cudaMemcpyDeviceToHost, net->e->stream));
   CP_CUDA(cudaStreamSynchronize(net->e->stream));
@@ -301,8 +321,11 @@ double alg_bytes(const cp_net* net, const Acc& a, int64_t branches) {
 
 // ---- one AC fixpoint at a level ----------------------------------------
 // evt_dev: device list of seeds (nullptr = all variables); nevt: its length.
-int run_ac(cp_net* net, int level, const int* evt_dev, int nevt, int& launches) {
+// nevt_dev (optional, grid path only): the event count read on the device.
+int run_ac(cp_net* net, int level, const int* evt_dev, int nevt, int& launches, KStats* st = nullptr,
+           const int* nevt_dev = nullptr) {
   cp_engine* e = net->e;
+  if (!st) st = net->d_stats;
   if (net->prefer_grid) {
     cudaStream_t s = e->stream;
     CP_CUDA(cudaMemsetAsync(net->G.qlen, 0, 3 * sizeof(int), s));
@@ -312,11 +335,11 @@ int run_ac(cp_net* net, int level, const int* evt_dev, int nevt, int& launches) 
     CP_CUDA(cudaMemsetAsync(net->G.fb[0], 0, nw * 4, s));
     CP_CUDA(cudaMemsetAsync(net->G.fb[1], 0, nw * 4, s));
     net->G.wait_ns = e->wait_ns;
-    CP_CUDA(launch_ac_grid(net->dn, net->level_ptr(level), evt_dev, nullptr, evt_dev ? nevt : 0, net->G,
-                           net->d_stats, e->block_grid, net->grid_blocks, s));
+    CP_CUDA(launch_ac_grid(net->dn, net->level_ptr(level), evt_dev, nevt_dev, evt_dev ? nevt : 0, net->G, st,
+                           e->block_grid, net->grid_blocks, s));
   } else {
     const int op = evt_dev ? kOpEvents : kOpRoot;
-    CP_CUDA(launch_node(net->dn, net->d_levels, level, level, op, 0, 0, evt_dev, nevt, net->d_stats, nullptr,
+    CP_CUDA(launch_node(net->dn, net->d_levels, level, level, op, 0, 0, evt_dev, nevt, st, nullptr,
                         e->block_node, net->cta_in_smem ? nullptr : net->d_cta_scratch, e->stream));
   }
   ++launches;
@@ -676,26 +699,30 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   CP_CUDA(cudaMemsetAsync(G.epoch, 0, 4 * sizeof(int), s));
   SacScratch& S = net->S;
   CP_TRY(net->alloc(&S.work, total_values));
-  CP_TRY(net->alloc(&S.nwork, 4));
   CP_TRY(net->alloc(&S.ok, total_values));
-  CP_TRY(net->alloc(&S.cursor, 4));
   CP_TRY(net->alloc(&S.evt, n));
-  CP_TRY(net->alloc(&S.nevt, 4));
   CP_TRY(net->alloc(&S.evt_fb, nw));
   CP_TRY(net->alloc(&S.tiles, static_cast<size_t>(n) * 2 * Wi));
-  CP_TRY(net->alloc(&S.ntiles, 4));
-  CP_TRY(net->alloc(&S.tcursor, 4));
   CP_TRY(net->alloc(&S.deep, total_values));
-  CP_TRY(net->alloc(&S.ndeep, 4));
+  // The sweep counters sit together so that one memset clears them.
+  int* ctr = nullptr;
+  CP_TRY(net->alloc(&ctr, 8));
+  S.nwork = ctr;
+  S.cursor = ctr + 1;
+  S.nevt = ctr + 2;
+  S.ntiles = ctr + 3;
+  S.tcursor = ctr + 4;
+  S.ndeep = ctr + 5;
   S.weak = nullptr;
   if (n_tab == 0 && n_bin > 0) CP_TRY(net->alloc(&S.weak, static_cast<size_t>(2) * n_bin * (kWeakK + 1)));
   CP_TRY(net->alloc(&S.snap, static_cast<size_t>(n) * Wi));
-  CP_TRY(net->alloc(&net->d_stats, 1));
+  CP_TRY(net->alloc(&net->d_stats, 2));  // [0] the call's kernels, [1] a level AC queued without a sync
   CP_TRY(net->alloc(&net->d_evt, n));
   CP_TRY(net->alloc(&net->d_sizes, n));
   CP_TRY(net->alloc(&net->d_ok1, total_values));
   {
-    const size_t st_bytes = (sizeof(KStats) + 255) & ~size_t(255);
+    static_assert(2 * sizeof(KStats) <= 256, "two stats slots in the pinned block");
+    const size_t st_bytes = 256;
     const size_t dom_bytes = (static_cast<size_t>(n) * Wi * 8 + 255) & ~size_t(255);
     net->h_block_bytes = st_bytes + dom_bytes + static_cast<size_t>(n) * sizeof(int);
     CP_TRY(e->pinned_get(net->h_block_bytes, &net->h_block));
@@ -916,30 +943,24 @@ int cp_enforce_sac1(cp_net* net, int level, cp_stats* st) {
   Acc acc;
   int launches = 0;
   CP_CUDA(cudaEventRecord(e->ev0, s));
-  // Root AC (SAC1::enforce first runs AC on every variable, src/SAC1.cpp:58).
-  CP_TRY(stats_begin(net));
-  CP_TRY(run_ac(net, level, nullptr, 0, launches));
-  CP_TRY(stats_fetch(net));
-  acc.add(*net->h_stats, 0);
-  bool inconsistent = net->h_stats->inconsistent != 0;
+  // Each sweep is queued behind the level AC that precedes it (the root AC,
+  // SAC1::enforce src/SAC1.cpp:58, then the AC of the previous commit's
+  // removals, :85-92) with no host sync in between: the AC writes stats slot
+  // 1, the sweep slot 0, and one fetch reads both. A sweep queued behind an
+  // AC that wiped a domain out only wastes its work; its results are not used.
+  CP_TRY(stats_begin2(net));
+  CP_TRY(run_ac(net, level, nullptr, 0, launches, net->d_stats + 1));
+  bool inconsistent = false;
   int sweeps = 0;
   double kernel_ms = 0, kernel_bytes = 0;
   const size_t nw = (static_cast<size_t>(net->n) + 31) / 32;
-  while (!inconsistent) {
+  for (;;) {
     ++sweeps;
-    CP_TRY(stats_begin(net));
-    CP_CUDA(cudaMemsetAsync(net->S.nwork, 0, sizeof(int), s));
-    CP_CUDA(cudaMemsetAsync(net->S.cursor, 0, sizeof(int), s));
-    CP_CUDA(cudaMemsetAsync(net->S.nevt, 0, sizeof(int), s));
+    CP_CUDA(cudaMemsetAsync(net->S.nwork, 0, 6 * sizeof(int), s));  // nwork .. ndeep
     CP_CUDA(cudaMemsetAsync(net->S.evt_fb, 0, nw * 4, s));
     const bool tiled = net->tile_grid > 0 && e->sac_mode == 0;
     SacScratch S = net->S;
     if (!tiled) S.tiles = nullptr;
-    if (tiled) {
-      CP_CUDA(cudaMemsetAsync(S.ntiles, 0, sizeof(int), s));
-      CP_CUDA(cudaMemsetAsync(S.tcursor, 0, sizeof(int), s));
-      CP_CUDA(cudaMemsetAsync(S.ndeep, 0, sizeof(int), s));
-    }
     CP_CUDA(launch_build_work(net->dn, net->level_ptr(level), S, s));
     CP_CUDA(cudaEventRecord(e->evk0, s));
     // Mode 0: failed branches remove their value from the level at once
@@ -974,8 +995,14 @@ int cp_enforce_sac1(cp_net* net, int level, cp_stats* st) {
     CP_CUDA(launch_commit(net->dn, net->level_ptr(level), S, net->d_stats, s));
     launches += 3;
     e->launches += 3;
-    CP_TRY(stats_fetch(net));
-    const KStats k = *net->h_stats;
+    CP_TRY(stats_fetch2(net));
+    acc.add(net->h_stats[1], 0);  // the level AC before this sweep
+    if (net->h_stats[1].inconsistent) {
+      inconsistent = true;
+      --sweeps;  // the sweep queued behind the wipe-out does not count
+      break;
+    }
+    const KStats k = net->h_stats[0];
     {
       // Values removed at the level are the failed tests; removals inside the
       // branches' private domain copies are not deletions of this call.
@@ -994,16 +1021,16 @@ int cp_enforce_sac1(cp_net* net, int level, cp_stats* st) {
       kernel_bytes += alg_bytes(net, ka, static_cast<int64_t>(k.branches));
     }
     if (k.removed == 0) break;
-    // Propagate the removals at the level (SAC1.cpp:85-92, batched).
-    int nevt = 0;
-    CP_CUDA(cudaMemcpyAsync(&net->h_sizes[0], net->S.nevt, sizeof(int), cudaMemcpyDeviceToHost, s));
-    CP_CUDA(cudaStreamSynchronize(s));
-    nevt = net->h_sizes[0];
-    CP_TRY(stats_begin(net));
-    CP_TRY(run_ac(net, level, net->S.evt, nevt, launches));
-    CP_TRY(stats_fetch(net));
-    acc.add(*net->h_stats, 0);
-    inconsistent = net->h_stats->inconsistent != 0;
+    // Propagate the removals at the level (SAC1.cpp:85-92, batched) ahead of
+    // the next sweep; the grid path reads the event count on the device.
+    CP_TRY(stats_begin2(net));
+    if (net->prefer_grid) {
+      CP_TRY(run_ac(net, level, net->S.evt, 0, launches, net->d_stats + 1, net->S.nevt));
+    } else {
+      CP_CUDA(cudaMemcpyAsync(&net->h_sizes[0], net->S.nevt, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CP_CUDA(cudaStreamSynchronize(s));
+      CP_TRY(run_ac(net, level, net->S.evt, net->h_sizes[0], launches, net->d_stats + 1));
+    }
   }
   CP_CUDA(cudaEventRecord(e->ev1, s));
   CP_CUDA(cudaEventSynchronize(e->ev1));
