@@ -1519,35 +1519,51 @@ __global__ void k_commit(int W, const int2* work, const int* nwork, const uint8_
   }
 }
 
+// 32x32 bit-matrix transpose across a warp: lane r holds row r (bit c =
+// element (r, c)); afterwards lane r holds column r. Five butterfly steps
+// swap the off-diagonal k x k blocks between lanes r and r ^ k.
+__device__ __forceinline__ u32 warp_transpose32(u32 x) {
+  const int lane = threadIdx.x & 31;
+  const u32 masks[5] = {0x0000ffffu, 0x00ff00ffu, 0x0f0f0f0fu, 0x33333333u, 0x55555555u};
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    const int k = 16 >> i;
+    const u32 m = masks[i];
+    const u32 y = __shfl_xor_sync(kFull, x, k);
+    x = (lane & k) ? ((x & ~m) | ((y >> k) & m)) : ((x & m) | ((y << k) & ~m));
+  }
+  return x;
+}
+
 // B block of constraint c (rows of y values over x values) from its A block,
-// one warp per (c, group of 32 x values): each lane holds one x row; the
-// ballot over lanes of bit b is the 32-bit slice of y=b's row.
+// one warp per (c, 32 y values b): for each 32-value group g of x, the lanes
+// load the 32-bit slices [bb, bb + 32) of x rows g*32 + lane, transpose them
+// in registers, and lane j keeps the slice g of y row bb + j; each y row is
+// then written whole (2W u32 words) by its lane.
 template <int WT>
 __global__ void k_transpose(DevNet N, u64* rel, const int* bx, const int* by, const int64_t* offA,
-                            const int64_t* offB, int groups) {
+                            const int64_t* offB, int chunks) {
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nw = (gridDim.x * blockDim.x) >> 5;
-  for (int item = gw; item < N.nb * groups; item += nw) {
-    const int c = item / groups, g = item % groups;
+  for (int item = gw; item < N.nb * chunks; item += nw) {
+    const int c = item / chunks, bb = (item % chunks) * 32;
     const int dx = N.dsize[bx[c]], dy = N.dsize[by[c]];
-    if (g * 32 >= dx) continue;
-    const int a = g * 32 + lane;
-    u64 row[WT];
+    if (bb >= dy) continue;
+    const u64* A = rel + offA[c];
+    u32 out[2 * WT];
 #pragma unroll
-    for (int w = 0; w < WT; ++w) row[w] = (a < dx) ? rel[offA[c] + static_cast<int64_t>(a) * WT + w] : 0ull;
-    u32* out = reinterpret_cast<u32*>(rel + offB[c]);
-    for (int bb = 0; bb < dy; bb += 32) {
-      u32 mine = 0;
-#pragma unroll 4
-      for (int j = 0; j < 32; ++j) {
-        const int b = bb + j;
-        const bool bit = b < dy && ((sel<WT>(row, b >> 6) >> (b & 63)) & 1ull);
-        const u32 m = __ballot_sync(kFull, bit);
-        if (lane == j) mine = m;
-      }
-      const int b = bb + lane;
-      if (b < dy) out[(static_cast<int64_t>(b) * WT) * 2 + g] = mine;
+    for (int g = 0; g < 2 * WT; ++g) {
+      const int a = g * 32 + lane;
+      u32 slice = 0;
+      if (a < dx) slice = static_cast<u32>(A[static_cast<int64_t>(a) * WT + (bb >> 6)] >> (bb & 32));
+      out[g] = (g * 32 < dx) ? warp_transpose32(slice) : 0u;
+    }
+    const int b = bb + lane;
+    if (b < dy) {
+      u32* row = reinterpret_cast<u32*>(rel + offB[c] + static_cast<int64_t>(b) * WT);
+#pragma unroll
+      for (int g = 0; g < 2 * WT; ++g) row[g] = out[g];
     }
   }
 }
@@ -2072,12 +2088,12 @@ cudaError_t launch_commit(const DevNet& N, u64* dom, SacScratch S, KStats* st, c
 cudaError_t launch_transpose(const DevNet& N, u64* rel, const int* bx, const int* by, const int64_t* offA,
                              const int64_t* offB, cudaStream_t s) {
   if (N.nb == 0) return cudaSuccess;
-  const int groups = 2 * N.W;
+  const int chunks = 2 * N.W;  // 32-value groups of y
   return dispatch_w(N.W, [&](auto wt) -> cudaError_t {
     constexpr int WT = decltype(wt)::value;
-    const int64_t warps = static_cast<int64_t>(N.nb) * groups;
+    const int64_t warps = static_cast<int64_t>(N.nb) * chunks;
     const int blocks = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(8192, (warps * 32 + 255) / 256)));
-    k_transpose<WT><<<blocks, 256, 0, s>>>(N, rel, bx, by, offA, offB, groups);
+    k_transpose<WT><<<blocks, 256, 0, s>>>(N, rel, bx, by, offA, offB, chunks);
     return cudaGetLastError();
   });
 }
