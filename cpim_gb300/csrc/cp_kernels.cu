@@ -1157,8 +1157,8 @@ template <int WT>
 __device__ __forceinline__ void tile_one(const DevNet& N, u64* root, const u64* snap, const u32* weak, bool gs, int x,
                                          int base, int b0,
                                          u32 live, uint8_t* ok, int* deep, int* ndeep, int slot_cap, u64* T,
-                                         int* slot_of, u32& s_fail, u32& s_deep, int& s_next, u64& c_rev, u64& c_rows,
-                                         u64& c_done) {
+                                         int* slot_of, u32& s_fail, u32& s_deep, int& s_next, int* s_rem, u64& c_rev,
+                                         u64& c_rows, u64& c_done) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   {
     const int a0 = N.arc_start[x], deg = N.arc_start[x + 1] - a0;
@@ -1211,7 +1211,15 @@ __device__ __forceinline__ void tile_one(const DevNet& N, u64* root, const u64* 
       if (threadIdx.x == 0) s_next = 0;
       __syncthreads();
       // Round two, tested only; warps take neighbours y dynamically (their
-      // costs differ), so fewer wait at the barrier that ends the tile.
+      // costs differ), so fewer wait at the barrier that ends the tile. Lane j
+      // of a warp owns arc jb + j out of y. A value v of z can lose every
+      // support in branch b only if its support count in D0(y) is at most the
+      // number of values of D0(y) that b's round one removed (pigeonhole), so a
+      // lane tests just those (branch, value) pairs, taking v from the arc's
+      // weak list in increasing count order: one row load per value serves all
+      // its branches. Branches that reach past the end of an arc's list need
+      // the whole arc: the warp revises such arcs together, one lane per branch.
+      int* rem = s_rem + warp * 32;  // removed count of each open branch, -1 if closed
       for (;;) {
         int item = 0;
         if (lane == 0) item = atomicAdd(&s_next, 1);
@@ -1220,146 +1228,184 @@ __device__ __forceinline__ void tile_one(const DevNet& N, u64* root, const u64* 
         if (s >= deg) break;
         const int y = N.arcs[a0 + s].z;
         if (slot_of[y] != s) continue;
+        const u64* Ty = T + static_cast<size_t>(s) * 32 * WT;  // D_b(y) at Ty + b * WT
         u64 dy[WT];
-        int removed = 0;  // values of y this lane's round one removed
+        int removed = 0;  // values of D0(y) this lane's round one removed
 #pragma unroll
         for (int w = 0; w < WT; ++w) {
-          dy[w] = T[(static_cast<size_t>(s) * 32 + lane) * WT + w];
+          dy[w] = Ty[lane * WT + w];
           removed += __popcll(__ldg(snap + static_cast<size_t>(y) * WT + w)) - __popcll(dy[w]);
         }
-        // Above thr every value of z keeps a support in any lane's D(y)
-        // (pigeonhole over the removed values): only the listed weak values
-        // need a row test.
-        int thr = ((live >> lane) & 1u) ? removed : 0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) thr = max(thr, __shfl_xor_sync(kFull, thr, o));
         const int y0 = N.arc_start[y], y1 = N.arc_start[y + 1];
         for (int jb = y0 + 32 * half; jb < y1; jb += 64) {
-          // Lanes still open (live, not failed, not handed over), warp-uniform.
+          // Branches still open (live, not failed, not handed over), warp-uniform.
           const u32 done_m = __shfl_sync(kFull, *reinterpret_cast<volatile u32*>(&s_fail) |
                                                     *reinterpret_cast<volatile u32*>(&s_deep), 0);
           const u32 open = live & ~done_m;
           if (!open) break;
-          // 32 arcs classified at once (lane l: arc jb + l), so their loads
-          // overlap: an arc whose weakest value of z has more supports than
-          // any lane's D(y) lost can remove nothing and needs no test.
+          const int r_own = ((open >> lane) & 1u) ? removed : -1;
+          __syncwarp();
+          rem[lane] = r_own;
+          __syncwarp();
           const int jl = jb + lane;
-          bool arc_in = false, act = false;
+          Arc A{};
+          bool arc_in = false;
           if (jl < y1) {
-            arc_in = N.arcs[jl].z != x;
-            const u32 e0 = weak ? __ldg(weak + static_cast<size_t>(jl) * (kWeakK + 1)) : 0u;
-            act = arc_in && static_cast<int>(e0 >> 16) <= thr;
+            A = N.arcs[jl];
+            arc_in = A.z != x;
           }
+          // Lowest support count among the arc's values (0 without lists:
+          // every open branch then needs the whole arc).
+          const u32* wl = weak ? weak + static_cast<size_t>(jl) * (kWeakK + 1) : nullptr;
+          const u32 e0 = (wl && arc_in) ? __ldg(wl) : 0u;
+          const int c0 = static_cast<int>(e0 >> 16);
           const u32 arcs_m = __ballot_sync(kFull, arc_in);
-          u32 todo = __ballot_sync(kFull, act);
-          if (lane == 0) c_rev += __popc(arcs_m & ~todo);
-          while (todo) {
-            const int j = jb + __ffs(todo) - 1;
-            todo &= todo - 1;
-            const Arc A = N.arcs[j];
-            const int z = A.z;
-            const int sz = slot_of[z];
-            u64 cur[WT];
-            if (sz >= 0) {
-#pragma unroll
-              for (int w = 0; w < WT; ++w) cur[w] = T[(static_cast<size_t>(sz) * 32 + lane) * WT + w];
-            } else {
-#pragma unroll
-              for (int w = 0; w < WT; ++w) cur[w] = root[static_cast<size_t>(z) * WT + w];
+          if (lane == 0) c_rev += __popc(arcs_m);
+          // This lane's branches: open ones whose removed count reaches c0.
+          const int cmin = __reduce_min_sync(kFull, arc_in ? c0 : 0x7fffffff);
+          u32 bm = 0;
+          for (u32 m = __ballot_sync(kFull, r_own >= cmin); m; m &= m - 1) {
+            const int b = __ffs(m) - 1;
+            const int rb = __shfl_sync(kFull, r_own, b);
+            if (arc_in && rb >= c0) bm |= 1u << b;
+          }
+          u32 fm = 0;  // branches that need this lane's arc in full
+          if (bm) {
+            const int cnext = wl ? static_cast<int>(__ldg(wl + kWeakK) >> 16) : 0;
+            u32 wm = 0;
+            for (u32 m = bm; m; m &= m - 1) {
+              const int b = __ffs(m) - 1;
+              if (rem[b] >= cnext)
+                fm |= 1u << b;
+              else
+                wm |= 1u << b;
             }
-            const bool mine = (open >> lane) & 1u;
-            bool still = false, left = false;
-            int loaded = 0;
-            // Lane k < kWeakK holds list entry k, lane kWeakK the next count;
-            // the lanes of candidate entries load their rows at once.
-            const u32* wl = weak ? weak + static_cast<size_t>(j) * (kWeakK + 1) : nullptr;
-            const u32 ent = (wl && lane <= kWeakK) ? __ldg(wl + lane) : 0xffffffffu;
-            const int next_cnt = static_cast<int>(__shfl_sync(kFull, ent, kWeakK) >> 16);
-            if (wl && next_cnt > thr) {
-              // Weak values only: v loses all supports iff its row misses D(y).
-              const bool cand = lane < kWeakK && static_cast<int>(ent >> 16) <= thr;
-              u64 row[WT];
+            if (wm) {
+              const int sz = slot_of[A.z];
+              const u64* Tz = T + static_cast<size_t>(sz < 0 ? 0 : sz) * 32 * WT;  // D_b(z) if z neighbours x
+              u64 cz[WT];  // D(z) otherwise, the same in every branch
 #pragma unroll
-              for (int q = 0; q < WT; ++q) row[q] = 0;
-              if (cand) load_row<WT>(N.rel, A.zy + static_cast<size_t>(ent & 0xffffu) * WT, row);
-              u32 cm = __ballot_sync(kFull, cand);
-              loaded = __popc(cm);
-              int unsup = 0;
-              while (cm) {
-                const int k = __ffs(cm) - 1;
-                cm &= cm - 1;
-                const u32 e = __shfl_sync(kFull, ent, k);
+              for (int w = 0; w < WT; ++w) cz[w] = sz < 0 ? root[static_cast<size_t>(A.z) * WT + w] : 0ull;
+              u32 hitm = 0;  // branches in which some listed value of z loses every support
+              u64 nrows = 0;
+              for (int k = 0; k < kWeakK; ++k) {
+                const u32 e = k == 0 ? e0 : __ldg(wl + k);
                 const int cnt = static_cast<int>(e >> 16);
+                // Counts increase along the list: a branch out of reach stays so.
+                u32 bk = 0;
+                for (u32 m = wm; m; m &= m - 1) {
+                  const int b = __ffs(m) - 1;
+                  if (rem[b] >= cnt) bk |= 1u << b;
+                }
+                wm = bk;
+                if (!bk) break;
                 const int v = static_cast<int>(e & 0xffffu);
-                u64 hit = 0;
+                const int vw = v >> 6;
+                const u64 vbit = 1ull << (v & 63);
+                u64 row[WT];
+                load_row<WT>(N.rel, A.zy + static_cast<size_t>(v) * WT, row);
+                ++nrows;
+                const bool in_cz = (sel<WT>(cz, vw) & vbit) != 0;
+                for (u32 m = bk; m; m &= m - 1) {
+                  const int b = __ffs(m) - 1;
+                  if (!(sz < 0 ? in_cz : (Tz[b * WT + vw] & vbit) != 0)) continue;
+                  u64 hit = 0;
 #pragma unroll
-                for (int q = 0; q < WT; ++q) hit |= shfl64(row[q], k) & dy[q];
-                const bool need = mine && removed >= cnt && ((sel<WT>(cur, v >> 6) >> (v & 63)) & 1ull);
-                if (need && hit == 0) ++unsup;
+                  for (int w = 0; w < WT; ++w) hit |= row[w] & Ty[b * WT + w];
+                  if (!hit) hitm |= 1u << b;
+                }
               }
-              if (unsup) {
-                int size = 0;
+              // Rare: round two removes values of z in branch b. A wipeout of
+              // D_b(z) fails b, anything less hands it over.
+              for (u32 m = hitm; m; m &= m - 1) {
+                const int b = __ffs(m) - 1;
+                const int rb = rem[b];
+                int unsup = 0, size = 0;
 #pragma unroll
-                for (int q = 0; q < WT; ++q) size += __popcll(cur[q]);
-                still = true;
-                left = unsup < size;
+                for (int w = 0; w < WT; ++w) size += __popcll(sz < 0 ? cz[w] : Tz[b * WT + w]);
+                for (int k = 0; k < kWeakK; ++k) {
+                  const u32 e = __ldg(wl + k);
+                  if (static_cast<int>(e >> 16) > rb) break;
+                  const int v = static_cast<int>(e & 0xffffu);
+                  const u64 vbit = 1ull << (v & 63);
+                  if (!((sz < 0 ? sel<WT>(cz, v >> 6) : Tz[b * WT + (v >> 6)]) & vbit)) continue;
+                  u64 row[WT];
+                  load_row<WT>(N.rel, A.zy + static_cast<size_t>(v) * WT, row);
+                  ++nrows;
+                  u64 hit = 0;
+#pragma unroll
+                  for (int w = 0; w < WT; ++w) hit |= row[w] & Ty[b * WT + w];
+                  if (!hit) ++unsup;
+                }
+                atomicOr(unsup < size ? &s_deep : &s_fail, 1u << b);
               }
-            } else {
-              u64 uc[WT], acc[WT];
+              c_rows += nrows;
+            }
+          }
+          // Arcs whose list does not cover some branch: the warp revises each,
+          // lane l for branch l, over the rows of the values of y that some
+          // such branch still has, 32 values per chunk, 8 rows between
+          // coverage tests; a lane ORs the rows of its own values (a
+          // predicated OR per row: the row address and the skip test are
+          // warp-uniform). Stops once every such branch's accumulated support
+          // covers its D(z).
+          for (u32 fullm = __ballot_sync(kFull, fm != 0); fullm; fullm &= fullm - 1) {
+            const int k = __ffs(fullm) - 1;
+            const bool mine = (__shfl_sync(kFull, fm, k) >> lane) & 1u;
+            const Arc Af = N.arcs[jb + k];
+            const int sz = slot_of[Af.z];
+            u64 cur[WT];
 #pragma unroll
-              for (int w = 0; w < WT; ++w) {
-                uc[w] = warp_or64(mine ? dy[w] : 0ull);
-                acc[w] = 0;
-              }
-              // Rows of the values of y that some open lane still has, 32 values
-              // per chunk, 8 rows between coverage tests; a lane ORs the rows of
-              // its own values (a predicated OR per row: the row address and the
-              // skip test are warp-uniform). Stops once every open lane's
-              // accumulated support covers its D(z).
-              bool go = true;
+            for (int w = 0; w < WT; ++w)
+              cur[w] = sz >= 0 ? T[(static_cast<size_t>(sz) * 32 + lane) * WT + w] : root[static_cast<size_t>(Af.z) * WT + w];
+            u64 uc[WT], acc[WT];
 #pragma unroll
-              for (int h = 0; h < 2 * WT; ++h) {
-                const u32 ucw = static_cast<u32>(sel<WT>(uc, h >> 1) >> ((h & 1) * 32));
-                const u32 myb = mine ? static_cast<u32>(sel<WT>(dy, h >> 1) >> ((h & 1) * 32)) : 0u;
-                if (ucw == 0) continue;
-                const u64* rc = N.rel + A.yz + static_cast<size_t>(h) * 32 * WT;
+            for (int w = 0; w < WT; ++w) {
+              uc[w] = warp_or64(mine ? dy[w] : 0ull);
+              acc[w] = 0;
+            }
+            int loaded = 0;
+            bool go = true;
 #pragma unroll
-                for (int j0 = 0; j0 < 32; j0 += 8) {
-                  const u32 chunk = (ucw >> j0) & 0xffu;
-                  if (!go || chunk == 0) continue;
+            for (int h = 0; h < 2 * WT; ++h) {
+              const u32 ucw = static_cast<u32>(sel<WT>(uc, h >> 1) >> ((h & 1) * 32));
+              const u32 myb = mine ? static_cast<u32>(sel<WT>(dy, h >> 1) >> ((h & 1) * 32)) : 0u;
+              if (ucw == 0) continue;
+              const u64* rc = N.rel + Af.yz + static_cast<size_t>(h) * 32 * WT;
 #pragma unroll
-                  for (int jj = 0; jj < 8; ++jj) {
-                    if ((chunk >> jj) & 1u) {
-                      u64 r[WT];
-                      load_row<WT>(rc, static_cast<size_t>(j0 + jj) * WT, r);
-                      ++loaded;
-                      if ((myb >> (j0 + jj)) & 1u) {
+              for (int j0 = 0; j0 < 32; j0 += 8) {
+                const u32 chunk = (ucw >> j0) & 0xffu;
+                if (!go || chunk == 0) continue;
 #pragma unroll
-                        for (int q = 0; q < WT; ++q) acc[q] |= r[q];
-                      }
+                for (int jj = 0; jj < 8; ++jj) {
+                  if ((chunk >> jj) & 1u) {
+                    u64 r[WT];
+                    load_row<WT>(rc, static_cast<size_t>(j0 + jj) * WT, r);
+                    ++loaded;
+                    if ((myb >> (j0 + jj)) & 1u) {
+#pragma unroll
+                      for (int q = 0; q < WT; ++q) acc[q] |= r[q];
                     }
                   }
-                  u64 gap = 0;
-#pragma unroll
-                  for (int q = 0; q < WT; ++q) gap |= cur[q] & ~acc[q];
-                  if (__ballot_sync(kFull, mine && gap != 0) == 0) go = false;  // every open lane covered
                 }
-              }
-              if (go) {
-                u64 gap = 0, kept = 0;
+                u64 gap = 0;
 #pragma unroll
-                for (int q = 0; q < WT; ++q) {
-                  gap |= cur[q] & ~acc[q];
-                  kept |= cur[q] & acc[q];
-                }
-                still = mine && gap != 0;
-                left = kept != 0;
+                for (int q = 0; q < WT; ++q) gap |= cur[q] & ~acc[q];
+                if (__ballot_sync(kFull, mine && gap != 0) == 0) go = false;  // every such branch covered
               }
             }
-            if (lane == 0) {
-              ++c_rev;
-              c_rows += loaded;
+            bool still = false, left = false;
+            if (go) {
+              u64 gap = 0, kept = 0;
+#pragma unroll
+              for (int q = 0; q < WT; ++q) {
+                gap |= cur[q] & ~acc[q];
+                kept |= cur[q] & acc[q];
+              }
+              still = mine && gap != 0;
+              left = kept != 0;
             }
+            if (lane == 0) c_rows += loaded;
             if (still) atomicOr(left ? &s_deep : &s_fail, 1u << lane);
           }
         }
@@ -1482,6 +1528,7 @@ __global__ void __launch_bounds__(256, WT <= 2 ? 5 : 1) k_sac_tile(DevNet N, u64
   __shared__ int s_t;
   __shared__ u32 s_fail, s_deep;
   __shared__ int s_next;
+  __shared__ int s_rem[256];  // 256-thread CTAs: 32 per warp
   const int total = *ntiles;
   for (int i = threadIdx.x; i < N.n; i += blockDim.x) slot_of[i] = -1;
   u64 c_rev = 0, c_rows = 0, c_done = 0;
@@ -1496,7 +1543,7 @@ __global__ void __launch_bounds__(256, WT <= 2 ? 5 : 1) k_sac_tile(DevNet N, u64
     if (t >= total) break;
     const int4 tl = tiles[t];
     tile_one<WT>(N, root, snap ? snap : root, weak, snap != nullptr, tl.x, tl.y, tl.z, static_cast<u32>(tl.w), ok,
-                 deep, ndeep, slot_cap, T, slot_of, s_fail, s_deep, s_next, c_rev, c_rows, c_done);
+                 deep, ndeep, slot_cap, T, slot_of, s_fail, s_deep, s_next, s_rem, c_rev, c_rows, c_done);
   }
   flush_tile_counts(st, c_rev, c_rows, c_done);
 }
@@ -1717,6 +1764,7 @@ __global__ void __launch_bounds__(256, WT <= 2 ? 4 : 1) k_batch_tile(BatchDev B,
   __shared__ int s_t;
   __shared__ u32 s_fail, s_deep;
   __shared__ int s_next;
+  __shared__ int s_rem[256];  // 256-thread CTAs: 32 per warp
   __shared__ DevNet sN;
   const int total = *B.ntiles;
   for (int i = threadIdx.x; i < max_n; i += blockDim.x) slot_of[i] = -1;
@@ -1735,7 +1783,7 @@ __global__ void __launch_bounds__(256, WT <= 2 ? 4 : 1) k_batch_tile(BatchDev B,
     const int inst = tl.x >> 16;
     tile_one<WT>(sN, B.roots[inst], B.snap ? B.snap + static_cast<size_t>(B.var_base[inst]) * WT : B.roots[inst],
                  B.weak ? B.weak + B.weak_off[inst] : nullptr, B.snap != nullptr, tl.x & 0xffff, tl.y, tl.z, static_cast<u32>(tl.w), B.ok, B.deep, B.ndeep,
-                 slot_cap, T, slot_of, s_fail, s_deep, s_next, c_rev, c_rows, c_done);
+                 slot_cap, T, slot_of, s_fail, s_deep, s_next, s_rem, c_rev, c_rows, c_done);
   }
   flush_tile_counts(st, c_rev, c_rows, c_done);
 }
@@ -2050,6 +2098,7 @@ int sac_tile_blocks_per_sm(const DevNet& N, int slot_cap, int block) {
 
 cudaError_t launch_sac_tile(const DevNet& N, u64* root, SacScratch S, uint8_t* ok, int slot_cap, KStats* st,
                             int block, int grid, cudaStream_t s) {
+  if (block > 256 || block % 32) return cudaErrorInvalidValue;  // per-warp shared arrays are sized for 256
   const size_t smem = sac_tile_smem(N, slot_cap);
   return dispatch_w(N.W, [&](auto wt) -> cudaError_t {
     constexpr int WT = decltype(wt)::value;
