@@ -714,7 +714,7 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   S.tcursor = ctr + 4;
   S.ndeep = ctr + 5;
   S.weak = nullptr;
-  if (n_tab == 0 && n_bin > 0) CP_TRY(net->alloc(&S.weak, static_cast<size_t>(2) * n_bin * (kWeakK + 1)));
+  if (n_tab == 0 && n_bin > 0) CP_TRY(net->alloc(&S.weak, static_cast<size_t>(2) * n_bin * kWeakStride));
   CP_TRY(net->alloc(&S.snap, static_cast<size_t>(n) * Wi));
   CP_TRY(net->alloc(&net->d_stats, 2));  // [0] the call's kernels, [1] a level AC queued without a sync
   CP_TRY(net->alloc(&net->d_evt, n));
@@ -757,7 +757,7 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   // domains of up to slot_cap neighbours for 32 branches, plus a slot map.
   for (int x = 0; x < n; ++x) net->max_deg = std::max(net->max_deg, arc_deg[x]);
   if (n_tab == 0) {
-    const size_t per_slot = static_cast<size_t>(32) * Wi * 8;
+    const size_t per_slot = static_cast<size_t>(32) * Wi * 8 + 16;  // domains + neighbour record
     int cap = std::max(net->max_deg, 1);
     // 100 KB keeps two or more tile CTAs per SM; a network whose densest
     // variable needs more gets up to the opt-in limit (fewer, larger CTAs)
@@ -2011,7 +2011,7 @@ int batch_group_setup(cp_batch* b, BatchGroup& g) {
     offs[i] = b->out_off[g.members[i]];
     wuser[i] = n->W_user;
     woff[i] = weak_words;
-    weak_words += static_cast<int64_t>(2) * n->nb * (kWeakK + 1);
+    weak_words += static_cast<int64_t>(2) * n->nb * kWeakStride;
     var_base[i + 1] = var_base[i] + n->n;
     g.max_n = std::max(g.max_n, n->n);
     g.cta_bytes = std::max(g.cta_bytes, cta_state_bytes(n->dn));
@@ -2103,7 +2103,7 @@ int batch_group_setup(cp_batch* b, BatchGroup& g) {
   g.tiled = false;
   g.tile_grid = 0;
   if (!g.tables && g.max_n < 65536) {
-    const size_t per_slot = static_cast<size_t>(32) * g.W * 8;
+    const size_t per_slot = static_cast<size_t>(32) * g.W * 8 + 16;  // domains + neighbour record
     const size_t optin = e->smem_optin > 4096 ? e->smem_optin - 4096 : 0;
     const size_t need = static_cast<size_t>(g.max_n) * 4 + per_slot * static_cast<size_t>(max_deg);
     const size_t budget = std::min<size_t>(optin, g.dense ? need : 100 * 1024);

@@ -28,10 +28,12 @@ using u64 = unsigned long long;
 using u32 = unsigned int;
 
 constexpr int kMaxArity = 4;
-// Weak-support lists of the tiled SAC sweep: per directional arc, the kWeakK
-// values of the revised variable with the fewest supports, then the count of
-// the next one.
+// Weak-support lists of the tiled SAC sweep: per directional arc, kWeakStride
+// words (80 bytes, 16-byte aligned): the support count of the (kWeakK+1)-th
+// weakest value, then the kWeakK values of the revised variable with the
+// fewest supports, then padding.
 constexpr int kWeakK = 16;
+constexpr int kWeakStride = 20;
 constexpr int kItemVarShift = 12;             // work item = (var << 12) | chunk
 constexpr int kMaxChunksPerVar = 1 << kItemVarShift;
 constexpr int kMaxVars = 1 << (32 - kItemVarShift);
@@ -104,7 +106,7 @@ struct SacScratch {
   int* tcursor;       // [1]
   int* deep;          // work indices the tiled kernel hands to the general one
   int* ndeep;         // [1]
-  u32* weak;          // [2*nb][kWeakK + 1] weak-support lists (null: not built)
+  u32* weak;          // [2*nb][kWeakStride] weak-support lists (null: not built)
   u64* snap;          // [n*W] the level's domains at the start of the sweep
 };
 

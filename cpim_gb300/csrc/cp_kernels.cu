@@ -1157,7 +1157,7 @@ template <int WT>
 __device__ __forceinline__ void tile_one(const DevNet& N, u64* root, const u64* snap, const u32* weak, bool gs, int x,
                                          int base, int b0,
                                          u32 live, uint8_t* ok, int* deep, int* ndeep, int slot_cap, u64* T,
-                                         int* slot_of, u32& s_fail, u32& s_deep, int& s_next, int* s_rem, u64& c_rev,
+                                         int4* nbr, int* slot_of, u32& s_fail, u32& s_deep, int& s_next, int* s_rem, u64& c_rev,
                                          u64& c_rows, u64& c_done) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   {
@@ -1170,12 +1170,21 @@ __device__ __forceinline__ void tile_one(const DevNet& N, u64* root, const u64* 
       // The first arc to each neighbour z writes D_a(z) = D0(z) & row(x = a)
       // (lanes without a branch keep D0(z)); further constraints on the same
       // pair, if any, AND their rows in afterwards.
+      // Lane 0 also records the neighbour for round two: z, its arc range
+      // and |D0(z)| in the sweep-start snapshot (-1: a repeated neighbour).
       bool dup = false;
       for (int i = warp; i < deg; i += nwarps) {
         const Arc A = N.arcs[a0 + i];
         if (slot_of[A.z] != i) {
           dup = true;
+          if (lane == 0) nbr[i] = make_int4(-1, 0, 0, 0);
           continue;
+        }
+        if (lane == 0) {
+          int c = 0;
+#pragma unroll
+          for (int w = 0; w < WT; ++w) c += __popcll(__ldg(snap + static_cast<size_t>(A.z) * WT + w));
+          nbr[i] = make_int4(A.z, N.arc_start[A.z], N.arc_start[A.z + 1], c);
         }
         u64 d[WT], r[WT];
 #pragma unroll
@@ -1226,17 +1235,17 @@ __device__ __forceinline__ void tile_one(const DevNet& N, u64* root, const u64* 
         item = __shfl_sync(kFull, item, 0);
         const int s = item >> 1, half = item & 1;  // two items per neighbour: alternate 32-arc chunks
         if (s >= deg) break;
-        const int y = N.arcs[a0 + s].z;
-        if (slot_of[y] != s) continue;
+        const int4 ny = nbr[s];
+        if (ny.x < 0) continue;
+        const int y0 = ny.y, y1 = ny.z;
         const u64* Ty = T + static_cast<size_t>(s) * 32 * WT;  // D_b(y) at Ty + b * WT
         u64 dy[WT];
-        int removed = 0;  // values of D0(y) this lane's round one removed
+        int removed = ny.w;  // values of D0(y) this lane's round one removed
 #pragma unroll
         for (int w = 0; w < WT; ++w) {
           dy[w] = Ty[lane * WT + w];
-          removed += __popcll(__ldg(snap + static_cast<size_t>(y) * WT + w)) - __popcll(dy[w]);
+          removed -= __popcll(dy[w]);
         }
-        const int y0 = N.arc_start[y], y1 = N.arc_start[y + 1];
         for (int jb = y0 + 32 * half; jb < y1; jb += 64) {
           // Branches still open (live, not failed, not handed over), warp-uniform.
           const u32 done_m = __shfl_sync(kFull, *reinterpret_cast<volatile u32*>(&s_fail) |
@@ -1248,17 +1257,18 @@ __device__ __forceinline__ void tile_one(const DevNet& N, u64* root, const u64* 
           rem[lane] = r_own;
           __syncwarp();
           const int jl = jb + lane;
+          const u32* wl = weak ? weak + static_cast<size_t>(jl) * kWeakStride : nullptr;
           Arc A{};
           bool arc_in = false;
+          uint4 wv = make_uint4(0u, 0u, 0u, 0u);  // next count, entries 0..2 (zeros without lists)
           if (jl < y1) {
             A = N.arcs[jl];
+            if (wl) wv = __ldg(reinterpret_cast<const uint4*>(wl));
             arc_in = A.z != x;
           }
           // Lowest support count among the arc's values (0 without lists:
           // every open branch then needs the whole arc).
-          const u32* wl = weak ? weak + static_cast<size_t>(jl) * (kWeakK + 1) : nullptr;
-          const u32 e0 = (wl && arc_in) ? __ldg(wl) : 0u;
-          const int c0 = static_cast<int>(e0 >> 16);
+          const int c0 = static_cast<int>(wv.y >> 16);
           const u32 arcs_m = __ballot_sync(kFull, arc_in);
           if (lane == 0) c_rev += __popc(arcs_m);
           // This lane's branches: open ones whose removed count reaches c0.
@@ -1271,16 +1281,33 @@ __device__ __forceinline__ void tile_one(const DevNet& N, u64* root, const u64* 
           }
           u32 fm = 0;  // branches that need this lane's arc in full
           if (bm) {
-            const int cnext = wl ? static_cast<int>(__ldg(wl + kWeakK) >> 16) : 0;
+            const int cnext = static_cast<int>(wv.x >> 16);
             u32 wm = 0;
+            int rmax = -1;  // the largest removed count among the list's branches
             for (u32 m = bm; m; m &= m - 1) {
               const int b = __ffs(m) - 1;
-              if (rem[b] >= cnext)
+              const int r = rem[b];
+              if (r >= cnext) {
                 fm |= 1u << b;
-              else
+              } else {
                 wm |= 1u << b;
+                rmax = max(rmax, r);
+              }
             }
             if (wm) {
+              // Rows of the first kPre entries in one wave of loads, with D(z).
+              constexpr int kPre = WT <= 2 ? 3 : 1;
+              const u32 ent[3] = {wv.y, wv.z, wv.w};
+              u64 pre[kPre][WT];
+#pragma unroll
+              for (int p = 0; p < kPre; ++p) {
+                if (static_cast<int>(ent[p] >> 16) <= rmax) {
+                  load_row<WT>(N.rel, A.zy + static_cast<size_t>(ent[p] & 0xffffu) * WT, pre[p]);
+                } else {
+#pragma unroll
+                  for (int w = 0; w < WT; ++w) pre[p][w] = 0;
+                }
+              }
               const int sz = slot_of[A.z];
               const u64* Tz = T + static_cast<size_t>(sz < 0 ? 0 : sz) * 32 * WT;  // D_b(z) if z neighbours x
               u64 cz[WT];  // D(z) otherwise, the same in every branch
@@ -1288,32 +1315,42 @@ __device__ __forceinline__ void tile_one(const DevNet& N, u64* root, const u64* 
               for (int w = 0; w < WT; ++w) cz[w] = sz < 0 ? root[static_cast<size_t>(A.z) * WT + w] : 0ull;
               u32 hitm = 0;  // branches in which some listed value of z loses every support
               u64 nrows = 0;
-              for (int k = 0; k < kWeakK; ++k) {
-                const u32 e = k == 0 ? e0 : __ldg(wl + k);
+              // Entry e with row r: the branches that reach its count test it.
+              // Counts increase along the list, so a branch out of reach stays so.
+              auto entry = [&](u32 e, const u64 (&r)[WT]) -> bool {
                 const int cnt = static_cast<int>(e >> 16);
-                // Counts increase along the list: a branch out of reach stays so.
                 u32 bk = 0;
                 for (u32 m = wm; m; m &= m - 1) {
                   const int b = __ffs(m) - 1;
                   if (rem[b] >= cnt) bk |= 1u << b;
                 }
                 wm = bk;
-                if (!bk) break;
+                if (!bk) return false;
+                ++nrows;
                 const int v = static_cast<int>(e & 0xffffu);
                 const int vw = v >> 6;
                 const u64 vbit = 1ull << (v & 63);
-                u64 row[WT];
-                load_row<WT>(N.rel, A.zy + static_cast<size_t>(v) * WT, row);
-                ++nrows;
                 const bool in_cz = (sel<WT>(cz, vw) & vbit) != 0;
                 for (u32 m = bk; m; m &= m - 1) {
                   const int b = __ffs(m) - 1;
                   if (!(sz < 0 ? in_cz : (Tz[b * WT + vw] & vbit) != 0)) continue;
                   u64 hit = 0;
 #pragma unroll
-                  for (int w = 0; w < WT; ++w) hit |= row[w] & Ty[b * WT + w];
+                  for (int w = 0; w < WT; ++w) hit |= r[w] & Ty[b * WT + w];
                   if (!hit) hitm |= 1u << b;
                 }
+                return true;
+              };
+              bool more = true;
+#pragma unroll
+              for (int p = 0; p < kPre; ++p)
+                if (more) more = entry(ent[p], pre[p]);
+              for (int k = kPre; more && k < kWeakK; ++k) {
+                const u32 e = __ldg(wl + 1 + k);
+                if (static_cast<int>(e >> 16) > rmax) break;
+                u64 r[WT];
+                load_row<WT>(N.rel, A.zy + static_cast<size_t>(e & 0xffffu) * WT, r);
+                more = entry(e, r);
               }
               // Rare: round two removes values of z in branch b. A wipeout of
               // D_b(z) fails b, anything less hands it over.
@@ -1324,7 +1361,7 @@ __device__ __forceinline__ void tile_one(const DevNet& N, u64* root, const u64* 
 #pragma unroll
                 for (int w = 0; w < WT; ++w) size += __popcll(sz < 0 ? cz[w] : Tz[b * WT + w]);
                 for (int k = 0; k < kWeakK; ++k) {
-                  const u32 e = __ldg(wl + k);
+                  const u32 e = __ldg(wl + 1 + k);
                   if (static_cast<int>(e >> 16) > rb) break;
                   const int v = static_cast<int>(e & 0xffffu);
                   const u64 vbit = 1ull << (v & 63);
@@ -1436,10 +1473,11 @@ __device__ __forceinline__ void tile_one(const DevNet& N, u64* root, const u64* 
 }
 
 // Weak-support lists for the root domains: per directional arc j (revise z
-// against y), the kWeakK values v of D(z) with the fewest supports
-// |row_zy(v) & D(y)| in increasing (count, v) order as count << 16 | v, then
-// the next count << 16 (0xffff: none). One warp per arc; the smallest keys are
-// taken by repeated warp minima.
+// against y), at word 0 the count of the (kWeakK+1)-th weakest value as
+// count << 16 | 0xffff (0xffffffff: none), then the kWeakK values v of D(z)
+// with the fewest supports |row_zy(v) & D(y)| in increasing (count, v) order
+// as count << 16 | v (0xffffffff past the end), then padding. One warp per
+// arc; the smallest keys are taken by repeated warp minima.
 template <int WT>
 __device__ void weak_list_arc(const DevNet& N, const u64* root, const u64 (&dy)[WT], int j, u32* weak) {
   const int lane = threadIdx.x & 31;
@@ -1461,16 +1499,24 @@ __device__ void weak_list_arc(const DevNet& N, const u64* root, const u64 (&dy)[
       key[t] = (static_cast<u32>(c) << 16) | static_cast<u32>(v);
     }
   }
-  u32* out = weak + static_cast<size_t>(j) * (kWeakK + 1);
+  u32* out = weak + static_cast<size_t>(j) * kWeakStride;
+  if (lane > kWeakK && lane < kWeakStride) out[lane] = 0xffffffffu;  // padding
   for (int k = 0; k <= kWeakK; ++k) {
     u32 m = key[0];
 #pragma unroll
     for (int t = 1; t < 2 * WT; ++t) m = min(m, key[t]);
     m = __reduce_min_sync(kFull, m);
-    if (lane == 0) out[k] = k < kWeakK ? m : (m | 0xffffu);
+    if (lane == 0) {
+      if (k < kWeakK)
+        out[1 + k] = m;
+      else
+        out[0] = m | 0xffffu;
+    }
     if (m == 0xffffffffu) {
-      if (lane == 0)
-        for (int r = k + 1; r <= kWeakK; ++r) out[r] = 0xffffffffu;
+      if (lane == 0) {
+        for (int r = k + 1; r < kWeakK; ++r) out[1 + r] = 0xffffffffu;
+        out[0] = 0xffffffffu;
+      }
       break;
     }
 #pragma unroll
@@ -1524,7 +1570,8 @@ __global__ void __launch_bounds__(256, WT <= 2 ? 5 : 1) k_sac_tile(DevNet N, u64
                                                                    KStats* st, const u32* weak) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   u64* T = reinterpret_cast<u64*>(smem_raw);  // [slot_cap][32][WT]
-  int* slot_of = reinterpret_cast<int*>(smem_raw + static_cast<size_t>(slot_cap) * 32 * WT * 8);  // [n]
+  int4* nbr = reinterpret_cast<int4*>(smem_raw + static_cast<size_t>(slot_cap) * 32 * WT * 8);  // [slot_cap]
+  int* slot_of = reinterpret_cast<int*>(nbr + slot_cap);  // [n]
   __shared__ int s_t;
   __shared__ u32 s_fail, s_deep;
   __shared__ int s_next;
@@ -1543,7 +1590,7 @@ __global__ void __launch_bounds__(256, WT <= 2 ? 5 : 1) k_sac_tile(DevNet N, u64
     if (t >= total) break;
     const int4 tl = tiles[t];
     tile_one<WT>(N, root, snap ? snap : root, weak, snap != nullptr, tl.x, tl.y, tl.z, static_cast<u32>(tl.w), ok,
-                 deep, ndeep, slot_cap, T, slot_of, s_fail, s_deep, s_next, s_rem, c_rev, c_rows, c_done);
+                 deep, ndeep, slot_cap, T, nbr, slot_of, s_fail, s_deep, s_next, s_rem, c_rev, c_rows, c_done);
   }
   flush_tile_counts(st, c_rev, c_rows, c_done);
 }
@@ -1760,7 +1807,8 @@ template <int WT>
 __global__ void __launch_bounds__(256, WT <= 2 ? 4 : 1) k_batch_tile(BatchDev B, int slot_cap, int max_n, KStats* st, int quota) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   u64* T = reinterpret_cast<u64*>(smem_raw);
-  int* slot_of = reinterpret_cast<int*>(smem_raw + static_cast<size_t>(slot_cap) * 32 * WT * 8);
+  int4* nbr = reinterpret_cast<int4*>(smem_raw + static_cast<size_t>(slot_cap) * 32 * WT * 8);
+  int* slot_of = reinterpret_cast<int*>(nbr + slot_cap);
   __shared__ int s_t;
   __shared__ u32 s_fail, s_deep;
   __shared__ int s_next;
@@ -1783,7 +1831,7 @@ __global__ void __launch_bounds__(256, WT <= 2 ? 4 : 1) k_batch_tile(BatchDev B,
     const int inst = tl.x >> 16;
     tile_one<WT>(sN, B.roots[inst], B.snap ? B.snap + static_cast<size_t>(B.var_base[inst]) * WT : B.roots[inst],
                  B.weak ? B.weak + B.weak_off[inst] : nullptr, B.snap != nullptr, tl.x & 0xffff, tl.y, tl.z, static_cast<u32>(tl.w), B.ok, B.deep, B.ndeep,
-                 slot_cap, T, slot_of, s_fail, s_deep, s_next, s_rem, c_rev, c_rows, c_done);
+                 slot_cap, T, nbr, slot_of, s_fail, s_deep, s_next, s_rem, c_rev, c_rows, c_done);
   }
   flush_tile_counts(st, c_rev, c_rows, c_done);
 }
@@ -2081,7 +2129,7 @@ cudaError_t launch_sac_branches(const DevNet& N, const u64* root, const int2* wo
 }
 
 size_t sac_tile_smem(const DevNet& N, int slot_cap) {
-  return static_cast<size_t>(slot_cap) * 32 * N.W * 8 + static_cast<size_t>(N.n) * 4;
+  return static_cast<size_t>(slot_cap) * (32 * N.W * 8 + 16) + static_cast<size_t>(N.n) * 4;
 }
 
 int sac_tile_blocks_per_sm(const DevNet& N, int slot_cap, int block) {
@@ -2219,7 +2267,7 @@ cudaError_t launch_batch_weak(int W, const BatchDev& B, cudaStream_t s) {
 }
 
 size_t batch_tile_smem(int W, int slot_cap, int max_n) {
-  return static_cast<size_t>(slot_cap) * 32 * W * 8 + static_cast<size_t>(max_n) * 4;
+  return static_cast<size_t>(slot_cap) * (32 * W * 8 + 16) + static_cast<size_t>(max_n) * 4;
 }
 
 int batch_tile_blocks_per_sm(int W, int slot_cap, int max_n) {
