@@ -64,6 +64,21 @@ __device__ __forceinline__ u64 shfl64(u64 x, int src) {
   return (static_cast<u64>(hi) << 32) | lo;
 }
 
+// A domain of WT words from shared memory, 128 bits per load (16-byte aligned for WT >= 2).
+template <int WT>
+__device__ __forceinline__ void load_sh(const u64* p, u64 (&r)[WT]) {
+  if constexpr (WT == 1) {
+    r[0] = p[0];
+  } else {
+#pragma unroll
+    for (int h = 0; h < WT / 2; ++h) {
+      const ulonglong2 v = reinterpret_cast<const ulonglong2*>(p)[h];
+      r[2 * h] = v.x;
+      r[2 * h + 1] = v.y;
+    }
+  }
+}
+
 // Support rows are read-only during a launch: non-coherent 128-bit loads.
 template <int WT>
 __device__ __forceinline__ void load_row(const u64* rel, size_t off, u64 (&r)[WT]) {
@@ -1157,7 +1172,7 @@ template <int WT>
 __device__ __forceinline__ void tile_one(const DevNet& N, u64* root, const u64* snap, const u32* weak, bool gs, int x,
                                          int base, int b0,
                                          u32 live, uint8_t* ok, int* deep, int* ndeep, int slot_cap, u64* T,
-                                         int4* nbr, int* slot_of, u32& s_fail, u32& s_deep, int& s_next, int* s_rem, u64& c_rev,
+                                         int4* nbr, int* slot_of, u32& s_fail, u32& s_deep, int& s_next, int* s_rem, u32* s_msk, u64& c_rev,
                                          u64& c_rows, u64& c_done) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   {
@@ -1229,12 +1244,16 @@ __device__ __forceinline__ void tile_one(const DevNet& N, u64* root, const u64* 
       // its branches. Branches that reach past the end of an arc's list need
       // the whole arc: the warp revises such arcs together, one lane per branch.
       int* rem = s_rem + warp * 32;  // removed count of each open branch, -1 if closed
+      u32* msk = s_msk + warp * 32;  // threshold masks of the current chunk
       for (;;) {
         int item = 0;
         if (lane == 0) item = atomicAdd(&s_next, 1);
         item = __shfl_sync(kFull, item, 0);
-        const int s = item >> 1, half = item & 1;  // two items per neighbour: alternate 32-arc chunks
-        if (s >= deg) break;
+        // Two items per neighbour, alternate 32-arc chunks: every first half,
+        // then the (shorter) second halves, so a tile ends on small items.
+        if (item >= 2 * deg) break;
+        const int half = item >= deg ? 1 : 0;
+        const int s = item - half * deg;
         const int4 ny = nbr[s];
         if (ny.x < 0) continue;
         const int y0 = ny.y, y1 = ny.z;
@@ -1253,9 +1272,6 @@ __device__ __forceinline__ void tile_one(const DevNet& N, u64* root, const u64* 
           const u32 open = live & ~done_m;
           if (!open) break;
           const int r_own = ((open >> lane) & 1u) ? removed : -1;
-          __syncwarp();
-          rem[lane] = r_own;
-          __syncwarp();
           const int jl = jb + lane;
           const u32* wl = weak ? weak + static_cast<size_t>(jl) * kWeakStride : nullptr;
           Arc A{};
@@ -1271,37 +1287,43 @@ __device__ __forceinline__ void tile_one(const DevNet& N, u64* root, const u64* 
           const int c0 = static_cast<int>(wv.y >> 16);
           const u32 arcs_m = __ballot_sync(kFull, arc_in);
           if (lane == 0) c_rev += __popc(arcs_m);
-          // This lane's branches: open ones whose removed count reaches c0.
           const int cmin = __reduce_min_sync(kFull, arc_in ? c0 : 0x7fffffff);
-          u32 bm = 0;
-          for (u32 m = __ballot_sync(kFull, r_own >= cmin); m; m &= m - 1) {
-            const int b = __ffs(m) - 1;
-            const int rb = __shfl_sync(kFull, r_own, b);
-            if (arc_in && rb >= c0) bm |= 1u << b;
+          const int rtop = __reduce_max_sync(kFull, r_own);
+          if (rtop < cmin) continue;  // no open branch reaches any arc of the chunk
+          // ge(t): the open branches whose removed count is at least t, tabled
+          // for t in [cmin, cmin + 31] (no count of the chunk is below cmin).
+          __syncwarp();
+          rem[lane] = r_own;
+          const int thi = min(rtop, cmin + 31);
+          for (int t = cmin; t <= thi; ++t) {
+            const u32 mt = __ballot_sync(kFull, r_own >= t);
+            if (lane == 0) msk[t - cmin] = mt;
           }
+          __syncwarp();
+          auto ge = [&](int t) -> u32 {
+            if (t > rtop) return 0u;
+            if (t - cmin < 32) return msk[t - cmin];
+            u32 m = 0;
+            for (int b = 0; b < 32; ++b)
+              if (rem[b] >= t) m |= 1u << b;
+            return m;
+          };
           u32 fm = 0;  // branches that need this lane's arc in full
+          const u32 bm = arc_in ? ge(c0) : 0u;
           if (bm) {
-            const int cnext = static_cast<int>(wv.x >> 16);
-            u32 wm = 0;
-            int rmax = -1;  // the largest removed count among the list's branches
-            for (u32 m = bm; m; m &= m - 1) {
-              const int b = __ffs(m) - 1;
-              const int r = rem[b];
-              if (r >= cnext) {
-                fm |= 1u << b;
-              } else {
-                wm |= 1u << b;
-                rmax = max(rmax, r);
-              }
-            }
+            const u32 fmask = ge(static_cast<int>(wv.x >> 16));  // past the list's end
+            fm = bm & fmask;
+            const u32 wm = bm & ~fmask;
             if (wm) {
               // Rows of the first kPre entries in one wave of loads, with D(z).
               constexpr int kPre = WT <= 2 ? 3 : 1;
               const u32 ent[3] = {wv.y, wv.z, wv.w};
+              u32 pk[kPre];  // branches that test entry p
               u64 pre[kPre][WT];
 #pragma unroll
               for (int p = 0; p < kPre; ++p) {
-                if (static_cast<int>(ent[p] >> 16) <= rmax) {
+                pk[p] = wm & ge(static_cast<int>(ent[p] >> 16));
+                if (pk[p]) {
                   load_row<WT>(N.rel, A.zy + static_cast<size_t>(ent[p] & 0xffffu) * WT, pre[p]);
                 } else {
 #pragma unroll
@@ -1315,17 +1337,8 @@ __device__ __forceinline__ void tile_one(const DevNet& N, u64* root, const u64* 
               for (int w = 0; w < WT; ++w) cz[w] = sz < 0 ? root[static_cast<size_t>(A.z) * WT + w] : 0ull;
               u32 hitm = 0;  // branches in which some listed value of z loses every support
               u64 nrows = 0;
-              // Entry e with row r: the branches that reach its count test it.
-              // Counts increase along the list, so a branch out of reach stays so.
-              auto entry = [&](u32 e, const u64 (&r)[WT]) -> bool {
-                const int cnt = static_cast<int>(e >> 16);
-                u32 bk = 0;
-                for (u32 m = wm; m; m &= m - 1) {
-                  const int b = __ffs(m) - 1;
-                  if (rem[b] >= cnt) bk |= 1u << b;
-                }
-                wm = bk;
-                if (!bk) return false;
+              // Entry e (row r) in the branches bk that reach its count.
+              auto test = [&](u32 e, u32 bk, const u64 (&r)[WT]) {
                 ++nrows;
                 const int v = static_cast<int>(e & 0xffffu);
                 const int vw = v >> 6;
@@ -1334,23 +1347,28 @@ __device__ __forceinline__ void tile_one(const DevNet& N, u64* root, const u64* 
                 for (u32 m = bk; m; m &= m - 1) {
                   const int b = __ffs(m) - 1;
                   if (!(sz < 0 ? in_cz : (Tz[b * WT + vw] & vbit) != 0)) continue;
+                  u64 t[WT];
+                  load_sh<WT>(Ty + b * WT, t);
                   u64 hit = 0;
 #pragma unroll
-                  for (int w = 0; w < WT; ++w) hit |= r[w] & Ty[b * WT + w];
+                  for (int w = 0; w < WT; ++w) hit |= r[w] & t[w];
                   if (!hit) hitm |= 1u << b;
                 }
-                return true;
               };
-              bool more = true;
 #pragma unroll
               for (int p = 0; p < kPre; ++p)
-                if (more) more = entry(ent[p], pre[p]);
-              for (int k = kPre; more && k < kWeakK; ++k) {
-                const u32 e = __ldg(wl + 1 + k);
-                if (static_cast<int>(e >> 16) > rmax) break;
-                u64 r[WT];
-                load_row<WT>(N.rel, A.zy + static_cast<size_t>(e & 0xffffu) * WT, r);
-                more = entry(e, r);
+                if (pk[p]) test(ent[p], pk[p], pre[p]);
+              // Counts increase along the list: once an entry reaches no
+              // branch, no later one does.
+              if (pk[kPre - 1]) {
+                for (int k = kPre; k < kWeakK; ++k) {
+                  const u32 e = __ldg(wl + 1 + k);
+                  const u32 bk = wm & ge(static_cast<int>(e >> 16));
+                  if (!bk) break;
+                  u64 r[WT];
+                  load_row<WT>(N.rel, A.zy + static_cast<size_t>(e & 0xffffu) * WT, r);
+                  test(e, bk, r);
+                }
               }
               // Rare: round two removes values of z in branch b. A wipeout of
               // D_b(z) fails b, anything less hands it over.
@@ -1576,6 +1594,7 @@ __global__ void __launch_bounds__(256, WT <= 2 ? 5 : 1) k_sac_tile(DevNet N, u64
   __shared__ u32 s_fail, s_deep;
   __shared__ int s_next;
   __shared__ int s_rem[256];  // 256-thread CTAs: 32 per warp
+  __shared__ u32 s_msk[256];
   const int total = *ntiles;
   for (int i = threadIdx.x; i < N.n; i += blockDim.x) slot_of[i] = -1;
   u64 c_rev = 0, c_rows = 0, c_done = 0;
@@ -1590,7 +1609,7 @@ __global__ void __launch_bounds__(256, WT <= 2 ? 5 : 1) k_sac_tile(DevNet N, u64
     if (t >= total) break;
     const int4 tl = tiles[t];
     tile_one<WT>(N, root, snap ? snap : root, weak, snap != nullptr, tl.x, tl.y, tl.z, static_cast<u32>(tl.w), ok,
-                 deep, ndeep, slot_cap, T, nbr, slot_of, s_fail, s_deep, s_next, s_rem, c_rev, c_rows, c_done);
+                 deep, ndeep, slot_cap, T, nbr, slot_of, s_fail, s_deep, s_next, s_rem, s_msk, c_rev, c_rows, c_done);
   }
   flush_tile_counts(st, c_rev, c_rows, c_done);
 }
@@ -1813,6 +1832,7 @@ __global__ void __launch_bounds__(256, WT <= 2 ? 4 : 1) k_batch_tile(BatchDev B,
   __shared__ u32 s_fail, s_deep;
   __shared__ int s_next;
   __shared__ int s_rem[256];  // 256-thread CTAs: 32 per warp
+  __shared__ u32 s_msk[256];
   __shared__ DevNet sN;
   const int total = *B.ntiles;
   for (int i = threadIdx.x; i < max_n; i += blockDim.x) slot_of[i] = -1;
@@ -1831,7 +1851,7 @@ __global__ void __launch_bounds__(256, WT <= 2 ? 4 : 1) k_batch_tile(BatchDev B,
     const int inst = tl.x >> 16;
     tile_one<WT>(sN, B.roots[inst], B.snap ? B.snap + static_cast<size_t>(B.var_base[inst]) * WT : B.roots[inst],
                  B.weak ? B.weak + B.weak_off[inst] : nullptr, B.snap != nullptr, tl.x & 0xffff, tl.y, tl.z, static_cast<u32>(tl.w), B.ok, B.deep, B.ndeep,
-                 slot_cap, T, nbr, slot_of, s_fail, s_deep, s_next, s_rem, c_rev, c_rows, c_done);
+                 slot_cap, T, nbr, slot_of, s_fail, s_deep, s_next, s_rem, s_msk, c_rev, c_rows, c_done);
   }
   flush_tile_counts(st, c_rev, c_rows, c_done);
 }
