@@ -1397,71 +1397,69 @@ __device__ __forceinline__ void tile_one(const DevNet& N, u64* root, const u64* 
               c_rows += nrows;
             }
           }
-          // Arcs whose list does not cover some branch: the warp revises each,
-          // lane l for branch l, over the rows of the values of y that some
-          // such branch still has, 32 values per chunk, 8 rows between
-          // coverage tests; a lane ORs the rows of its own values (a
-          // predicated OR per row: the row address and the skip test are
-          // warp-uniform). Stops once every such branch's accumulated support
-          // covers its D(z).
+          // Arcs whose list does not cover some branch: the warp revises each
+          // value-wise, lane l holding the rows of the values l, l + 32, ...
+          // of z (one wave of loads), and tests them against D_b(y) of every
+          // such branch b: v in D_b(z) keeps a support iff its row meets D_b(y).
           for (u32 fullm = __ballot_sync(kFull, fm != 0); fullm; fullm &= fullm - 1) {
             const int k = __ffs(fullm) - 1;
-            const bool mine = (__shfl_sync(kFull, fm, k) >> lane) & 1u;
+            const u32 fmk = __shfl_sync(kFull, fm, k);
             const Arc Af = N.arcs[jb + k];
             const int sz = slot_of[Af.z];
-            u64 cur[WT];
+            const u64* Tz = T + static_cast<size_t>(sz < 0 ? 0 : sz) * 32 * WT;
+            u64 cz[WT], un[WT];  // D(z) if z is no neighbour of x; the values some such branch has
 #pragma unroll
-            for (int w = 0; w < WT; ++w)
-              cur[w] = sz >= 0 ? T[(static_cast<size_t>(sz) * 32 + lane) * WT + w] : root[static_cast<size_t>(Af.z) * WT + w];
-            u64 uc[WT], acc[WT];
+            for (int w = 0; w < WT; ++w) un[w] = cz[w] = sz < 0 ? root[static_cast<size_t>(Af.z) * WT + w] : 0ull;
+            if (sz >= 0) {
+              for (u32 m = fmk; m; m &= m - 1) {
+                const int b = __ffs(m) - 1;
 #pragma unroll
-            for (int w = 0; w < WT; ++w) {
-              uc[w] = warp_or64(mine ? dy[w] : 0ull);
-              acc[w] = 0;
+                for (int w = 0; w < WT; ++w) un[w] |= Tz[b * WT + w];
+              }
             }
+            u32 stillm = 0, leftm = 0;  // branches with an unsupported / a supported value of z
             int loaded = 0;
-            bool go = true;
+            constexpr int kG = WT <= 2 ? 2 * WT : 2;  // rows in flight per lane
 #pragma unroll
-            for (int h = 0; h < 2 * WT; ++h) {
-              const u32 ucw = static_cast<u32>(sel<WT>(uc, h >> 1) >> ((h & 1) * 32));
-              const u32 myb = mine ? static_cast<u32>(sel<WT>(dy, h >> 1) >> ((h & 1) * 32)) : 0u;
-              if (ucw == 0) continue;
-              const u64* rc = N.rel + Af.yz + static_cast<size_t>(h) * 32 * WT;
+            for (int h0 = 0; h0 < 2 * WT; h0 += kG) {
+              u64 r[kG][WT];
+              bool need[kG];
 #pragma unroll
-              for (int j0 = 0; j0 < 32; j0 += 8) {
-                const u32 chunk = (ucw >> j0) & 0xffu;
-                if (!go || chunk == 0) continue;
+              for (int g = 0; g < kG; ++g) {
+                const int h = h0 + g;
+                need[g] = (sel<WT>(un, h >> 1) >> ((h & 1) * 32 + lane)) & 1ull;
+                if (need[g]) {
+                  load_row<WT>(N.rel, Af.zy + static_cast<size_t>(h * 32 + lane) * WT, r[g]);
+                } else {
 #pragma unroll
-                for (int jj = 0; jj < 8; ++jj) {
-                  if ((chunk >> jj) & 1u) {
-                    u64 r[WT];
-                    load_row<WT>(rc, static_cast<size_t>(j0 + jj) * WT, r);
-                    ++loaded;
-                    if ((myb >> (j0 + jj)) & 1u) {
-#pragma unroll
-                      for (int q = 0; q < WT; ++q) acc[q] |= r[q];
-                    }
-                  }
+                  for (int w = 0; w < WT; ++w) r[g][w] = 0;
                 }
-                u64 gap = 0;
+                loaded += __popc(__ballot_sync(kFull, need[g]));
+              }
+              for (u32 m = fmk; m; m &= m - 1) {
+                const int b = __ffs(m) - 1;
+                u64 t[WT];
+                load_sh<WT>(Ty + b * WT, t);
 #pragma unroll
-                for (int q = 0; q < WT; ++q) gap |= cur[q] & ~acc[q];
-                if (__ballot_sync(kFull, mine && gap != 0) == 0) go = false;  // every such branch covered
+                for (int g = 0; g < kG; ++g) {
+                  const int h = h0 + g;
+                  const u64 curw = sz < 0 ? sel<WT>(cz, h >> 1) : Tz[b * WT + (h >> 1)];
+                  const bool vin = (curw >> ((h & 1) * 32 + lane)) & 1ull;
+                  u64 hit = 0;
+#pragma unroll
+                  for (int w = 0; w < WT; ++w) hit |= r[g][w] & t[w];
+                  if (__ballot_sync(kFull, vin && hit == 0)) stillm |= 1u << b;
+                  if (__ballot_sync(kFull, vin && hit != 0)) leftm |= 1u << b;
+                }
               }
             }
-            bool still = false, left = false;
-            if (go) {
-              u64 gap = 0, kept = 0;
-#pragma unroll
-              for (int q = 0; q < WT; ++q) {
-                gap |= cur[q] & ~acc[q];
-                kept |= cur[q] & acc[q];
+            if (lane == 0) {
+              c_rows += loaded;
+              for (u32 m = stillm; m; m &= m - 1) {
+                const int b = __ffs(m) - 1;
+                atomicOr(((leftm >> b) & 1u) ? &s_deep : &s_fail, 1u << b);
               }
-              still = mine && gap != 0;
-              left = kept != 0;
             }
-            if (lane == 0) c_rows += loaded;
-            if (still) atomicOr(left ? &s_deep : &s_fail, 1u << lane);
           }
         }
       }
