@@ -88,6 +88,7 @@ def lib():
         "cp_engine_launches": ([vp], i64),
         "cp_engine_set_tuning": ([vp, i, i, i], i),
         "cp_engine_set_sac_mode": ([vp, i], i),
+        "cp_engine_set_graphs": ([vp, i], i),
         "cp_net_upload": ([vp, i, PI, i, P64, i, PI, P64, i, PI, PI, PI, PI, i, PV], i),
         "cp_net_destroy": ([vp], i),
         "cp_net_device_bytes": ([vp], i64),
@@ -284,6 +285,10 @@ class Engine:
     def set_sac_mode(self, mode: int):
         """0: tiled SAC sweep where eligible; 1: general per-branch kernel only."""
         _check(lib().cp_engine_set_sac_mode(self._h, mode))
+
+    def set_graphs(self, on: bool):
+        """SAC1 rounds of single networks as CUDA graph replays (default) or direct launches."""
+        _check(lib().cp_engine_set_graphs(self._h, 1 if on else 0))
 
     def upload(self, inst: Instance, max_levels: int = 0) -> "Net":
         return Net(self, inst, max_levels)

@@ -5,6 +5,7 @@
 #include <sys/stat.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <chrono>
 #include <cstdio>
@@ -75,6 +76,7 @@ struct cp_engine {
   int chunk = 0;
   int ctas_per_sm = 0;
   int sac_mode = 0;  // 0: tiled sweep where eligible, 1: general kernel only
+  bool sac_graphs = true;  // single-network SAC1 rounds replayed as CUDA graphs
   int cta_quota = 0;  // batch sweep CTAs retire after this many units (0: persistent)
   int search_mode = 0;  // 0: MAC searches run on the device where they fit one CTA; 1: host-driven nodes
   long long wait_ns = 2000000000ll;  // longest grid-barrier wait of a block (then CP_E_TIMEOUT)
@@ -225,8 +227,22 @@ struct cp_net {
 
   void* h_block = nullptr;  // pinned block holding h_stats, h_dom, h_sizes
   size_t h_block_bytes = 0;
+  // SAC1 rounds captured as CUDA graphs: [0] root AC + sweep, [1] events AC +
+  // sweep; valid for the level and knobs in sac_key.
+  cudaGraphExec_t sac_exec[2] = {nullptr, nullptr};
+  int sac_launches[2] = {0, 0};
+  std::array<int64_t, 10> sac_key{};
+  bool sac_graph_off = false;  // capture failed once: rounds run uncaptured
+
+  void drop_sac_graphs() {
+    for (auto& x : sac_exec) {
+      if (x) cudaGraphExecDestroy(x);
+      x = nullptr;
+    }
+  }
 
   ~cp_net() {
+    drop_sac_graphs();
     if (e) {
       for (void* p : allocs) e->dev_free(p);
       e->pinned_put(h_block, h_block_bytes);
@@ -264,26 +280,6 @@ int stats_begin(cp_net* net) {
   z.fail_var = -1;
   *net->h_stats = z;
   CP_CUDA(cudaMemcpyAsync(net->d_stats, net->h_stats, sizeof(KStats), cudaMemcpyHostToDevice, net->e->stream));
-  return CP_OK;
-}
-
-// Both stats slots: zeroed together, fetched together (one sync).
-int stats_begin2(cp_net* net) {
-  KStats z{};
-  z.fail_var = -1;
-  net->h_stats[0] = z;
-  net->h_stats[1] = z;
-  CP_CUDA(cudaMemcpyAsync(net->d_stats, net->h_stats, 2 * sizeof(KStats), cudaMemcpyHostToDevice, net->e->stream));
-  return CP_OK;
-}
-
-int stats_fetch2(cp_net* net) {
-  CP_CUDA(cudaMemcpyAsync(net->h_stats, net->d_stats, 2 * sizeof(KStats), cudaMemcpyDeviceToHost, net->e->stream));
-  CP_CUDA(cudaStreamSynchronize(net->e->stream));
-  for (int i = 0; i < 2; ++i) {
-    if (net->h_stats[i].grid_err) return fail(CP_E_TIMEOUT, "device grid barrier wait ran out");
-    if (net->h_stats[i].error) return fail(net->h_stats[i].error, "device-side check failed (round limit)");
-  }
   return CP_OK;
 }
 
@@ -460,6 +456,12 @@ int cp_engine_set_sac_mode(cp_engine* e, int mode) {
   if (!e) return fail(CP_E_ARG, "null engine");
   if (mode != 0 && mode != 1) return fail(CP_E_ARG, "SAC mode must be 0 (tiled where eligible) or 1 (general)");
   e->sac_mode = mode;
+  return CP_OK;
+}
+
+int cp_engine_set_graphs(cp_engine* e, int use_graphs) {
+  if (!e) return fail(CP_E_ARG, "null engine");
+  e->sac_graphs = use_graphs != 0;
   return CP_OK;
 }
 
@@ -721,13 +723,17 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   CP_TRY(net->alloc(&net->d_sizes, n));
   CP_TRY(net->alloc(&net->d_ok1, total_values));
   {
-    static_assert(2 * sizeof(KStats) <= 256, "two stats slots in the pinned block");
-    const size_t st_bytes = 256;
+    static_assert(4 * sizeof(KStats) <= 512, "four stats slots in the pinned block");
+    const size_t st_bytes = 512;  // two fetched slots, then two reset values
     const size_t dom_bytes = (static_cast<size_t>(n) * Wi * 8 + 255) & ~size_t(255);
     net->h_block_bytes = st_bytes + dom_bytes + static_cast<size_t>(n) * sizeof(int);
     CP_TRY(e->pinned_get(net->h_block_bytes, &net->h_block));
     char* hb = static_cast<char*>(net->h_block);
     net->h_stats = reinterpret_cast<KStats*>(hb);
+    KStats z{};
+    z.fail_var = -1;
+    net->h_stats[2] = z;  // constant: the source of every captured stats reset
+    net->h_stats[3] = z;
     net->h_dom = reinterpret_cast<u64*>(hb + st_bytes);
     net->h_sizes = reinterpret_cast<int*>(hb + st_bytes + dom_bytes);
   }
@@ -935,6 +941,131 @@ int cp_enforce_ac(cp_net* net, int level, int n_evt, const int* evt, cp_stats* s
   return CP_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// One SAC1 round on the engine stream: both stats slots reset, the level AC
+// into slot 1 (the root AC, SAC1::enforce src/SAC1.cpp:58, or the AC of the
+// previous commit's removals, :85-92), then one sweep into slot 0, then both
+// slots copied to the pinned mirror. Nothing waits on the host, except the
+// events AC of a network without the grid path, which reads the event count
+// first. A sweep queued behind an AC that wiped a domain out only wastes its
+// work; its results are not used.
+int sac_round_launches(cp_net* net, int level, bool root, int& launches, bool captured) {
+  cp_engine* e = net->e;
+  cudaStream_t s = e->stream;
+  // Kernel-time events: external records become event nodes of a captured round.
+  const unsigned evf = captured ? cudaEventRecordExternal : cudaEventRecordDefault;
+  CP_CUDA(cudaMemcpyAsync(net->d_stats, net->h_stats + 2, 2 * sizeof(KStats), cudaMemcpyHostToDevice, s));
+  if (root) {
+    CP_TRY(run_ac(net, level, nullptr, 0, launches, net->d_stats + 1));
+  } else if (net->prefer_grid) {
+    CP_TRY(run_ac(net, level, net->S.evt, 0, launches, net->d_stats + 1, net->S.nevt));
+  } else {
+    CP_CUDA(cudaMemcpyAsync(&net->h_sizes[0], net->S.nevt, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CP_CUDA(cudaStreamSynchronize(s));
+    CP_TRY(run_ac(net, level, net->S.evt, net->h_sizes[0], launches, net->d_stats + 1));
+  }
+  const size_t nw = (static_cast<size_t>(net->n) + 31) / 32;
+  CP_CUDA(cudaMemsetAsync(net->S.nwork, 0, 6 * sizeof(int), s));  // nwork .. ndeep
+  CP_CUDA(cudaMemsetAsync(net->S.evt_fb, 0, nw * 4, s));
+  const bool tiled = net->tile_grid > 0 && e->sac_mode == 0;
+  SacScratch S = net->S;
+  if (!tiled) S.tiles = nullptr;
+  CP_CUDA(launch_build_work(net->dn, net->level_ptr(level), S, s));
+  CP_CUDA(cudaEventRecordWithFlags(e->evk0, s, evf));
+  // Mode 0: failed branches remove their value from the level at once
+  // (later branches of the sweep start without it; the closure is the
+  // same, since a wipe-out on a larger domain implies one on a smaller);
+  // mode 1 keeps the plain Jacobi sweep as the reference path.
+  u64* gs_root = e->sac_mode == 0 ? net->level_ptr(level) : nullptr;
+  if (tiled) {
+    // Two-round branches resolved by the tiled kernel, the rest (the deep
+    // list) by the general kernel; the sweep-start domains and the
+    // weak-support lists counted against them come first.
+    CP_CUDA(cudaMemcpyAsync(S.snap, net->level_ptr(level), static_cast<size_t>(net->n) * net->W * 8,
+                            cudaMemcpyDeviceToDevice, s));
+    if (S.weak) {
+      CP_CUDA(launch_weak(net->dn, S.snap, S.weak, s));
+      launches += 1;
+      e->launches += 1;
+    }
+    CP_CUDA(launch_sac_tile(net->dn, net->level_ptr(level), S, S.ok, net->slot_cap, net->d_stats, kTileBlock,
+                            net->tile_grid, s));
+    CP_CUDA(launch_sac_branches(net->dn, net->level_ptr(level), S.work, S.nwork, S.cursor, S.ok, net->d_stats,
+                                e->block_sac, net->sac_grid, net->d_sac_scratch, net->sac_stride, s, S.deep,
+                                S.ndeep, gs_root));
+    launches += 1;
+    e->launches += 1;
+  } else {
+    CP_CUDA(launch_sac_branches(net->dn, net->level_ptr(level), S.work, S.nwork, S.cursor, S.ok, net->d_stats,
+                                e->block_sac, net->sac_grid, net->d_sac_scratch, net->sac_stride, s, nullptr,
+                                nullptr, gs_root));
+  }
+  CP_CUDA(cudaEventRecordWithFlags(e->evk1, s, evf));
+  CP_CUDA(launch_commit(net->dn, net->level_ptr(level), S, net->d_stats, s));
+  launches += 3;
+  e->launches += 3;
+  CP_CUDA(cudaMemcpyAsync(net->h_stats, net->d_stats, 2 * sizeof(KStats), cudaMemcpyDeviceToHost, s));
+  return CP_OK;
+}
+
+// A round as one graph launch: captured on first use for this level and
+// these knobs, replayed afterwards (the host's launch cost of a dozen
+// operations becomes one). Rounds that must read a count on the host, and
+// networks whose round cannot be captured, run uncaptured.
+int sac_round(cp_net* net, int level, bool root, int& launches) {
+  cp_engine* e = net->e;
+  cudaStream_t s = e->stream;
+  if (!e->sac_graphs || net->sac_graph_off || !(root || net->prefer_grid))
+    return sac_round_launches(net, level, root, launches, false);
+  const std::array<int64_t, 10> key = {level, e->sac_mode, e->block_sac, e->block_grid, e->block_node,
+                                       net->sac_grid, net->tile_grid, net->slot_cap, net->grid_blocks, e->wait_ns};
+  if (key != net->sac_key) {
+    net->drop_sac_graphs();
+    net->sac_key = key;
+  }
+  const int k = root ? 0 : 1;
+  if (!net->sac_exec[k]) {
+    cudaGraph_t graph = nullptr;
+    CP_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    const int64_t l0 = e->launches;
+    int cnt = 0;
+    const int rc = sac_round_launches(net, level, root, cnt, true);
+    e->launches = l0;
+    const cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    cudaError_t ie = cudaErrorUnknown;
+    if (rc == CP_OK && ce == cudaSuccess && graph) ie = cudaGraphInstantiate(&net->sac_exec[k], graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) {
+      cudaGetLastError();
+      net->sac_exec[k] = nullptr;
+      net->sac_graph_off = true;
+      return sac_round_launches(net, level, root, launches, false);
+    }
+    net->sac_launches[k] = cnt;
+  }
+  CP_CUDA(cudaGraphLaunch(net->sac_exec[k], s));
+  launches += net->sac_launches[k];
+  e->launches += net->sac_launches[k];
+  return CP_OK;
+}
+
+// Waits for the round's stats copy and checks the device-side error flags.
+int sac_round_wait(cp_net* net) {
+  CP_CUDA(cudaStreamSynchronize(net->e->stream));
+  for (int i = 0; i < 2; ++i) {
+    if (net->h_stats[i].grid_err) return fail(CP_E_TIMEOUT, "device grid barrier wait ran out");
+    if (net->h_stats[i].error) return fail(net->h_stats[i].error, "device-side check failed (round limit)");
+  }
+  return CP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int cp_enforce_sac1(cp_net* net, int level, cp_stats* st) {
   if (!net) return fail(CP_E_ARG, "null net");
   CP_TRY(check_level(net, level));
@@ -943,59 +1074,13 @@ int cp_enforce_sac1(cp_net* net, int level, cp_stats* st) {
   Acc acc;
   int launches = 0;
   CP_CUDA(cudaEventRecord(e->ev0, s));
-  // Each sweep is queued behind the level AC that precedes it (the root AC,
-  // SAC1::enforce src/SAC1.cpp:58, then the AC of the previous commit's
-  // removals, :85-92) with no host sync in between: the AC writes stats slot
-  // 1, the sweep slot 0, and one fetch reads both. A sweep queued behind an
-  // AC that wiped a domain out only wastes its work; its results are not used.
-  CP_TRY(stats_begin2(net));
-  CP_TRY(run_ac(net, level, nullptr, 0, launches, net->d_stats + 1));
   bool inconsistent = false;
   int sweeps = 0;
   double kernel_ms = 0, kernel_bytes = 0;
-  const size_t nw = (static_cast<size_t>(net->n) + 31) / 32;
-  for (;;) {
+  for (bool root = true;; root = false) {
     ++sweeps;
-    CP_CUDA(cudaMemsetAsync(net->S.nwork, 0, 6 * sizeof(int), s));  // nwork .. ndeep
-    CP_CUDA(cudaMemsetAsync(net->S.evt_fb, 0, nw * 4, s));
-    const bool tiled = net->tile_grid > 0 && e->sac_mode == 0;
-    SacScratch S = net->S;
-    if (!tiled) S.tiles = nullptr;
-    CP_CUDA(launch_build_work(net->dn, net->level_ptr(level), S, s));
-    CP_CUDA(cudaEventRecord(e->evk0, s));
-    // Mode 0: failed branches remove their value from the level at once
-    // (later branches of the sweep start without it; the closure is the
-    // same, since a wipe-out on a larger domain implies one on a smaller);
-    // mode 1 keeps the plain Jacobi sweep as the reference path.
-    u64* gs_root = e->sac_mode == 0 ? net->level_ptr(level) : nullptr;
-    if (tiled) {
-      // Two-round branches resolved by the tiled kernel, the rest (the deep
-      // list) by the general kernel; the sweep-start domains and the
-      // weak-support lists counted against them come first.
-      CP_CUDA(cudaMemcpyAsync(S.snap, net->level_ptr(level), static_cast<size_t>(net->n) * net->W * 8,
-                              cudaMemcpyDeviceToDevice, s));
-      if (S.weak) {
-        CP_CUDA(launch_weak(net->dn, S.snap, S.weak, s));
-        launches += 1;
-        e->launches += 1;
-      }
-      CP_CUDA(launch_sac_tile(net->dn, net->level_ptr(level), S, S.ok, net->slot_cap, net->d_stats, kTileBlock,
-                              net->tile_grid, s));
-      CP_CUDA(launch_sac_branches(net->dn, net->level_ptr(level), S.work, S.nwork, S.cursor, S.ok, net->d_stats,
-                                  e->block_sac, net->sac_grid, net->d_sac_scratch, net->sac_stride, s, S.deep,
-                                  S.ndeep, gs_root));
-      launches += 1;
-      e->launches += 1;
-    } else {
-      CP_CUDA(launch_sac_branches(net->dn, net->level_ptr(level), S.work, S.nwork, S.cursor, S.ok, net->d_stats,
-                                  e->block_sac, net->sac_grid, net->d_sac_scratch, net->sac_stride, s, nullptr,
-                                  nullptr, gs_root));
-    }
-    CP_CUDA(cudaEventRecord(e->evk1, s));
-    CP_CUDA(launch_commit(net->dn, net->level_ptr(level), S, net->d_stats, s));
-    launches += 3;
-    e->launches += 3;
-    CP_TRY(stats_fetch2(net));
+    CP_TRY(sac_round(net, level, root, launches));
+    CP_TRY(sac_round_wait(net));
     acc.add(net->h_stats[1], 0);  // the level AC before this sweep
     if (net->h_stats[1].inconsistent) {
       inconsistent = true;
@@ -1012,7 +1097,7 @@ int cp_enforce_sac1(cp_net* net, int level, cp_stats* st) {
     }
     {
       float kms = 0;
-      cudaEventElapsedTime(&kms, e->evk0, e->evk1);
+      CP_CUDA(cudaEventElapsedTime(&kms, e->evk0, e->evk1));
       kernel_ms += kms;
       Acc ka;
       KStats kk = k;
@@ -1021,16 +1106,6 @@ int cp_enforce_sac1(cp_net* net, int level, cp_stats* st) {
       kernel_bytes += alg_bytes(net, ka, static_cast<int64_t>(k.branches));
     }
     if (k.removed == 0) break;
-    // Propagate the removals at the level (SAC1.cpp:85-92, batched) ahead of
-    // the next sweep; the grid path reads the event count on the device.
-    CP_TRY(stats_begin2(net));
-    if (net->prefer_grid) {
-      CP_TRY(run_ac(net, level, net->S.evt, 0, launches, net->d_stats + 1, net->S.nevt));
-    } else {
-      CP_CUDA(cudaMemcpyAsync(&net->h_sizes[0], net->S.nevt, sizeof(int), cudaMemcpyDeviceToHost, s));
-      CP_CUDA(cudaStreamSynchronize(s));
-      CP_TRY(run_ac(net, level, net->S.evt, net->h_sizes[0], launches, net->d_stats + 1));
-    }
   }
   CP_CUDA(cudaEventRecord(e->ev1, s));
   CP_CUDA(cudaEventSynchronize(e->ev1));

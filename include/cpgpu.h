@@ -82,6 +82,10 @@ int cp_engine_set_tuning(cp_engine* e, int block, int chunk, int ctas_per_sm);
  * test, deeper branches re-run by the general kernel) wherever the network is
  * binary and fits, 1 = general per-branch kernel only. Results are identical. */
 int cp_engine_set_sac_mode(cp_engine* e, int mode);
+/* Single-network SAC1 (cp_enforce_sac1): 1 (default) replays each round (level
+ * AC + sweep) as a CUDA graph captured on first use per level, 0 launches its
+ * operations one by one. Results are identical. */
+int cp_engine_set_graphs(cp_engine* e, int use_graphs);
 /* Stream priority of the engine (-1 low, 0 default, 1 high); only before the
  * first network is uploaded. CTAs of a high-priority stream are scheduled
  * first whenever SM resources free up. */

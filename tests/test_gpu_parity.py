@@ -260,3 +260,28 @@ def test_sac_tiled_with_repeated_pairs(p):
                 assert np.array_equal(net.dom_get(0), d_o), mode
                 assert st.deletions == dels_o, mode
             net.close()
+
+
+@pytest.mark.parametrize("args", [(500, 12, 4500, 0.5, 0.5, 0.0, 1), (500, 12, 4500, 0.51, 0.51, 0.0, 1),
+                                  (100, 128, 1000, 0.4, 0.4, 0.0, 7), (40, 70, 200, 0.88, 0.88, 0.0, 4)])
+def test_sac_graph_rounds_equal_direct(args):
+    # SAC1 rounds replayed as CUDA graphs (the root-AC round and the
+    # events-AC round, captured per level) give the oracle's closure, as the
+    # uncaptured launches do, across levels and repeated calls. The first two
+    # networks take the grid AC path and need several sweeps (the second ends
+    # in a wipe-out).
+    inst = cp.gen_binary(*args)
+    ok_o, d_o, dels_o = O.sac1(oracle_view_of(inst))
+    for graphs in (True, False):
+        with cp.Engine(0) as eng:
+            eng.set_graphs(graphs)
+            net = eng.upload(inst, max_levels=3)
+            for _ in range(2):
+                for level in (0, 1):
+                    net.dom_set(level, inst.init)
+                    st = net.enforce_sac1(level)
+                    assert bool(st.inconsistent) == (not ok_o), (graphs, level)
+                    if ok_o:
+                        assert np.array_equal(net.dom_get(level), d_o), (graphs, level)
+                        assert st.deletions == dels_o, (graphs, level)
+            net.close()
