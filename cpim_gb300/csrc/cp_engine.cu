@@ -324,12 +324,9 @@ int run_ac(cp_net* net, int level, const int* evt_dev, int nevt, int& launches, 
   if (!st) st = net->d_stats;
   if (net->prefer_grid) {
     cudaStream_t s = e->stream;
-    CP_CUDA(cudaMemsetAsync(net->G.qlen, 0, 3 * sizeof(int), s));
-    CP_CUDA(cudaMemsetAsync(net->G.failed, 0, 2 * sizeof(int), s));
-    CP_CUDA(cudaMemsetAsync(net->G.bar, 0, 2 * sizeof(unsigned), s));
+    CP_CUDA(cudaMemsetAsync(net->G.qlen, 0, 12 * sizeof(int), s));  // qlen, failed, bar
     const size_t nw = (static_cast<size_t>(net->n) + 31) / 32;
-    CP_CUDA(cudaMemsetAsync(net->G.fb[0], 0, nw * 4, s));
-    CP_CUDA(cudaMemsetAsync(net->G.fb[1], 0, nw * 4, s));
+    CP_CUDA(cudaMemsetAsync(net->G.fb[0], 0, 2 * nw * 4, s));  // both bitmaps
     net->G.wait_ns = e->wait_ns;
     CP_CUDA(launch_ac_grid(net->dn, net->level_ptr(level), evt_dev, nevt_dev, evt_dev ? nevt : 0, net->G, st,
                            e->block_grid, net->grid_blocks, s));
@@ -625,6 +622,9 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   int64_t max_items = 0;
   for (int x = 0; x < n; ++x) max_items += std::max(1, (arc_deg[x] + tab_deg[x] + chunk - 1) / chunk);
   if (max_items >= (int64_t(1) << 31)) return fail(CP_E_UNSUPPORTED, "too many work items");
+  // Queue offsets of every variable's items when all are seeded (root AC).
+  std::vector<int> root_base(n + 1, 0);
+  for (int x = 0; x < n; ++x) root_base[x + 1] = root_base[x] + std::max(1, (arc_deg[x] + tab_deg[x] + chunk - 1) / chunk);
   int64_t total_values = 0;
   for (int x = 0; x < n; ++x) total_values += dom[x];
 
@@ -658,6 +658,8 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   mp.add(&d_tnt, t_ntup.data(), n_tab);
   mp.add(&d_toff, t_off.data(), n_tab);
   mp.add(&d_ttup, t_tup.data(), t_tup.size());
+  int* d_root_base;
+  mp.add(&d_root_base, root_base.data(), n + 1);
   mp.add(&net->d_bx, net->bx.data(), n_bin);
   mp.add(&net->d_by, net->by.data(), n_bin);
   mp.add(&net->d_offA, offA.data(), n_bin);
@@ -684,19 +686,24 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   D.t_ntup = d_tnt;
   D.t_off = d_toff;
   D.t_tup = d_ttup;
+  net->G.root_base = d_root_base;
 
   // Scratch.
   const size_t nw = (static_cast<size_t>(n) + 31) / 32;
   GridScratch& G = net->G;
   CP_TRY(net->alloc(&G.q[0], max_items));
   CP_TRY(net->alloc(&G.q[1], max_items));
-  CP_TRY(net->alloc(&G.fb[0], nw));
-  CP_TRY(net->alloc(&G.fb[1], nw));
-  CP_TRY(net->alloc(&G.qlen, 4));
+  CP_TRY(net->alloc(&G.fb[0], 2 * nw));  // both bitmaps: cleared by one memset
+  G.fb[1] = G.fb[0] + nw;
+  {
+    int* ctl;  // qlen[4] | failed[2] + pad | bar[2]: cleared by one memset
+    CP_TRY(net->alloc(&ctl, 12));
+    G.qlen = ctl;
+    G.failed = ctl + 4;
+    G.bar = reinterpret_cast<unsigned*>(ctl + 8);
+  }
   CP_TRY(net->alloc(&G.tstamp, std::max(1, n_tab)));
   CP_TRY(net->alloc(&G.epoch, 4));
-  CP_TRY(net->alloc(&G.failed, 4));
-  CP_TRY(net->alloc(&G.bar, 4));
   CP_CUDA(cudaMemsetAsync(G.tstamp, 0, std::max(1, n_tab) * sizeof(int), s));
   CP_CUDA(cudaMemsetAsync(G.epoch, 0, 4 * sizeof(int), s));
   SacScratch& S = net->S;

@@ -83,8 +83,9 @@ struct KStats {
 // Global-memory state of the grid-wide fixpoint (one per network).
 struct GridScratch {
   u32* q[2];          // work queues, max_items each
-  u32* fb[2];         // dedupe bitmaps, ceil(n/32) words each
-  int* qlen;          // [3] rotating queue lengths
+  u32* fb[2];         // dedupe bitmaps, ceil(n/32) words each (one block)
+  const int* root_base;  // [n+1] first work item of each variable when all are seeded
+  int* qlen;          // [3] rotating queue lengths; qlen, failed, bar share one block
   int* tstamp;        // [nt] round stamp of the last table revision
   int* epoch;         // [1] stamp base carried across calls
   int* failed;        // [1]

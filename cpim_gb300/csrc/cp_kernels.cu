@@ -204,20 +204,18 @@ __device__ __forceinline__ void commit(const DevNet& N, const Fix& F, u32* qn, u
   }
 }
 
+// Revises z against y along arc A; dy / cy: D(y) and its size, read by the
+// caller once per work item.
 template <int WT, bool kGlobal>
 __device__ __forceinline__ void revise_arc(const DevNet& N, const Fix& F, u32* qn, u32* fbn, int* qlenn, int slot,
-                                           int y, const Arc A, Cnt& cn) {
+                                           int y, const u64 (&dy)[WT], int cy, const Arc A, Cnt& cn) {
   const int lane = threadIdx.x & 31;
   const int z = A.z;
-  u64 dy[WT], dz[WT];
-  load_dom_uniform<WT>(F.D + static_cast<size_t>(y) * WT, dy);
+  u64 dz[WT];
   load_dom_uniform<WT>(F.D + static_cast<size_t>(z) * WT, dz);
-  int cy = 0, cz = 0;
+  int cz = 0;
 #pragma unroll
-  for (int w = 0; w < WT; ++w) {
-    cy += __popcll(dy[w]);
-    cz += __popcll(dz[w]);
-  }
+  for (int w = 0; w < WT; ++w) cz += __popcll(dz[w]);
   if (lane == 0) ++cn.rev;
   if (cy == 0 || cz == 0) {
     if (lane == 0) set_failed(F, slot, cy == 0 ? y : z);
@@ -258,22 +256,33 @@ __device__ __forceinline__ void revise_arc(const DevNet& N, const Fix& F, u32* q
     for (int w = 0; w < WT; ++w) rm[w] = dz[w] & ~cov[w];
     if (lane == 0) cn.rows += loaded;
   } else {
-    // Every live value of z tests its support row against D(y).
+    // Every live value of z tests its support row against D(y); the rows of
+    // kVG groups of 32 values are loaded before any is tested.
+    constexpr int kVG = WT <= 2 ? 2 * WT : (WT == 4 ? 4 : 2);
 #pragma unroll
-    for (int base = 0; base < 64 * WT; base += 32) {
-      const u32 bits = static_cast<u32>(dz[base >> 6] >> (base & 32));
-      if (bits == 0) continue;
-      bool unsup = false;
-      if ((bits >> lane) & 1u) {
-        u64 r[WT];
-        load_row<WT>(N.rel, A.zy + static_cast<size_t>(base + lane) * WT, r);
+    for (int g0 = 0; g0 < 2 * WT; g0 += kVG) {
+      u64 r[kVG][WT];
+      bool live[kVG];
+#pragma unroll
+      for (int g = 0; g < kVG; ++g) {
+        const int base = (g0 + g) * 32;
+        live[g] = (dz[base >> 6] >> ((base & 32) + lane)) & 1ull;
+        if (live[g]) {
+          load_row<WT>(N.rel, A.zy + static_cast<size_t>(base + lane) * WT, r[g]);
+        } else {
+#pragma unroll
+          for (int w = 0; w < WT; ++w) r[g][w] = 0;
+        }
+      }
+#pragma unroll
+      for (int g = 0; g < kVG; ++g) {
+        const int base = (g0 + g) * 32;
         u64 hit = 0;
 #pragma unroll
-        for (int w = 0; w < WT; ++w) hit |= r[w] & dy[w];
-        unsup = hit == 0;
+        for (int w = 0; w < WT; ++w) hit |= r[g][w] & dy[w];
+        const u32 m = __ballot_sync(kFull, live[g] && hit == 0);
+        rm[base >> 6] |= static_cast<u64>(m) << (base & 32);
       }
-      const u32 m = __ballot_sync(kFull, unsup);
-      rm[base >> 6] |= static_cast<u64>(m) << (base & 32);
     }
     if (lane == 0) cn.rows += cz;
   }
@@ -361,12 +370,27 @@ __device__ __forceinline__ void process_item(const DevNet& N, const Fix& F, u32 
   const int t0 = N.tinc_start[y], dt = N.tinc_start[y + 1] - t0;
   const int lo = c * N.chunk;
   const int hi = min(lo + N.chunk, da + dt);
+  const int hb = min(hi, da);  // binary arcs of this item: [lo, hb)
+  // D(y) once per item: these revisions change other variables only (a
+  // change of D(y) by another warp queues y again). The next arc's record is
+  // read while the current one is revised.
+  u64 dy[WT];
+  int cy = 0;
+  Arc nxt{};
+  if (lo < hb) {
+    load_dom_uniform<WT>(F.D + static_cast<size_t>(y) * WT, dy);
+#pragma unroll
+    for (int w = 0; w < WT; ++w) cy += __popcll(dy[w]);
+    nxt = N.arcs[a0 + lo];
+  }
   for (int i = lo; i < hi; ++i) {
-    if (any_failed(F)) return;
     if (i < da) {
-      const Arc A = N.arcs[a0 + i];
-      revise_arc<WT, kGlobal>(N, F, qn, fbn, qlenn, slot, y, A, cn);
+      const Arc A = nxt;
+      if (i + 1 < hb) nxt = N.arcs[a0 + i + 1];
+      if (any_failed(F)) return;
+      revise_arc<WT, kGlobal>(N, F, qn, fbn, qlenn, slot, y, dy, cy, A, cn);
     } else if constexpr (kTab) {
+      if (any_failed(F)) return;
       const int t = N.vtab[t0 + i - da];
       int prev = 0;
       if (lane == 0) prev = atomicMax(F.tstamp + t, stamp);
@@ -1076,8 +1100,22 @@ __global__ void __launch_bounds__(512) k_ac_grid(DevNet N, u64* D, const int* ev
   const unsigned nblocks = gridDim.x;
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const int gthreads = gridDim.x * blockDim.x;
-  const int ne = evt ? (nevt_dev ? vloadi(nevt_dev) : nevt) : N.n;
-  for (int i = gtid; i < ne; i += gthreads) seed_var<WT>(N, F, evt ? evt[i] : i);
+  if (evt) {
+    const int ne = nevt_dev ? vloadi(nevt_dev) : nevt;
+    for (int i = gtid; i < ne; i += gthreads) seed_var<WT>(N, F, evt[i]);
+  } else {
+    // Root: every variable, its items written at precomputed queue offsets
+    // (no appends); an empty domain is a wipe-out.
+    for (int z = gtid; z < N.n; z += gthreads) {
+      u64 any = 0;
+#pragma unroll
+      for (int w = 0; w < WT; ++w) any |= vload(F.D + static_cast<size_t>(z) * WT + w);
+      if (!any) set_failed(F, 0, z);
+      const int b0 = G.root_base[z], nch = G.root_base[z + 1] - b0;
+      for (int c = 0; c < nch; ++c) F.q0[b0 + c] = (static_cast<u32>(z) << kItemVarShift) | static_cast<u32>(c);
+    }
+    if (gtid == 0) F.qlen[0] = G.root_base[N.n];
+  }
   int* err = &st->grid_err;
   Cnt cn;
   const long long max_rounds = N.total_values + 2;
