@@ -256,16 +256,17 @@ __device__ __forceinline__ void revise_arc(const DevNet& N, const Fix& F, u32* q
     for (int w = 0; w < WT; ++w) rm[w] = dz[w] & ~cov[w];
     if (lane == 0) cn.rows += loaded;
   } else {
-    // Every live value of z tests its support row against D(y); the rows of
-    // kVG groups of 32 values are loaded before any is tested.
-    constexpr int kVG = WT <= 2 ? 2 * WT : (WT == 4 ? 4 : 2);
-#pragma unroll
-    for (int g0 = 0; g0 < 2 * WT; g0 += kVG) {
+    // Every live value of z tests its support row against D(y); in the
+    // global-memory fixpoint with domains up to 128 values all rows are loaded
+    // before any is tested (elsewhere group by group: the registers are
+    // needed).
+    constexpr int kVG = (kGlobal && WT <= 2) ? 2 * WT : 1;
+    if constexpr (kVG > 1) {
       u64 r[kVG][WT];
       bool live[kVG];
 #pragma unroll
       for (int g = 0; g < kVG; ++g) {
-        const int base = (g0 + g) * 32;
+        const int base = g * 32;
         live[g] = (dz[base >> 6] >> ((base & 32) + lane)) & 1ull;
         if (live[g]) {
           load_row<WT>(N.rel, A.zy + static_cast<size_t>(base + lane) * WT, r[g]);
@@ -276,11 +277,28 @@ __device__ __forceinline__ void revise_arc(const DevNet& N, const Fix& F, u32* q
       }
 #pragma unroll
       for (int g = 0; g < kVG; ++g) {
-        const int base = (g0 + g) * 32;
+        const int base = g * 32;
         u64 hit = 0;
 #pragma unroll
         for (int w = 0; w < WT; ++w) hit |= r[g][w] & dy[w];
         const u32 m = __ballot_sync(kFull, live[g] && hit == 0);
+        rm[base >> 6] |= static_cast<u64>(m) << (base & 32);
+      }
+    } else {
+#pragma unroll
+      for (int base = 0; base < 64 * WT; base += 32) {
+        const u32 bits = static_cast<u32>(dz[base >> 6] >> (base & 32));
+        if (bits == 0) continue;
+        bool unsup = false;
+        if ((bits >> lane) & 1u) {
+          u64 r[WT];
+          load_row<WT>(N.rel, A.zy + static_cast<size_t>(base + lane) * WT, r);
+          u64 hit = 0;
+#pragma unroll
+          for (int w = 0; w < WT; ++w) hit |= r[w] & dy[w];
+          unsup = hit == 0;
+        }
+        const u32 m = __ballot_sync(kFull, unsup);
         rm[base >> 6] |= static_cast<u64>(m) << (base & 32);
       }
     }
@@ -371,24 +389,41 @@ __device__ __forceinline__ void process_item(const DevNet& N, const Fix& F, u32 
   const int lo = c * N.chunk;
   const int hi = min(lo + N.chunk, da + dt);
   const int hb = min(hi, da);  // binary arcs of this item: [lo, hb)
-  // D(y) once per item: these revisions change other variables only (a
-  // change of D(y) by another warp queues y again). The next arc's record is
-  // read while the current one is revised.
+  // Global-memory fixpoints with domains up to 256 values read D(y) once per
+  // item (these revisions change other variables only; a change of D(y) by
+  // another warp queues y again) and read the next arc's record while the
+  // current one is revised. The CTA-local fixpoints (shared-memory domains,
+  // short latencies) and the widest domains read both per arc and keep the
+  // registers.
+  constexpr bool kHoist = kGlobal && WT <= 4;
   u64 dy[WT];
   int cy = 0;
   Arc nxt{};
-  if (lo < hb) {
-    load_dom_uniform<WT>(F.D + static_cast<size_t>(y) * WT, dy);
+  if constexpr (kHoist) {
+    if (lo < hb) {
+      load_dom_uniform<WT>(F.D + static_cast<size_t>(y) * WT, dy);
 #pragma unroll
-    for (int w = 0; w < WT; ++w) cy += __popcll(dy[w]);
-    nxt = N.arcs[a0 + lo];
+      for (int w = 0; w < WT; ++w) cy += __popcll(dy[w]);
+      nxt = N.arcs[a0 + lo];
+    }
   }
   for (int i = lo; i < hi; ++i) {
     if (i < da) {
-      const Arc A = nxt;
-      if (i + 1 < hb) nxt = N.arcs[a0 + i + 1];
-      if (any_failed(F)) return;
-      revise_arc<WT, kGlobal>(N, F, qn, fbn, qlenn, slot, y, dy, cy, A, cn);
+      if constexpr (kHoist) {
+        const Arc A = nxt;
+        if (i + 1 < hb) nxt = N.arcs[a0 + i + 1];
+        if (any_failed(F)) return;
+        revise_arc<WT, kGlobal>(N, F, qn, fbn, qlenn, slot, y, dy, cy, A, cn);
+      } else {
+        if (any_failed(F)) return;
+        const Arc A = N.arcs[a0 + i];
+        u64 dyl[WT];
+        load_dom_uniform<WT>(F.D + static_cast<size_t>(y) * WT, dyl);
+        int cyl = 0;
+#pragma unroll
+        for (int w = 0; w < WT; ++w) cyl += __popcll(dyl[w]);
+        revise_arc<WT, kGlobal>(N, F, qn, fbn, qlenn, slot, y, dyl, cyl, A, cn);
+      }
     } else if constexpr (kTab) {
       if (any_failed(F)) return;
       const int t = N.vtab[t0 + i - da];
