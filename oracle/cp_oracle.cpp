@@ -355,8 +355,9 @@ bool sac1(const Net& N, u64* D, int64_t* deletions) {
 }
 
 // ---------------------------------------------------------------------------
-// MAC with dom/min variable order and min value order: restates MAC::enforce
-// (src/MAC.cpp:100-165), select_var VRH_DOM_MIN (:357-365), select_val
+// MAC with dom/min (or dom/deg) variable order and min value order: restates
+// MAC::enforce (src/MAC.cpp:100-165), select_var VRH_DOM_MIN (:357-365) and
+// VRH_DOM_DEG_MIN (:371-386), select_val
 // VLH_MIN (:423-425), get_solution (:256-271), the level operations of
 // Network / IntVar (src/Network.cpp:106-118, 235-256, 438-455) and
 // AssignedStack push / pop / update_model_assigned (src/Solver.cpp:36-56,
@@ -404,13 +405,30 @@ struct MacState {
   }
 };
 
-int mac(const Net& N, const u64* d0, int64_t time_limit_ms, int64_t* npos, int64_t* nneg, int* solution) {
+// Number of distinct other variables sharing a constraint with each variable:
+// the size of Network::neighborhood (get_neighbor, src/Network.cpp:467-476).
+std::vector<int> neighbour_counts(const Net& N) {
+  std::vector<int> cnt(N.n, 0);
+  std::vector<int> mark(N.n, -1);
+  for (int v = 0; v < N.n; ++v)
+    for (int c : N.subs[v])
+      for (int x : N.scope[c])
+        if (x != v && mark[x] != v) {
+          mark[x] = v;
+          ++cnt[v];
+        }
+  return cnt;
+}
+
+// varh: 1 = VRH_DOM_MIN, 4 = VRH_DOM_DEG_MIN (Heuristic::Var, include/Solver.h:55-63).
+int mac(const Net& N, const u64* d0, int64_t time_limit_ms, int varh, int64_t* npos, int64_t* nneg, int* solution) {
   const auto t0 = std::chrono::steady_clock::now();
   auto elapsed_ms = [&]() {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   };
   MacState S(N, d0);
   Prop P(N);
+  const std::vector<int> deg = varh == 4 ? neighbour_counts(N) : std::vector<int>();
   *npos = *nneg = 0;
   if (!P.enforce(S.D(0), all_vars(N.n), S.A(0), nullptr)) return 0;
   for (;;) {
@@ -418,11 +436,16 @@ int mac(const Net& N, const u64* d0, int64_t time_limit_ms, int64_t* npos, int64
     const int p = int(S.I.size());
     int var = -1;
     double min_size = 1e300;
-    for (int v = 0; v < N.n; ++v)
-      if (!S.A(p)[v] && dsize(S.D(p), N.W, v) < min_size) {
-        min_size = dsize(S.D(p), N.W, v);
+    for (int v = 0; v < N.n; ++v) {
+      if (S.A(p)[v]) continue;
+      // dom/deg: integer size / |neighbourhood|, -1 for a variable without
+      // neighbours; both orders take the first strict minimum.
+      const int key = varh == 4 ? (deg[v] == 0 ? -1 : dsize(S.D(p), N.W, v) / deg[v]) : dsize(S.D(p), N.W, v);
+      if (key < min_size) {
+        min_size = key;
         var = v;
       }
+    }
     const int a = head(S.D(p), N.W, var);
     S.new_level(p);
     S.push(var, a);
@@ -563,7 +586,14 @@ int orc_sac1(const OrcNet* v, uint64_t* dom, int64_t* deletions) {
 int orc_mac(const OrcNet* v, const uint64_t* dom0, int64_t time_limit_ms, int64_t* num_positive,
             int64_t* num_negative, int* solution) {
   Net N = build_net(v);
-  return mac(N, dom0, time_limit_ms, num_positive, num_negative, solution);
+  return mac(N, dom0, time_limit_ms, 1, num_positive, num_negative, solution);
+}
+
+int orc_mac_h(const OrcNet* v, const uint64_t* dom0, int64_t time_limit_ms, int varh, int64_t* num_positive,
+              int64_t* num_negative, int* solution) {
+  if (varh != 1 && varh != 4) return -1;
+  Net N = build_net(v);
+  return mac(N, dom0, time_limit_ms, varh, num_positive, num_negative, solution);
 }
 
 // Lexicographic backtracking that checks each constraint once its scope is

@@ -56,6 +56,7 @@ def lib():
         L.orc_gac_definitional.argtypes = [PN, P64]
         L.orc_sac1.argtypes = [PN, P64, Pi64]
         L.orc_mac.argtypes = [PN, P64, C.c_int64, Pi64, Pi64, PI]
+        L.orc_mac_h.argtypes = [PN, P64, C.c_int64, C.c_int, Pi64, Pi64, PI]
         L.orc_brute_solve.argtypes = [PN, P64, C.c_double]
         L.orc_check_solution.argtypes = [PN, PI]
         L.orc_singleton.argtypes = [PN, P64, C.c_int, C.c_int]
@@ -177,11 +178,14 @@ def sac1(inst: Instance, dom=None):
     return bool(ok), d, dels.value
 
 
-def mac(inst: Instance, time_limit_ms=600000):
+def mac(inst: Instance, time_limit_ms=600000, varh=1):
+    """varh: 1 = VRH_DOM_MIN, 4 = VRH_DOM_DEG_MIN."""
     npos, nneg = C.c_int64(), C.c_int64()
     sol = np.full(inst.n, -1, dtype=np.int32)
-    st = lib().orc_mac(C.byref(inst.view()), _ptr(inst.init, C.c_uint64), time_limit_ms, C.byref(npos),
-                       C.byref(nneg), _ptr(sol, C.c_int))
+    st = lib().orc_mac_h(C.byref(inst.view()), _ptr(inst.init, C.c_uint64), time_limit_ms, varh, C.byref(npos),
+                         C.byref(nneg), _ptr(sol, C.c_int))
+    if st < 0:
+        raise ValueError("variable heuristic must be 1 (dom/min) or 4 (dom/deg)")
     return {"status": st, "num_positive": npos.value, "num_negative": nneg.value,
             "solution": sol.tolist() if st == 1 else []}
 

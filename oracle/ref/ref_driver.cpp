@@ -175,8 +175,8 @@ int main(int argc, char** argv) {
     }
     out << ", \"consistent\": " << (ok ? "true" : "false") << ", \"deletions\": " << sac.del();
     if (ok) out << ", \"domains\": \"" << domains_hex(net, I, 0) << "\"";
-  } else if (op == "mac") {
-    MAC mac(&net, AC_3bit, Heuristic::VRH_DOM_MIN, Heuristic::VLH_MIN);
+  } else if (op == "mac" || op == "mac_domdeg") {
+    MAC mac(&net, AC_3bit, op == "mac" ? Heuristic::VRH_DOM_MIN : Heuristic::VRH_DOM_DEG_MIN, Heuristic::VLH_MIN);
     SearchStatistics st;
     {
       Silence s;

@@ -29,6 +29,10 @@ def cases():
     for s in range(1, 11):
         for op in ("ac3bit", "sac1", "mac"):
             out.append(("cfg1", ["binary", 50, 16, 250, 0.3, 0.3, 0.0, s], op))
+    # MAC with the dom/deg variable order (VRH_DOM_DEG_MIN), same networks.
+    for s in range(1, 11):
+        out.append(("cfg1", ["binary", 50, 16, 250, 0.3, 0.3, 0.0, s], "mac_domdeg"))
+        out.append(("tight", ["binary", 30, 8, 120, 0.35, 0.35, 0.1, s], "mac_domdeg"))
     # Tight small networks: AC and SAC delete values, MAC backtracks.
     for s in range(1, 11):
         for op in ("ac3bit", "sac1", "mac"):

@@ -67,6 +67,29 @@ def test_mac_matches_reference(golden):
             assert O.check_solution(inst, m["solution"])
 
 
+def test_mac_domdeg_matches_reference(golden):
+    # VRH_DOM_DEG_MIN (src/MAC.cpp:371-386): integer size / |neighbourhood|,
+    # the first strict minimum; decision counts and first solution exact.
+    cases = _cases(golden, "mac_domdeg")
+    assert len(cases) >= 20
+    for c in cases:
+        inst = make_oracle_instance(c["args"])
+        m = O.mac(inst, varh=4)
+        r = c["result"]
+        assert m["num_positive"] == r["num_positive"], c["args"]
+        assert m["num_negative"] == r["num_negative"], c["args"]
+        assert (m["status"] == 1) == (r["num_sol"] == 1), c["args"]
+        if m["status"] == 1:
+            assert m["solution"] == r["solution"], c["args"]
+            assert O.check_solution(inst, m["solution"])
+
+
+def test_mac_rejects_unknown_heuristic(golden):
+    inst = make_oracle_instance(_cases(golden, "mac")[0]["args"])
+    with pytest.raises(ValueError):
+        O.mac(inst, varh=6)
+
+
 def test_gac_equals_ac3bit_on_binary(golden):
     # The GAC worklist restatement gives the AC3bit closure on binary networks.
     for c in _cases(golden, "ac3bit"):
