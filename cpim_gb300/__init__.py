@@ -44,6 +44,7 @@ class VarHeuristic(enum.IntEnum):
     """Heuristic::Var, include/Solver.h:56-64."""
     VRH_LEX = 0
     VRH_DOM_MIN = 1
+    VRH_DOM_DEG_MIN = 4
 
 
 class ValHeuristic(enum.IntEnum):

@@ -194,6 +194,7 @@ struct cp_net {
   cp_engine* e = nullptr;
   int n = 0, W_user = 1, W = 1, nb = 0, nt = 0, levels = 0;
   std::vector<int> dom;
+  std::vector<int> nbr_count;  // distinct neighbour variables (Network::neighborhood sizes)
   std::vector<int> bx, by;
   DevNet dn;
   std::vector<void*> allocs;
@@ -604,6 +605,27 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
           t_tup[t_off[t] + static_cast<int64_t>(i) * k + j] = static_cast<uint16_t>(v);
         }
       src += static_cast<int64_t>(k) * r;
+    }
+  }
+  {
+    // Network::get_neighbor (src/Network.cpp:467-476): the distinct other
+    // variables of every constraint on x; the dom/deg variable order divides
+    // by their number.
+    std::vector<std::vector<int>> adj(n);
+    for (int c = 0; c < n_bin; ++c) {
+      adj[net->bx[c]].push_back(net->by[c]);
+      adj[net->by[c]].push_back(net->bx[c]);
+    }
+    for (int t = 0; t < n_tab; ++t)
+      for (int i = 0; i < t_arity[t]; ++i)
+        for (int j = 0; j < t_arity[t]; ++j)
+          if (i != j)
+            adj[t_scope[static_cast<size_t>(t) * kMaxArity + i]].push_back(
+                t_scope[static_cast<size_t>(t) * kMaxArity + j]);
+    net->nbr_count.resize(n);
+    for (int x = 0; x < n; ++x) {
+      std::sort(adj[x].begin(), adj[x].end());
+      net->nbr_count[x] = static_cast<int>(std::unique(adj[x].begin(), adj[x].end()) - adj[x].begin());
     }
   }
   std::vector<int> tinc_start(n + 1, 0);
@@ -1312,16 +1334,21 @@ class DeviceMAC {
     return CP_OK;
   }
   // VRH_DOM_MIN (src/MAC.cpp:357-365): first unassigned variable of strictly
-  // smaller size; VRH_LEX (:366-368).
+  // smaller size; VRH_LEX (:366-368); VRH_DOM_DEG_MIN (:371-386): the same
+  // with the integer key size / |neighbourhood| (-1 without neighbours).
   int select_var(int p) {
     if (varh_ == 0) return static_cast<int>(I_.size()) + 1 < n_ ? static_cast<int>(I_.size()) + 1 : -1;
     int var = -1;
     double min_size = 1e300;
-    for (int v = 0; v < n_; ++v)
-      if (!A(p)[v] && R.size(v) < min_size) {
-        min_size = R.size(v);
+    for (int v = 0; v < n_; ++v) {
+      if (A(p)[v]) continue;
+      const int deg = R.net->nbr_count[v];
+      const int key = varh_ == 4 ? (deg == 0 ? -1 : R.size(v) / deg) : R.size(v);
+      if (key < min_size) {
+        min_size = key;
         var = v;
       }
+    }
     return var;
   }
   void new_level(int src) {
@@ -1640,10 +1667,11 @@ extern "C" {
 int cp_mac_solve(cp_net* net, int var_heuristic, int val_heuristic, int64_t time_limit_ms, cp_search_result* res,
                  int* solution) {
   if (!net || !res || !solution) return fail(CP_E_ARG, "null argument");
-  if (var_heuristic != 0 && var_heuristic != 1)
-    return fail(CP_E_UNSUPPORTED, "variable heuristic: 0 (VRH_LEX) or 1 (VRH_DOM_MIN)");
+  if (var_heuristic != 0 && var_heuristic != 1 && var_heuristic != 4)
+    return fail(CP_E_UNSUPPORTED, "variable heuristic: 0 (VRH_LEX), 1 (VRH_DOM_MIN) or 4 (VRH_DOM_DEG_MIN)");
   if (val_heuristic != 0) return fail(CP_E_UNSUPPORTED, "value heuristic: 0 (VLH_MIN)");
-  if (net->e->search_mode == 0 && !net->prefer_grid) {
+  // dom/deg is chosen on the host (the device search has the dom/min key only).
+  if (net->e->search_mode == 0 && !net->prefer_grid && var_heuristic != 4) {
     // The whole search in one CTA, on the network's own level stack.
     std::vector<MacSpec> spec(1);
     spec[0].net = net;

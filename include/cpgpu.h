@@ -271,9 +271,11 @@ int cp_server_run_trace(cp_server* s, int k, const double* t_arrival_s, const cp
 
 /* ---- search: MAC on device-resident domains -------------------------------
  * MAC::enforce (src/MAC.cpp:100-165) with the reference's variable and value
- * heuristics (include/Solver.h:55-66: var 1 = VRH_DOM_MIN, value 0 =
- * VLH_MIN); the host keeps the reference's control flow, the level stack
- * and every propagation stay on the device. */
+ * heuristics (include/Solver.h:55-66: var 0 = VRH_LEX, 1 = VRH_DOM_MIN,
+ * 4 = VRH_DOM_DEG_MIN; value 0 = VLH_MIN); the host keeps the reference's
+ * control flow, the level stack and every propagation stay on the device.
+ * VRH_DOM_DEG_MIN always runs host-driven (the variable is chosen on the host
+ * from the device's domain sizes); batches take 0 and 1 only. */
 typedef struct cp_search_result {
   int32_t status;        /* 1 solution, 0 proved unsatisfiable, 2 time out */
   int32_t pad;

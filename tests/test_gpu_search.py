@@ -162,3 +162,23 @@ def test_xcsp_instances_on_the_device(which):
     assert (r["num_positive"], r["num_negative"]) == (ref["num_positive"], ref["num_negative"])
     if r["status"] == 1:
         assert r["solution"] == ref["solution"]
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_mac_domdeg_matches_reference(golden, mode):
+    # VRH_DOM_DEG_MIN (src/MAC.cpp:371-386): the variable is chosen on the host
+    # from the device's domain sizes in either search mode; decision counts and
+    # first solutions equal the reference's own MAC runs.
+    cases = [c for c in golden if c["op"] == "mac_domdeg"]
+    assert len(cases) >= 20
+    with cp.Engine(0) as e:
+        e.set_search_mode(mode)
+        for c in cases:
+            net = e.upload(make_engine_instance(c["args"]))
+            m = net.mac_solve(cp.VarHeuristic.VRH_DOM_DEG_MIN, cp.ValHeuristic.VLH_MIN, time_limit_ms=120000)
+            r = c["result"]
+            assert (m["status"] == 1) == (r["num_sol"] == 1), c["args"]
+            assert (m["num_positive"], m["num_negative"]) == (r["num_positive"], r["num_negative"]), c["args"]
+            if m["status"] == 1:
+                assert m["solution"] == r["solution"], c["args"]
+            net.close()
