@@ -1220,14 +1220,17 @@ __global__ void k_build_work(DevNet N, const u64* dom, int2* work, int* nwork, i
 // rounds unless round two removes something: round one only shrinks the
 // neighbours y of x to D0(y) & R[x=a -> y]; round two revises every arc
 // (z <- y) out of those neighbours. This kernel computes round one for all 32
-// branches into shared memory, then only tests round two: for each arc it
-// ORs the support rows R[y=c -> z] over c in each lane's D_a(y) (one
-// broadcast load per row serves all 32 branches) and stops as soon as every
-// lane's D(z) is covered. A branch whose round two would remove nothing is
-// consistent; one whose round two empties a domain is not; any other branch
-// (round two removes values) is handed to the general kernel, which computes
-// its fixpoint in full. Arcs back into x need no test: x's single value keeps
-// a support in every non-empty D_a(y) by construction.
+// branches into shared memory, then only tests round two, one lane per arc:
+// a value v of z can lose every support in branch b only if its support count
+// in D0(y) is at most the number of values b's round one removed from D0(y),
+// so the lane tests just those (branch, value) pairs, taking v from the arc's
+// weak-support list; an arc whose list does not reach far enough for some
+// branch is revised value-wise by the whole warp for those branches. A branch
+// whose round two would remove nothing is consistent; one whose round two
+// empties a domain is not; any other branch (round two removes values) is
+// handed to the general kernel, which computes its fixpoint in full. Arcs
+// back into x need no test: x's single value keeps a support in every
+// non-empty D_a(y) by construction.
 // ---------------------------------------------------------------------------
 template <int WT>
 __device__ __forceinline__ int pop_low(u64& m, int word) {
