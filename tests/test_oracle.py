@@ -111,6 +111,51 @@ def test_gac_matches_definition_mixed(seed):
         assert np.array_equal(d1, d2)
 
 
+def _nary_instance(seed, n=14, d=4, n_tab=5, arities=(5, 6), ntup=(14, 48)):
+    # Positive tables of arity 5 and 6 over small domains (no binary rows);
+    # over seeds 1..8 GAC deletes values in most, wipes one out, and one has
+    # a solution.
+    rng = np.random.default_rng(seed)
+    ar, sc, nt, tu = [], [], [], []
+    for _ in range(n_tab):
+        r = int(rng.choice(arities))
+        scope = rng.choice(n, size=r, replace=False)
+        k = int(rng.integers(*ntup))
+        space = rng.choice(d ** r, size=k, replace=False)
+        tuples = [[(int(code) // d ** i) % d for i in range(r)] for code in space]
+        ar.append(r)
+        sc.extend(int(v) for v in scope)
+        nt.append(k)
+        tu.extend(v for t in tuples for v in t)
+    init = np.full(n, (1 << d) - 1, dtype=np.uint64)
+    for x in rng.choice(n, size=3, replace=False):  # a few values removed up front
+        init[x] &= ~np.uint64(1 << int(rng.integers(0, d)))
+    z = np.zeros(0, np.int32)
+    return O.Instance(n=n, W=1, dom=np.full(n, d, np.int32), init=init, bx=z, by=z.copy(),
+                      brows=np.zeros(0, np.uint64), tarity=np.array(ar, np.int32), tscope=np.array(sc, np.int32),
+                      tntup=np.array(nt, np.int32), ttup=np.array(tu, np.int32))
+
+
+@pytest.mark.parametrize("seed", range(1, 9))
+def test_gac_nary_matches_definition(seed):
+    # Tables beyond arity 4 (the device table revise stops at 4): the oracle's
+    # worklist GAC equals the literal definition of samples/verify_gac.cpp,
+    # and every solution's values survive it.
+    inst = _nary_instance(seed)
+    ok1, d1, _ = O.gac(inst)
+    ok2, d2 = O.gac_definitional(inst)
+    assert ok1 == ok2
+    if ok1:
+        assert np.array_equal(d1, d2)
+        m = O.mac(inst)
+        if m["status"] == 1:
+            assert O.check_solution(inst, m["solution"])
+            for x, a in enumerate(m["solution"]):
+                assert (int(d1[x]) >> a) & 1
+    else:
+        assert O.brute_solve(inst) == 0
+
+
 def test_gac_mixed_binary_part_pinned(golden):
     # The binary sub-network of each mixed instance matches the reference
     # AC3bit, and adding the tables only removes more.
