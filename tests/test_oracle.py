@@ -140,7 +140,7 @@ def _nary_instance(seed, n=14, d=4, n_tab=5, arities=(5, 6), ntup=(14, 48)):
 def test_gac_nary_matches_definition(seed):
     # Tables beyond arity 4 (the device table revise stops at 4): the oracle's
     # worklist GAC equals the literal definition of samples/verify_gac.cpp,
-    # and every solution's values survive it.
+    # every solution's values survive it, and a wipe-out has no solution.
     inst = _nary_instance(seed)
     ok1, d1, _ = O.gac(inst)
     ok2, d2 = O.gac_definitional(inst)
@@ -153,7 +153,7 @@ def test_gac_nary_matches_definition(seed):
             for x, a in enumerate(m["solution"]):
                 assert (int(d1[x]) >> a) & 1
     else:
-        assert O.brute_solve(inst) == 0
+        assert O.mac(inst)["status"] == 0
 
 
 def test_gac_mixed_binary_part_pinned(golden):
