@@ -648,7 +648,9 @@ def run_mac(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 300; 3 for the uneven batch, whose step is a full AC + SAC1 of "
+                         "4096 instances)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="timed steps only (for profiling)")
@@ -667,6 +669,8 @@ def main():
     ap.add_argument("--solvers", type=int, default=4, help="serving: MAC solver threads")
     ap.add_argument("--solve-limit-ms", type=int, default=500, help="serving: MAC solve time limit")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 3 if args.workload == "uneven" and args.impl == "ours" else 300
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "uneven":
