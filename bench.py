@@ -7,11 +7,21 @@ then every live (x, a) singleton test (n*d = 64000 branch fixpoints) in one
 persistent launch per sweep, until no test fails. Synthetic inputs with the
 shape of the published workload; generated by cpim_gb300/csrc/cp_gen.h.
 
-value: singleton fixpoints per second over K steps, inputs resident in HBM,
-CUDA-event device time of each enforce call; L2 is flushed (a 256 MiB write)
-before every step. e2e: the same metric through the C ABI with host buffers:
-every step re-uploads the relations and domains from pinned host memory
-(cp_net_reload), runs cp_enforce_sac1 and reads the final domains back.
+A step is a batch of R such closures (R = --closures-per-step, default 128),
+so that even a short run (--steps 20) keeps the GPU busy for over a second
+and the clock sampler sees it. value: singleton fixpoints per second over K
+steps, inputs resident in HBM, CUDA-event device time of each enforce call;
+L2 is flushed (a 256 MiB write) before every closure. e2e: the same metric
+through the C ABI with host buffers: every closure re-uploads the relations
+and domains from pinned host memory (cp_net_reload), runs cp_enforce_sac1 and
+reads the final domains back.
+
+Outside the timed region the line also carries: parity (every first-sweep
+singleton verdict and the SAC closure against the oracle on the host cores),
+the roofline of the sweep kernels (with and without the per-branch domain
+copy term, and the DRAM fraction from the committed ncu capture in
+profiles/k_sac_tile_cfg3_sweep.json), the large GAC fixpoint, and a
+256-instance sample of the uneven batch against its one-by-one rate.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -45,24 +55,22 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def profile_field(name):
-    """A 'name: value' line of the committed ncu summary of the SAC sweep
-    kernels (profiles/k_sac_tile_cfg3_sweep.md), or None."""
-    path = os.path.join(ROOT, "profiles", "k_sac_tile_cfg3_sweep.md")
+def sweep_profile():
+    """The committed ncu figures of the SAC sweep kernels on this workload
+    (profiles/k_sac_tile_cfg3_sweep.json: DRAM bytes per sweep, limiter), or
+    an empty dict."""
     try:
-        for line in open(path):
-            if line.startswith(name + ":"):
-                return line.split(":", 1)[1].strip()
-    except OSError:
-        pass
-    return None
+        with open(os.path.join(ROOT, "profiles", "k_sac_tile_cfg3_sweep.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
 
 
-def profile_traffic():
-    """DRAM bytes (read + write) per sweep of the SAC sweep kernels, from the
-    committed ncu summary, or None."""
-    v = profile_field("traffic_bytes_per_launch")
-    return float(v.split()[0]) if v else None
+def bench_config(**extra):
+    """The config dict both arms print."""
+    c = {"workload": WORKLOAD, "n": N, "d": D, "e": E, "p": P, "seed": SEED}
+    c.update(extra)
+    return c
 
 
 class ClockSampler:
@@ -127,19 +135,21 @@ def dist_env():
     return rank, world, local
 
 
-def cpu_baseline_port(inst, threads, budget_s=15.0):
+def oracle_instance():
+    """The benchmark network from the oracle library's copy of the generator
+    (the same cp_gen.h the engine compiles; fingerprints are compared)."""
+    from oracle import pyoracle as O
+    return O.gen_binary(N, D, E, P, P, 0.0, SEED)
+
+
+def cpu_baseline_port(ov, threads, budget_s=15.0):
     """The oracle's SAC singleton test (the reference's AC3bit inner loop,
     restated) on host cores over an evenly spread sample of branches."""
     from oracle import pyoracle as O
-    import numpy as np
-    ov = O.Instance(n=inst.n, W=inst.W, dom=inst.dom, init=inst.init,
-                    bx=np.ascontiguousarray(inst.bin_scope[0::2]), by=np.ascontiguousarray(inst.bin_scope[1::2]),
-                    brows=inst.bin_rows, tarity=inst.tab_arity, tscope=inst.tab_scope, tntup=inst.tab_ntup,
-                    ttup=inst.tab_tuples)
-    s1, done1, _ = O.time_singletons(ov, inst.init, 64, 1)
+    s1, done1, _ = O.time_singletons(ov, ov.init, 64, 1)
     per_branch = s1 / max(1, done1)
     count = int(max(256, min(64000, budget_s / per_branch)))
-    secs, done, failed = O.time_singletons(ov, inst.init, count, threads)
+    secs, done, failed = O.time_singletons(ov, ov.init, count, threads)
     return {"value": done / secs, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": "%d of the %d singleton branches (evenly spread), oracle AC3bit restatement, %d host threads"
                       % (done, N * D, threads),
@@ -147,13 +157,15 @@ def cpu_baseline_port(inst, threads, budget_s=15.0):
 
 
 def run_reference(args):
+    """The reference's CPU singleton test (its restatement in oracle/; the
+    reference's own build does not travel to this host) on all host threads.
+    Loads only the oracle library: the engine is not imported."""
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    import cpim_gb300 as cp
     from oracle import pyoracle
     pyoracle.build()
-    inst = cp.gen_binary(N, D, E, P, P, 0.0, SEED)
+    inst = oracle_instance()
     threads = os.cpu_count() or 1
     vals = []
     # Each step is a bounded sample sized so the whole run stays near 90 s of
@@ -168,7 +180,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded generator)",
-            "config": {"workload": WORKLOAD, "parallelism": "host threads"},
+            "config": bench_config(parallelism="host threads (%d)" % threads),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": base["sample"] + "; per step, median over steps"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -176,6 +188,103 @@ def run_reference(args):
                     "on this host its restatement in oracle/ is timed"}
     print(json.dumps(line))
     return 0
+
+
+def parity_check(net, final, eng_fp):
+    """Outside the timed region: one Jacobi sweep of singleton tests through
+    the sweep kernels (cp_sac_sweep) against the oracle's verdicts for every
+    live (x, a), and the timed closure against the oracle's SAC closure, both
+    on all host threads."""
+    import numpy as np
+    from oracle import pyoracle as O
+    ov = oracle_instance()
+    assert ov.fingerprint == eng_fp, "engine and oracle generators disagree"
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    ok_ac, d_ac, _ = O.ac3bit(ov)
+    ver_o, failed_o = O.singleton_verdicts(ov, d_ac, threads)
+    ok_s, d_sac, _, sweeps_o = O.sac_jacobi(ov, None, threads)
+    oracle_s = time.perf_counter() - t0
+    net.dom_set(0, ov.init)
+    ver_g, deep, st = net.sac_sweep(0)
+    live = int(sum(bin(int(w)).count("1") for w in d_ac))
+    diff = int(sum(bin(int(a) ^ int(b)).count("1") for a, b in zip(ver_g, ver_o)))
+    return {"first_sweep_verdicts": {"live_values": live, "equal": live - diff, "failed_oracle": failed_o,
+                                     "deep_list": int(deep), "bit_exact": diff == 0},
+            "closure": {"bit_exact": bool(ok_s and np.array_equal(final, d_sac)), "oracle_sweeps": sweeps_o},
+            "oracle": "oracle/ restatement of AC3bit + SAC1 singleton tests, %d host threads, %.1f s"
+                      % (threads, oracle_s)}
+
+
+def gac_sample(eng, peak, flush, steps=20, warmup=3):
+    """The large GAC fixpoint (n=2000, d=64, 30000 binary + 5000 ternary
+    tables with 500 tuples, 20% of values removed, seed 1) on the grid-wide
+    kernel: median CUDA-event time over `steps` runs, L2 flushed before each,
+    verdict checked against the oracle."""
+    import torch
+    import cpim_gb300 as cp
+    from oracle import pyoracle as O
+    inst = cp.gen_mixed(2000, 64, 30000, 0.2, 0.5, 5000, 500, 0.2, 1)
+    net = eng.upload(inst, max_levels=2)
+    sts = []
+    for i in range(warmup + steps):
+        net.dom_set(0, inst.init)
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        st = net.enforce_ac(0)
+        if i >= warmup:
+            sts.append(st)
+    ms = statistics.median(s.device_ms for s in sts)
+    st = sts[-1]
+    ok, _, dels = O.gac(O.Instance(n=inst.n, W=inst.W, dom=inst.dom, init=inst.init,
+                                   bx=inst.bin_scope[0::2].copy(), by=inst.bin_scope[1::2].copy(),
+                                   brows=inst.bin_rows, tarity=inst.tab_arity, tscope=inst.tab_scope,
+                                   tntup=inst.tab_ntup, ttup=inst.tab_tuples))
+    net.close()
+    ach = st.alg_bytes / (ms / 1e3) / 1e9
+    return {"workload": "GAC fixpoint: n=2000 d=64, 30000 binary (p~U[0.2,0.5]) + 5000 ternary positive tables "
+                        "(500 tuples), 20% of values removed, seed 1; L2 flushed before each run",
+            "ms": ms, "revisions_per_s": st.revisions / (ms / 1e3), "rounds": int(st.rounds),
+            "inconsistent": bool(st.inconsistent), "verdict_equals_oracle": ok == (not st.inconsistent),
+            "alg_gb_per_s": ach, "frac_of_hbm_peak": ach / peak}
+
+
+def uneven_sample(eng, k=256, per_instance=64):
+    """A k-instance sample of the uneven batch (seeds 7*1000003+i): AC + SAC1
+    of every member in one batch (graph-replayed sweeps, tuned), against the
+    first `per_instance` members run one by one."""
+    import cpim_gb300 as cp
+    nets = []
+    for i in range(k):
+        net = cp.upload_uneven_device(eng, 7 * 1000003 + i, 20, 400, 256, max_levels=2)
+        net.level_copy(0, 1)
+        nets.append(net)
+    batch = cp.Batch(eng, nets, level=0)
+    batch.tune()
+    ms = []
+    for _ in range(3):
+        batch.copy_level(1)
+        st, inc = batch.sac1()
+        ms.append(st.device_ms)
+    batch.close()
+    t = 0.0
+    for net in nets[:per_instance]:
+        net.level_copy(1, 0)
+        t += net.enforce_sac1(0).device_ms
+    sub = cp.Batch(eng, nets[:per_instance], level=0)
+    sub_ms = []
+    for _ in range(2):
+        sub.copy_level(1)
+        sub_ms.append(sub.sac1()[0].device_ms)
+    sub.close()
+    for n in nets:
+        n.close()
+    one = per_instance / (t / 1e3)
+    same = per_instance / (min(sub_ms) / 1e3)
+    return {"workload": UNEVEN_WORKLOAD.format(k=k), "instances_per_s": k / (min(ms) / 1e3),
+            "ms_per_batch": min(ms), "inconsistent_instances": int(inc.sum()),
+            "one_by_one": {"instances": per_instance, "instances_per_s": one,
+                           "batched_same_instances_per_s": same, "batched_over_one_by_one": same / one}}
 
 
 def run_ours(args):
@@ -194,17 +303,21 @@ def run_ours(args):
             import torch.distributed as dist
             dist.barrier()
 
+    R = args.closures_per_step
     inst = cp.gen_binary(N, D, E, P, P, 0.0, SEED)
     eng = cp.Engine(local)
     net = eng.upload(inst, max_levels=2)
     pristine = inst.init.copy()
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
 
-    def step():
+    def closure():
         net.dom_set(0, pristine)
         flush.fill_(1)
         torch.cuda.synchronize()
         return net.enforce_sac1(0)
+
+    def step():
+        return [closure() for _ in range(R)]
 
     for _ in range(args.warmup):
         step()
@@ -215,17 +328,20 @@ def run_ours(args):
     if args.quick:
         # Profiling mode: the timed steps only, no baselines and no e2e leg.
         for _ in range(args.steps):
-            sts.append(step())
+            sts += step()
         torch.cuda.synchronize()
         if rank == 0:
-            print(json.dumps({"quick": True, "steps": len(sts), "ms_per_step": sum(s.device_ms for s in sts) / len(sts),
+            print(json.dumps({"quick": True, "closures": len(sts),
+                              "ms_per_closure": sum(s.device_ms for s in sts) / len(sts),
                               "kernel_ms": sum(s.kernel_ms for s in sts) / len(sts),
                               "branches": int(sts[-1].branches)}))
         return 0
+    t_wall = time.perf_counter()
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
-            sts.append(step())
-    torch.cuda.synchronize()
+            sts += step()
+        torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall
     barrier()
     gpu_launches = eng.launches - launches0
     dev_ms = [s.device_ms for s in sts]
@@ -234,17 +350,21 @@ def run_ours(args):
     from cpim_gb300.replicas import job_rate
     _, job_s, value = job_rate(branches, sum(dev_ms) / 1e3, device="cuda")
     total_ms = job_s * 1e3
-    # Parity of the timed result (deterministic closure): consistent, no test fails.
     final = net.dom_get(0)
     assert not sts[-1].inconsistent
 
-    # Roofline of the dominant kernel: the batched singleton kernel.
+    # Roofline of the dominant kernels: the sweep kernels of each closure.
     kern_ms = sum(s.kernel_ms for s in sts)
     kern_bytes = sum(s.kernel_bytes for s in sts)
     launches_k = sum(s.sweeps for s in sts)
+    copy_bytes = float(branches) * 2 * N * inst.W * 8
     peak, peak_kind = measured_peaks()
     achieved = (kern_bytes / (kern_ms / 1e3)) / 1e9 if kern_ms > 0 else 0.0
-    traffic = profile_traffic()
+    achieved_nc = ((kern_bytes - copy_bytes) / (kern_ms / 1e3)) / 1e9 if kern_ms > 0 else 0.0
+    prof = sweep_profile()
+    traffic = prof.get("dram_bytes_per_sweep")
+    kms_launch = kern_ms / max(1, launches_k)
+    dram_gbs = traffic / (kms_launch / 1e3) / 1e9 if traffic else None
 
     # e2e through the C ABI with pinned host buffers.
     rows_pin = torch.from_numpy(inst.bin_rows.view(np.int64)).pin_memory()
@@ -256,19 +376,20 @@ def run_ours(args):
                            tab_ntup=inst.tab_ntup, tab_tuples=inst.tab_tuples)
     out = np.zeros(inst.n * inst.W, np.uint64)
 
-    def e2e_step():
+    def e2e_closure():
         net.reload(e2e_inst)
         st = net.enforce_sac1(0)
         r = net.dom_get(0)
         return st, r
 
     for _ in range(max(1, args.warmup)):
-        e2e_step()
+        e2e_closure()
     torch.cuda.synchronize()
+    e2e_steps = max(1, args.steps // 4)
     t0 = time.perf_counter()
     e2e_br = 0
-    for _ in range(args.steps):
-        st, r = e2e_step()
+    for _ in range(e2e_steps * R):
+        st, r = e2e_closure()
         e2e_br += st.branches
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
@@ -280,6 +401,7 @@ def run_ours(args):
     k = 2000
     xs = rng.integers(0, N, k).astype(np.int32)
     vs = rng.integers(0, D, k).astype(np.int32)
+    net.dom_set(0, pristine)
     net.singletons(xs[:100], vs[:100], mode=1)
     ok_p, st_p = net.singletons(xs, vs, mode=1)
     ok_b, st_b = net.singletons(xs, vs, mode=0)
@@ -289,31 +411,42 @@ def run_ours(args):
     if rank != 0:
         return 0
     clocks = clk.summary()
-    base = cpu_baseline_port(inst, os.cpu_count() or 1)
+    parity = parity_check(net, final, inst.fingerprint)
+    gac = gac_sample(eng, peak, flush) if not args.no_extras else None
+    uneven = uneven_sample(eng) if not args.no_extras else None
+    base = cpu_baseline_port(oracle_instance(), os.cpu_count() or 1)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": total_ms / len(sts), "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic (seeded generator, shape of the published workload)",
-        "config": {"workload": WORKLOAD, "n": N, "d": D, "e": E, "p": P, "seed": SEED,
-                   "branches_per_step": int(sts[-1].branches), "sweeps_per_step": int(sts[-1].sweeps),
-                   "l2": "flushed before every step (256 MiB write); relations 41 MB fit in L2 within a step",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": bench_config(),
+        "step": "%d SAC closures of the network (each %d branch fixpoints over %d sweep(s)), L2 flushed "
+                "(256 MiB write) and the domains reset before each closure" % (R, int(sts[-1].branches),
+                                                                                int(sts[-1].sweeps)),
+        "parallelism": "replicas (%d GPUs)" % world if world > 1 else "single GPU",
+        "timed_wall_s": t_wall,
         "e2e": {"value": e2e_value, "unit": UNIT,
-                "h2d_bytes_per_step": int(inst.bin_rows.nbytes + inst.init.nbytes),
-                "d2h_bytes_per_step": int(out.nbytes)},
+                "h2d_bytes_per_step": int(R * (inst.bin_rows.nbytes + inst.init.nbytes)),
+                "d2h_bytes_per_step": int(R * out.nbytes), "steps": e2e_steps},
         "gpu_launches": int(gpu_launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
+                     "frac_without_branch_copy": achieved_nc / peak,
+                     "dram_frac": (dram_gbs / peak) if dram_gbs else None,
                      "kernel": "SAC sweep kernels (k_weak + k_sac_tile + k_sac on the deep list), per sweep",
-                     "kernel_ms_per_launch": kern_ms / max(1, launches_k),
+                     "kernel_ms_per_launch": kms_launch,
                      "alg_bytes_per_launch": kern_bytes / max(1, launches_k),
+                     "branch_copy_bytes_per_launch": copy_bytes / max(1, launches_k),
                      "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
-                     "limiter": profile_field("limiter")},
+                     "traffic_source": prof.get("source"), "limiter": prof.get("limiter")},
+        "parity": parity,
         "cpu_baseline": {k2: base[k2] for k2 in ("value", "unit", "cores", "kind", "sample")},
         "plain_single_instance": {"value": plain_rate, "unit": UNIT,
                                   "sample": "%d singleton tests, one single-CTA launch each" % k,
                                   "batched_over_plain": value / plain_rate},
+        "gac_large": gac,
+        "uneven_sample": uneven,
         "clocks": clocks,
     }
     print(json.dumps(line))
@@ -649,11 +782,15 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=None,
-                    help="timed steps (default 300; 3 for the uneven batch, whose step is a full AC + SAC1 of "
-                         "4096 instances)")
+                    help="timed steps (default 20 for the SAC sweep, whose step is 128 closures; 3 for the "
+                         "uneven batch, whose step is a full AC + SAC1 of 4096 instances; 300 otherwise)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="timed steps only (for profiling)")
+    ap.add_argument("--closures-per-step", type=int, default=128,
+                    help="SAC closures per timed step of the default workload")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default workload without the GAC and uneven-batch samples")
     ap.add_argument("--workload", default="sac", choices=["sac", "uneven", "serving", "gac", "mac"],
                     help="sac: the batched SAC sweep (headline); uneven: the uneven multi-instance batch; "
                          "serving: the request server under Poisson load; gac: the large GAC fixpoint; "
@@ -670,7 +807,7 @@ def main():
     ap.add_argument("--solve-limit-ms", type=int, default=500, help="serving: MAC solve time limit")
     args = ap.parse_args()
     if args.steps is None:
-        args.steps = 3 if args.workload == "uneven" and args.impl == "ours" else 300
+        args.steps = 3 if args.workload == "uneven" and args.impl == "ours" else (20 if args.workload == "sac" else 300)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "uneven":

@@ -103,6 +103,7 @@ def lib():
         "cp_enforce_ac": ([vp, i, i, PI, C.POINTER(Stats)], i),
         "cp_enforce_sac1": ([vp, i, C.POINTER(Stats)], i),
         "cp_singletons": ([vp, i, i, PI, PI, PU8, i, C.POINTER(Stats)], i),
+        "cp_sac_sweep": ([vp, i, P64, C.POINTER(C.c_int64), C.POINTER(Stats)], i),
         "cp_mac_solve": ([vp, i, i, i64, C.POINTER(SearchResult), PI], i),
         "cp_gsolver_solve": ([vp, i64, C.POINTER(SearchResult), PI], i),
         "cp_gen_binary": ([i, i, i64, d, d, d, u64, PV], i),
@@ -374,6 +375,15 @@ class Net:
         _check(lib().cp_singletons(self._h, level, len(v), _p(v, C.c_int), _p(a, C.c_int), _p(ok, C.c_uint8), mode,
                                    C.byref(st)))
         return ok, st
+
+    def sac_sweep(self, level=0):
+        """One Jacobi sweep of singleton tests at `level` (after its AC):
+        (verdict words, tests handed to the general kernel, Stats)."""
+        out = np.zeros(self.n * self.W, np.uint64)
+        deep = C.c_int64()
+        st = Stats()
+        _check(lib().cp_sac_sweep(self._h, level, _p(out, C.c_uint64), C.byref(deep), C.byref(st)))
+        return out, deep.value, st
 
     # -- search --
     def mac_solve(self, var_h=VarHeuristic.VRH_DOM_MIN, val_h=ValHeuristic.VLH_MIN, time_limit_ms=600000):

@@ -981,7 +981,9 @@ namespace {
 // events AC of a network without the grid path, which reads the event count
 // first. A sweep queued behind an AC that wiped a domain out only wastes its
 // work; its results are not used.
-int sac_round_launches(cp_net* net, int level, bool root, int& launches, bool captured) {
+// sweep_only: a Jacobi sweep that removes nothing (no early removals, no
+// commit), for cp_sac_sweep.
+int sac_round_launches(cp_net* net, int level, bool root, int& launches, bool captured, bool sweep_only = false) {
   cp_engine* e = net->e;
   cudaStream_t s = e->stream;
   // Kernel-time events: external records become event nodes of a captured round.
@@ -1008,7 +1010,7 @@ int sac_round_launches(cp_net* net, int level, bool root, int& launches, bool ca
   // (later branches of the sweep start without it; the closure is the
   // same, since a wipe-out on a larger domain implies one on a smaller);
   // mode 1 keeps the plain Jacobi sweep as the reference path.
-  u64* gs_root = e->sac_mode == 0 ? net->level_ptr(level) : nullptr;
+  u64* gs_root = e->sac_mode == 0 && !sweep_only ? net->level_ptr(level) : nullptr;
   if (tiled) {
     // Two-round branches resolved by the tiled kernel, the rest (the deep
     // list) by the general kernel; the sweep-start domains and the
@@ -1020,7 +1022,11 @@ int sac_round_launches(cp_net* net, int level, bool root, int& launches, bool ca
       launches += 1;
       e->launches += 1;
     }
-    CP_CUDA(launch_sac_tile(net->dn, net->level_ptr(level), S, S.ok, net->slot_cap, net->d_stats, kTileBlock,
+    // Without the snapshot the tiled kernel reads the level itself and removes
+    // nothing at it (a pure Jacobi sweep: the level does not change).
+    SacScratch St = S;
+    if (sweep_only) St.snap = nullptr;
+    CP_CUDA(launch_sac_tile(net->dn, net->level_ptr(level), St, S.ok, net->slot_cap, net->d_stats, kTileBlock,
                             net->tile_grid, s));
     CP_CUDA(launch_sac_branches(net->dn, net->level_ptr(level), S.work, S.nwork, S.cursor, S.ok, net->d_stats,
                                 e->block_sac, net->sac_grid, net->d_sac_scratch, net->sac_stride, s, S.deep,
@@ -1033,9 +1039,13 @@ int sac_round_launches(cp_net* net, int level, bool root, int& launches, bool ca
                                 nullptr, gs_root));
   }
   CP_CUDA(cudaEventRecordWithFlags(e->evk1, s, evf));
-  CP_CUDA(launch_commit(net->dn, net->level_ptr(level), S, net->d_stats, s));
-  launches += 3;
-  e->launches += 3;
+  if (!sweep_only) {
+    CP_CUDA(launch_commit(net->dn, net->level_ptr(level), S, net->d_stats, s));
+    launches += 1;
+    e->launches += 1;
+  }
+  launches += 2;
+  e->launches += 2;
   CP_CUDA(cudaMemcpyAsync(net->h_stats, net->d_stats, 2 * sizeof(KStats), cudaMemcpyDeviceToHost, s));
   return CP_OK;
 }
@@ -1148,6 +1158,60 @@ int cp_enforce_sac1(cp_net* net, int level, cp_stats* st) {
     acc.s.kernel_ms = kernel_ms;
     acc.s.kernel_bytes = kernel_bytes;
     *st = acc.s;
+  }
+  return CP_OK;
+}
+
+int cp_sac_sweep(cp_net* net, int level, uint64_t* verdict, int64_t* deep, cp_stats* st) {
+  if (!net || !verdict) return fail(CP_E_ARG, "null argument");
+  CP_TRY(check_level(net, level));
+  cp_engine* e = net->e;
+  cudaStream_t s = e->stream;
+  int launches = 0;
+  CP_CUDA(cudaEventRecord(e->ev0, s));
+  CP_TRY(sac_round_launches(net, level, true, launches, false, true));
+  CP_CUDA(cudaEventRecord(e->ev1, s));
+  CP_TRY(sac_round_wait(net));
+  const KStats lac = net->h_stats[1], k = net->h_stats[0];
+  const int W = net->W_user, Wi = net->W;
+  std::fill(verdict, verdict + static_cast<size_t>(net->n) * W, 0ull);
+  int cnt[2] = {0, 0};  // nwork, ndeep
+  if (!lac.inconsistent) {
+    CP_CUDA(cudaMemcpyAsync(&cnt[0], net->S.nwork, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CP_CUDA(cudaMemcpyAsync(&cnt[1], net->S.ndeep, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CP_CUDA(cudaStreamSynchronize(s));
+    std::vector<int2> work(cnt[0]);
+    std::vector<uint8_t> ok(cnt[0]);
+    if (cnt[0]) {
+      CP_CUDA(cudaMemcpyAsync(work.data(), net->S.work, cnt[0] * sizeof(int2), cudaMemcpyDeviceToHost, s));
+      CP_CUDA(cudaMemcpyAsync(ok.data(), net->S.ok, cnt[0], cudaMemcpyDeviceToHost, s));
+      CP_CUDA(cudaStreamSynchronize(s));
+    }
+    for (int i = 0; i < cnt[0]; ++i) {
+      if (!ok[i]) continue;
+      const int x = work[i].x, a = work[i].y;
+      if ((a >> 6) < W) verdict[static_cast<size_t>(x) * W + (a >> 6)] |= 1ull << (a & 63);
+    }
+  }
+  (void)Wi;
+  if (deep) *deep = (e->sac_mode == 0 && net->tile_grid > 0) ? cnt[1] : 0;
+  if (st) {
+    Acc a;
+    a.add(lac, 0);
+    a.add(k, 0);
+    a.s.inconsistent = lac.inconsistent;
+    a.s.deletions = static_cast<int64_t>(lac.deletions);
+    a.s.sweeps = lac.inconsistent ? 0 : 1;
+    a.s.launches = launches;
+    a.s.device_ms = elapsed_ms(e);
+    a.s.alg_bytes = alg_bytes(net, a, a.s.branches);
+    float kms = 0;
+    CP_CUDA(cudaEventElapsedTime(&kms, e->evk0, e->evk1));
+    a.s.kernel_ms = kms;
+    Acc ka;
+    ka.add(k, 0);
+    a.s.kernel_bytes = alg_bytes(net, ka, static_cast<int64_t>(k.branches));
+    *st = a.s;
   }
   return CP_OK;
 }

@@ -18,7 +18,11 @@
 // overlaps on the GPU (different streams, or other host threads) race on it.
 // The first call on a device looks up the array's device address
 // (cudaGetSymbolAddress) with that device current; make that first call
-// before any stream capture begins.
+// before any stream capture begins. The address is kept for the life of the
+// device's current context: a call that finds another context current (the
+// primary context was reset and re-created) looks it up again.
+#include <cuda.h>
+
 #include <cstdint>
 #include <mutex>
 #include <string>
@@ -62,6 +66,49 @@ StaticLayout static_layout(int n, int W, int nb, size_t cta_bytes) {
   L.cta = o;       o = up256(o + cta_bytes);
   L.total = o;
   return L;
+}
+
+// Exclusive prefix sum over value(0..m-1) by the whole CTA (blockDim.x a
+// multiple of 32, at most 1024): out[i] = value(0) + ... + value(i-1).
+// Returns the total to every thread; ends with the CTA synchronised.
+template <typename T, typename F>
+__device__ T cta_exclusive_scan(int m, F value, T* out) {
+  __shared__ T s_warp[32];
+  __shared__ T s_carry;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (threadIdx.x == 0) s_carry = T(0);
+  __syncthreads();
+  for (int base = 0; base < m; base += blockDim.x) {
+    const int i = base + threadIdx.x;
+    const T v = i < m ? value(i) : T(0);
+    T x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const T y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      T w = lane < nw ? s_warp[lane] : T(0);
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const T y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      s_warp[lane] = w;
+    }
+    __syncthreads();
+    const T carry = s_carry;
+    if (i < m) out[i] = carry + (warp ? s_warp[warp - 1] : T(0)) + x - v;
+    __syncthreads();
+    if (threadIdx.x == 0) s_carry = carry + s_warp[nw - 1];
+    __syncthreads();
+  }
+  // Every thread reads the total before the next scan may reset s_carry.
+  const T total = s_carry;
+  __syncthreads();
+  return total;
 }
 
 // One CTA: validates the inputs, zeroes the counters, and builds the arc
@@ -111,24 +158,15 @@ __global__ void k_static_prep(int n, int W, int nb, const int* dsize, const int*
     if (threadIdx.x == 0) st->error = CP_E_ARG;
     return;
   }
-  if (threadIdx.x == 0) {
-    int acc = 0;
-    for (int i = 0; i < n; ++i) {
-      arc_start[i] = acc;
-      acc += fill[i];
-      fill[i] = 0;
-    }
-    arc_start[n] = acc;
-    int64_t a = 0;
-    for (int c = 0; c < nb; ++c) {
-      offA[c] = a;
-      a += int64_t(dsize[bx[c]]) * W;
-    }
-    for (int c = 0; c < nb; ++c) {
-      offB[c] = a;
-      a += int64_t(dsize[by[c]]) * W;
-    }
-  }
+  // Incidence offsets and relation block offsets (A blocks of all
+  // constraints, then B blocks) by CTA-wide scans.
+  const int incidences = cta_exclusive_scan<int>(n, [&](int i) { return fill[i]; }, arc_start);
+  if (threadIdx.x == 0) arc_start[n] = incidences;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) fill[i] = 0;
+  const int64_t a_words =
+      cta_exclusive_scan<int64_t>(nb, [&](int c) { return int64_t(dsize[bx[c]]) * W; }, offA);
+  cta_exclusive_scan<int64_t>(nb, [&](int c) { return int64_t(dsize[by[c]]) * W; }, offB);
+  for (int c = threadIdx.x; c < nb; c += blockDim.x) offB[c] += a_words;
   __syncthreads();
   for (int c = threadIdx.x; c < nb; c += blockDim.x) {
     const int x = bx[c], y = by[c];
@@ -136,7 +174,6 @@ __global__ void k_static_prep(int n, int W, int nb, const int* dsize, const int*
     arcs[arc_start[x] + atomicAdd(&fill[x], 1)] = Arc{y, static_cast<u32>(offB[c]), static_cast<u32>(offA[c]), 0};
   }
   // A blocks are the caller's rows in constraint order; B blocks start zeroed.
-  const int64_t a_words = nb ? offB[0] : 0;
   const int64_t b_end = nb ? offB[nb - 1] + int64_t(dsize[by[nb - 1]]) * W : 0;
   for (int64_t i = threadIdx.x; i < a_words; i += blockDim.x) rel[i] = rows[i];
   for (int64_t i = a_words + threadIdx.x; i < b_end; i += blockDim.x) rel[i] = 0ull;
@@ -185,9 +222,37 @@ __global__ void k_static_finish(const unsigned char* scratch, StaticLayout L, in
 
 std::mutex g_static_mu;
 void* g_static_ptr[128];
+unsigned long long g_static_ctx[128];  // id of the context the address belongs to
 
-// Device address of the static array on the current device, looked up once
-// per device with that device current.
+// Unique id of the calling thread's current context (0 if none, or if the
+// driver is too old to say), through driver entry points fetched by the
+// runtime (the library does not link the driver library itself).
+unsigned long long current_context_id() {
+  using GetCurrent = CUresult (*)(CUcontext*);
+  using GetId = CUresult (*)(CUcontext, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", reinterpret_cast<void**>(&get_current), 12000,
+                                         cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      get_current = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", reinterpret_cast<void**>(&get_id), 12000,
+                                         cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      get_id = nullptr;
+  });
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
+// Device address of the static array on the current device, looked up with
+// that device current on the first call and again whenever the device's
+// current context has changed since.
 int static_scratch(unsigned char** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -200,7 +265,8 @@ int static_scratch(unsigned char** out) {
     return CP_E_UNSUPPORTED;
   }
   std::lock_guard<std::mutex> lock(g_static_mu);
-  if (!g_static_ptr[dev]) {
+  const unsigned long long ctx = current_context_id();
+  if (!g_static_ptr[dev] || (ctx && ctx != g_static_ctx[dev])) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_static_scratch);
     if (e != cudaSuccess || !p) {
@@ -208,6 +274,8 @@ int static_scratch(unsigned char** out) {
       return CP_E_CUDA;
     }
     g_static_ptr[dev] = p;
+    // The lookup makes the device's primary context current if none was.
+    g_static_ctx[dev] = ctx ? ctx : current_context_id();
   }
   *out = static_cast<unsigned char*>(g_static_ptr[dev]);
   return CP_OK;

@@ -152,6 +152,17 @@ int cp_enforce_sac1(cp_net* net, int level, cp_stats* st);
  * launch, mode 1 = one plain single-instance launch per test (the baseline). */
 int cp_singletons(cp_net* net, int level, int count, const int* vars, const int* vals, uint8_t* ok,
                   int mode, cp_stats* st);
+/* One Jacobi sweep of singleton tests, through the same kernels as the sweeps
+ * of cp_enforce_sac1: AC at `level` first (the level keeps that closure),
+ * then every live (x, a) tested against the same domains, nothing removed.
+ * The sweep of SAC1::one_pass (src/SAC1.cpp:31-55) and of the loop body of
+ * SAC1::enforce (:66-100), without their removals inside the sweep.
+ * verdict: n*W words; bit (x, a) is set iff a is in D(x) after the AC and
+ * the singleton AC fixpoint of x = a is consistent (all zero if the AC wiped
+ * a domain out: st->inconsistent = 1). deep (optional): the tests the
+ * two-round tiled kernel passed on to the general fixpoint kernel (0 where
+ * the tiled kernel does not run). */
+int cp_sac_sweep(cp_net* net, int level, uint64_t* verdict, int64_t* deep, cp_stats* st);
 
 /* ---- multi-instance batches ----------------------------------------------
  * Many independent networks (each uploaded with cp_net_upload, of any sizes)

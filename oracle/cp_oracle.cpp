@@ -471,6 +471,72 @@ int mac(const Net& N, const u64* d0, int64_t time_limit_ms, int varh, int64_t* n
   }
 }
 
+// ---------------------------------------------------------------------------
+// d-way search of GModelSolver: restates GModelSolver::Solve / Search
+// (src/GModelSolver.cu:31-189) with GModel::GetMinDomainVar
+// (src/GModel.cu:1553-1572: the first variable of smallest domain size above
+// one; -1 when every domain is a singleton). Every value of that variable in
+// increasing order opens a child level: one positive node each, one negative
+// node for each child whose GAC fixpoint wipes a domain out. The first
+// solution stops the search. The propagator is the unique AC / GAC closure.
+// ---------------------------------------------------------------------------
+struct DWay {
+  const Net& N;
+  Prop P;
+  std::chrono::steady_clock::time_point t0;
+  int64_t limit_ms, npos = 0, nneg = 0;
+  bool timed_out = false;
+  std::vector<std::vector<u64>> levels;
+  DWay(const Net& net, int64_t lim) : N(net), P(net), t0(std::chrono::steady_clock::now()), limit_ms(lim) {}
+
+  int min_domain_var(const u64* D) const {
+    int var = -1, best = 1 << 30;
+    for (int v = 0; v < N.n; ++v) {
+      const int sz = dsize(D, N.W, v);
+      if (sz > 1 && sz < best) {
+        best = sz;
+        var = v;
+      }
+    }
+    return var;
+  }
+  bool fully_assigned(const u64* D) const {
+    for (int v = 0; v < N.n; ++v)
+      if (dsize(D, N.W, v) != 1) return false;
+    return true;
+  }
+  // Returns true to stop (solution found or time out); the solution is then
+  // levels[level].
+  bool search(int level, int* solution) {
+    if (limit_ms > 0 &&
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count() >= limit_ms) {
+      timed_out = true;
+      return true;
+    }
+    const u64* D = levels[level].data();
+    const int var = min_domain_var(D);
+    if (var < 0) {
+      if (!fully_assigned(D)) return false;
+      for (int v = 0; v < N.n; ++v) solution[v] = head(D, N.W, v);
+      return true;
+    }
+    if (int(levels.size()) <= level + 1) levels.emplace_back(size_t(N.n) * N.W);
+    for (int a = 0; a < N.dom[var]; ++a) {
+      if (!have(levels[level].data(), N.W, var, a)) continue;
+      std::vector<u64>& child = levels[level + 1];
+      std::copy(levels[level].begin(), levels[level].end(), child.begin());
+      ++npos;
+      reduce_to(child.data(), N.W, var, a);
+      if (!P.enforce(child.data(), {var}, nullptr, nullptr)) {
+        ++nneg;
+        continue;
+      }
+      if (search(level + 1, solution)) return true;
+    }
+    return false;
+  }
+};
+
 bool satisfied(const Net& N, int c, const int* val) {
   if (c < N.nb) {
     const int a = val[N.scope[c][0]], b = val[N.scope[c][1]];
@@ -596,6 +662,23 @@ int orc_mac_h(const OrcNet* v, const uint64_t* dom0, int64_t time_limit_ms, int 
   return mac(N, dom0, time_limit_ms, varh, num_positive, num_negative, solution);
 }
 
+int orc_dway(const OrcNet* v, const uint64_t* dom0, int64_t time_limit_ms, int64_t* num_positive,
+             int64_t* num_negative, int* solution) {
+  Net N = build_net(v);
+  DWay S(N, time_limit_ms);
+  S.levels.emplace_back(dom0, dom0 + size_t(N.n) * N.W);
+  int status;
+  if (!S.P.enforce(S.levels[0].data(), all_vars(N.n), nullptr, nullptr)) {
+    status = 0;
+  } else {
+    const bool stop = S.search(0, solution);
+    status = S.timed_out ? 2 : (stop ? 1 : 0);
+  }
+  *num_positive = S.npos;
+  *num_negative = S.nneg;
+  return status;
+}
+
 // Lexicographic backtracking that checks each constraint once its scope is
 // fully assigned, in the spirit of the reference's BruteForceSolver
 // (samples/verify_search.cpp:26-93), capped by the size of the search space.
@@ -692,6 +775,76 @@ double orc_time_singletons(const OrcNet* v, const uint64_t* dom, int64_t count, 
   if (failed) *failed = nfail.load();
   if (done) *done = int64_t(pick.size());
   return s;
+}
+
+int64_t orc_singleton_verdicts(const OrcNet* v, const uint64_t* dom, int threads, uint64_t* verdict) {
+  Net N = build_net(v);
+  std::vector<std::pair<int, int>> live;
+  for (int x = 0; x < N.n; ++x)
+    for (int a = 0; a < N.dom[x]; ++a)
+      if (have(dom, N.W, x, a)) live.emplace_back(x, a);
+  std::vector<char> res(live.size(), 0);
+  std::atomic<size_t> next{0};
+  std::vector<std::thread> pool;
+  for (int t = 0; t < std::max(1, threads); ++t) {
+    pool.emplace_back([&]() {
+      Prop P(N);
+      std::vector<u64> tmp(size_t(N.n) * N.W);
+      std::vector<char> asg(N.n, 0);
+      for (;;) {
+        const size_t i = next.fetch_add(1);
+        if (i >= live.size()) break;
+        res[i] = singleton(N, P, dom, tmp, asg, live[i].first, live[i].second) ? 1 : 0;
+      }
+    });
+  }
+  for (auto& th : pool) th.join();
+  std::fill(verdict, verdict + size_t(N.n) * N.W, 0ull);
+  int64_t failed = 0;
+  for (size_t i = 0; i < live.size(); ++i) {
+    if (!res[i]) {
+      ++failed;
+      continue;
+    }
+    const int x = live[i].first, a = live[i].second;
+    verdict[size_t(x) * N.W + (a >> 6)] |= 1ull << (a & 63);
+  }
+  return failed;
+}
+
+// SAC closure in Jacobi order: the loop of SAC1::enforce (src/SAC1.cpp:57-103)
+// with every test of a sweep run against the sweep-start domains. Singleton
+// failure is monotone in the domains, so the greatest SAC sub-domain it
+// reaches is the one the sequential loop reaches.
+int orc_sac_jacobi(const OrcNet* v, uint64_t* dom, int threads, int64_t* deletions, int* sweeps) {
+  Net N = build_net(v);
+  Prop P(N);
+  int64_t del = 0, d = 0;
+  int sw = 0;
+  bool ok = P.enforce(dom, all_vars(N.n), nullptr, &d);
+  del += d;
+  std::vector<u64> verdict(size_t(N.n) * N.W);
+  while (ok) {
+    ++sw;
+    const int64_t failed = orc_singleton_verdicts(v, dom, threads, verdict.data());
+    if (failed == 0) break;
+    std::vector<int> evt;
+    for (int x = 0; x < N.n; ++x) {
+      bool changed = false;
+      for (int w = 0; w < N.W; ++w) {
+        const size_t i = size_t(x) * N.W + w;
+        if (dom[i] != verdict[i]) changed = true;
+        dom[i] = verdict[i];
+      }
+      if (changed) evt.push_back(x);
+    }
+    del += failed;
+    ok = P.enforce(dom, evt, nullptr, &d);
+    del += d;
+  }
+  if (deletions) *deletions = del;
+  if (sweeps) *sweeps = sw;
+  return ok ? 1 : 0;
 }
 
 double orc_time_ac(const OrcNet* v, const uint64_t* dom, int reps, int64_t* deletions) {

@@ -53,6 +53,11 @@ int orc_mac(const OrcNet* net, const uint64_t* dom0, int64_t time_limit_ms, int6
  * (-1 for any other). */
 int orc_mac_h(const OrcNet* net, const uint64_t* dom0, int64_t time_limit_ms, int varh, int64_t* num_positive,
               int64_t* num_negative, int* solution);
+/* The d-way search of GModelSolver (smallest domain above one value first,
+ * every value in order, one GAC fixpoint per child) to the first solution.
+ * status: 1 solution, 0 proved unsat, 2 time out. */
+int orc_dway(const OrcNet* net, const uint64_t* dom0, int64_t time_limit_ms, int64_t* num_positive,
+             int64_t* num_negative, int* solution);
 /* Brute force: 1 if a solution exists, 0 if none, -1 if the space exceeds limit. */
 int orc_brute_solve(const OrcNet* net, const uint64_t* dom0, double limit);
 /* 1 if the full assignment satisfies every constraint. */
@@ -64,6 +69,17 @@ int orc_singleton(const OrcNet* net, const uint64_t* dom, int x, int a);
  * number of failed tests. */
 double orc_time_singletons(const OrcNet* net, const uint64_t* dom, int64_t count, int threads,
                            int64_t* failed, int64_t* done);
+/* Every live (x, a) of dom (unchanged) tested by the singleton test above,
+ * spread over `threads` host threads: verdict (n*W words) gets bit (x, a) set
+ * iff a is in D(x) and the test is consistent. Returns the number of failed
+ * tests. */
+int64_t orc_singleton_verdicts(const OrcNet* net, const uint64_t* dom, int threads, uint64_t* verdict);
+/* The SAC closure by Jacobi sweeps on `threads` host threads: AC, then all
+ * singleton tests against the same domains, the failed values removed and AC
+ * re-run, until a sweep fails nothing. The SAC closure is unique, so dom ends
+ * where orc_sac1 (the reference's sequential order) ends. Returns 1 if
+ * consistent, 0 on wipe-out; sweeps (optional) counts the sweeps run. */
+int orc_sac_jacobi(const OrcNet* net, uint64_t* dom, int threads, int64_t* deletions, int* sweeps);
 /* Root AC (AC3bit, or GAC when tables are present) timed `reps` times on
  * fresh copies; returns the best seconds. */
 double orc_time_ac(const OrcNet* net, const uint64_t* dom, int reps, int64_t* deletions);

@@ -57,11 +57,15 @@ def lib():
         L.orc_sac1.argtypes = [PN, P64, Pi64]
         L.orc_mac.argtypes = [PN, P64, C.c_int64, Pi64, Pi64, PI]
         L.orc_mac_h.argtypes = [PN, P64, C.c_int64, C.c_int, Pi64, Pi64, PI]
+        L.orc_dway.argtypes = [PN, P64, C.c_int64, Pi64, Pi64, PI]
         L.orc_brute_solve.argtypes = [PN, P64, C.c_double]
         L.orc_check_solution.argtypes = [PN, PI]
         L.orc_singleton.argtypes = [PN, P64, C.c_int, C.c_int]
         L.orc_time_singletons.argtypes = [PN, P64, C.c_int64, C.c_int, Pi64, Pi64]
         L.orc_time_singletons.restype = C.c_double
+        L.orc_singleton_verdicts.argtypes = [PN, P64, C.c_int, P64]
+        L.orc_singleton_verdicts.restype = C.c_int64
+        L.orc_sac_jacobi.argtypes = [PN, P64, C.c_int, Pi64, PI]
         L.orc_time_ac.argtypes = [PN, P64, C.c_int, Pi64]
         L.orc_time_ac.restype = C.c_double
         L.orc_gen_binary.argtypes = [C.c_int, C.c_int, C.c_int64, C.c_double, C.c_double, C.c_double, C.c_uint64]
@@ -190,6 +194,16 @@ def mac(inst: Instance, time_limit_ms=600000, varh=1):
             "solution": sol.tolist() if st == 1 else []}
 
 
+def dway(inst: Instance, time_limit_ms=600000):
+    """GModelSolver's d-way search to the first solution."""
+    npos, nneg = C.c_int64(), C.c_int64()
+    sol = np.full(inst.n, -1, dtype=np.int32)
+    st = lib().orc_dway(C.byref(inst.view()), _ptr(inst.init, C.c_uint64), time_limit_ms, C.byref(npos),
+                        C.byref(nneg), _ptr(sol, C.c_int))
+    return {"status": st, "num_positive": npos.value, "num_negative": nneg.value,
+            "solution": sol.tolist() if st == 1 else []}
+
+
 def brute_solve(inst: Instance, limit=1e7):
     return lib().orc_brute_solve(C.byref(inst.view()), _ptr(inst.init, C.c_uint64), limit)
 
@@ -208,6 +222,24 @@ def time_singletons(inst: Instance, dom, count, threads):
     s = lib().orc_time_singletons(C.byref(inst.view()), _ptr(dom, C.c_uint64), count, threads,
                                   C.byref(failed), C.byref(done))
     return s, done.value, failed.value
+
+
+def singleton_verdicts(inst: Instance, dom, threads=0):
+    """(verdict words, failed tests): every live (x, a) of dom tested."""
+    threads = threads or (os.cpu_count() or 1)
+    d = np.ascontiguousarray(dom, dtype=np.uint64)
+    out = np.zeros(inst.n * inst.W, np.uint64)
+    f = lib().orc_singleton_verdicts(C.byref(inst.view()), _ptr(d, C.c_uint64), threads, _ptr(out, C.c_uint64))
+    return out, int(f)
+
+
+def sac_jacobi(inst: Instance, dom=None, threads=0):
+    """SAC closure by Jacobi sweeps on host threads: (ok, domains, deletions, sweeps)."""
+    threads = threads or (os.cpu_count() or 1)
+    d = (inst.init if dom is None else dom).copy()
+    dels, sw = C.c_int64(), C.c_int()
+    ok = lib().orc_sac_jacobi(C.byref(inst.view()), _ptr(d, C.c_uint64), threads, C.byref(dels), C.byref(sw))
+    return bool(ok), d, dels.value, sw.value
 
 
 def time_ac(inst: Instance, reps=3):

@@ -10,7 +10,8 @@
 //   ref_driver mixed  N D E P_LO P_HI K3 NTUP REMOVE SEED  OP [ARG]
 //   ref_driver mixedbin (same arguments as mixed; tables dropped)
 //   ref_driver uneven SEED N_LO N_HI D_CAP  OP [ARG]
-// OP: ac3bit | ac3 | sac1 | mac | time_ac REPS | time_branches K
+// OP: ac3bit | ac3 | sac1 | mac | mac_domdeg | time_ac REPS | time_branches K |
+//     verdicts [FIRST [COUNT]]
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -230,6 +231,52 @@ int main(int argc, char** argv) {
     }
     const double t1 = now_s();
     out << ", \"branches\": " << done << ", \"failed\": " << failed << ", \"seconds\": " << (t1 - t0);
+  } else if (op == "verdicts") {
+    // Root AC3bit, then the singleton test of SAC1::enforce (src/SAC1.cpp:
+    // 70-79) on every live (x, a) of the closure, in the reference's loop
+    // order, all against the same root domains (nothing is removed). Live
+    // pairs FIRST .. FIRST+COUNT-1 of that order are tested (all by default),
+    // so callers can split the work over processes. Prints the failed pairs.
+    const long first = arg;
+    const long count = (i + 2 < argc) ? std::atol(argv[i + 2]) : -1;
+    AC3bit ac(&net);
+    ConsistencyState cs;
+    {
+      Silence s;
+      cs = ac.enforce(net.vars, 0);
+    }
+    out << ", \"consistent\": " << (cs.state ? "true" : "false");
+    if (cs.state) {
+      std::vector<IntVar*> evt;
+      long idx = 0, tested = 0;
+      out << ", \"failed\": [";
+      bool firstf = true;
+      for (auto* x : net.vars) {
+        for (int a : x->values()) {
+          if (!x->have(a, 0)) continue;
+          const long k = idx++;
+          if (k < first || (count >= 0 && k >= first + count)) continue;
+          net.CopyLevel(0, net.tmp());
+          x->ReduceTo(a, net.tmp());
+          x->assign(true, net.tmp());
+          evt.push_back(x);
+          bool res;
+          {
+            Silence s;
+            res = ac.enforce(evt, net.tmp()).state;
+          }
+          evt.clear();
+          x->assign(false, 0);
+          net.ClearLevel(net.tmp());
+          ++tested;
+          if (!res) {
+            out << (firstf ? "" : ", ") << "[" << x->id() << ", " << a << "]";
+            firstf = false;
+          }
+        }
+      }
+      out << "], \"live\": " << idx << ", \"tested\": " << tested;
+    }
   } else {
     std::cerr << "unknown op " << op << std::endl;
     return 2;

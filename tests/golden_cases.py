@@ -1,6 +1,21 @@
 """Maps a golden case's generator arguments to an instance, for either the
 oracle's generator (CPU tests) or the engine's (GPU tests); both compile the
 same cpim_gb300/csrc/cp_gen.h."""
+import os
+import subprocess
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def reference_root():
+    """The reference checkout if its sources are present here ($CPIM_REFERENCE,
+    else the default oracle/ref/Makefile knows), or None."""
+    try:
+        out = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), "print-ref"],
+                             capture_output=True, text=True, timeout=60).stdout.strip()
+    except (OSError, subprocess.SubprocessError):
+        return None
+    return out or None
 
 
 def make_oracle_instance(args):

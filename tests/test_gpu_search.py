@@ -137,6 +137,37 @@ def test_gsolver_device_equals_host_driven(args):
         assert O.check_solution(oracle_view_of(inst), d["solution"])
 
 
+def test_gsolver_matches_oracle_dway(golden):
+    """cp_gsolver_solve against the oracle's restatement of GModelSolver's
+    d-way search (src/GModelSolver.cu:104-189, GetMinDomainVar
+    src/GModel.cu:1553-1572) on the networks of the MAC golden cases: the same
+    positive and negative node counts, verdict and first solution, in both
+    search modes."""
+    from oracle import pyoracle as O
+    from tests.golden_cases import oracle_view_of
+    seen, cases = set(), []
+    for c in golden:
+        if c["op"] == "mac" and tuple(c["args"]) not in seen:
+            seen.add(tuple(c["args"]))
+            cases.append(c["args"])
+    assert len(cases) >= 20
+    for mode in (0, 1):
+        with cp.Engine(0) as eng:
+            eng.set_search_mode(mode)
+            for args in cases:
+                inst = make_engine_instance(args)
+                ref = O.dway(oracle_view_of(inst), time_limit_ms=120000)
+                assert ref["status"] in (0, 1), args
+                net = eng.upload(inst)
+                r = net.gsolver_solve(time_limit_ms=120000)
+                net.close()
+                assert r["status"] == ref["status"], (args, mode)
+                assert (r["num_positive"], r["num_negative"]) == (ref["num_positive"], ref["num_negative"]), \
+                    (args, mode)
+                if r["status"] == 1:
+                    assert r["solution"] == ref["solution"], (args, mode)
+
+
 @pytest.mark.parametrize("which", ["queens8", "mixed"])
 def test_xcsp_instances_on_the_device(which):
     """Networks read from XCSP text: device GAC and MAC equal the oracle's."""

@@ -212,3 +212,55 @@ def test_sac_values_pass_singletons(seed):
                 assert O.singleton(inst, d, x, a)
     ok2, d2, dels2 = O.sac1(inst, d)
     assert ok2 and dels2 == 0 and np.array_equal(d, d2)
+
+
+def test_dway_verdicts_and_solutions(golden):
+    """The d-way restatement of GModelSolver agrees with the reference MAC's
+    verdict on every MAC golden network, and its solutions satisfy every
+    constraint."""
+    seen = set()
+    for c in golden:
+        if c["op"] != "mac" or tuple(c["args"]) in seen:
+            continue
+        seen.add(tuple(c["args"]))
+        inst = make_oracle_instance(c["args"])
+        r = O.dway(inst, time_limit_ms=60000)
+        assert r["status"] == (1 if c["result"]["num_sol"] == 1 else 0), c["args"]
+        if r["status"] == 1:
+            assert O.check_solution(inst, r["solution"])
+        assert r["num_negative"] <= r["num_positive"]
+
+
+def test_sac_jacobi_matches_reference_sac1(golden):
+    """The Jacobi-order SAC closure on host threads equals the reference's
+    sequential SAC1 on every SAC1 golden case (the closure is unique)."""
+    cases = [c for c in golden if c["op"] == "sac1"]
+    assert len(cases) >= 40
+    for c in cases:
+        inst = make_oracle_instance(c["args"])
+        ok, d, _, _ = O.sac_jacobi(inst, threads=4)
+        assert ok == c["result"]["consistent"], c["args"]
+        if ok:
+            assert O.dom_hex(d) == c["result"]["domains"], c["args"]
+
+
+def test_singleton_verdicts_match_reference(golden):
+    """Every singleton verdict over the root AC closure equals the reference's
+    own singleton test (the verdicts golden cases)."""
+    cases = [c for c in golden if c["op"] == "verdicts"]
+    assert len(cases) >= 8
+    for c in cases:
+        inst = make_oracle_instance(c["args"])
+        ok, d, _ = O.ac3bit(inst)
+        assert ok == c["result"]["consistent"], c["args"]
+        if not ok:
+            continue
+        ver, failed = O.singleton_verdicts(inst, d, threads=4)
+        got = set()
+        for x in range(inst.n):
+            for a in range(int(inst.dom[x])):
+                w = x * inst.W + a // 64
+                if (int(d[w]) >> (a % 64)) & 1 and not (int(ver[w]) >> (a % 64)) & 1:
+                    got.add((x, a))
+        assert got == set(map(tuple, c["result"]["failed"])), c["args"]
+        assert failed == len(got)

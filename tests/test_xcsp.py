@@ -9,7 +9,7 @@ import pytest
 
 from cpim_gb300.xcsp import read_xcsp
 from oracle import pyoracle as O
-from tests.golden_cases import oracle_view_of
+from tests.golden_cases import oracle_view_of, reference_root
 
 
 def _queens_xml(k):
@@ -113,7 +113,8 @@ def test_mixed_arity_unary_and_conflicts():
                 assert (int(d[x * m.inst.W + a // 64]) >> (a % 64)) & 1
 
 
-SAMPLES = "/root/reference/samples/bench"
+_REF = reference_root()
+SAMPLES = os.path.join(_REF, "samples", "bench") if _REF else ""
 
 
 @pytest.mark.skipif(not os.path.isdir(SAMPLES), reason="reference samples absent")
