@@ -28,6 +28,8 @@ import subprocess
 import sys
 from concurrent.futures import ThreadPoolExecutor
 
+import numpy as np
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
@@ -98,9 +100,145 @@ def large_cases():
     # Uneven-batch members over the whole configured range: n in [20, 400],
     # d in {8, ..., 256}, seeds 11*1000003 + i.
     for i in range(64):
-        args = ["uneven", 11 * 1000003 + i, 20, 400, 256]
-        out += [("uneven_full", args, "ac3bit"), ("uneven_full", args, "sac1")]
+        out.append(("uneven_full", ["uneven", 11 * 1000003 + i, 20, 400, 256], "sac1"))
     return out
+
+
+# The reference's Network keeps every allowed tuple of every constraint
+# (about 90 bytes each once built); cases whose estimate passes this limit are
+# computed by the oracle restatement instead (pinned against the reference on
+# the smaller cases), and say so.
+REF_BYTES_LIMIT = 16e9
+MEM_BUDGET = float(os.environ.get("GOLDEN_MEM_BUDGET", 36e9))
+
+
+def _estimate_bytes(args):
+    sys.path.insert(0, ROOT)
+    from tests.golden_cases import make_oracle_instance
+    inst = make_oracle_instance(args)
+    tuples = int(np.unpackbits(inst.brows.view(np.uint8)).sum())
+    return 90.0 * tuples + 64e6, inst
+
+
+def _oracle_case(args, op, inst):
+    from oracle import pyoracle as O
+    threads = os.cpu_count() or 4
+    if op == "sac1":
+        ok, d, dels, _ = O.sac_jacobi(inst, threads=threads)
+    elif op == "ac3bit":
+        ok, d, dels = O.ac3bit(inst)
+    else:
+        raise ValueError(op)
+    res = {"fingerprint": inst.fingerprint, "n": inst.n, "W": inst.W, "consistent": bool(ok), "deletions": int(dels),
+           "source": "oracle"}
+    if ok:
+        res["domains_sha256"] = hashlib.sha256(O.dom_hex(d).encode()).hexdigest()
+    return res
+
+
+class _MemGate:
+    """Admits jobs while the estimated memory of running jobs stays in budget
+    (a job larger than the budget runs alone)."""
+
+    def __init__(self, budget):
+        import threading
+        self.budget, self.used, self.cv = budget, 0.0, threading.Condition()
+
+    def take(self, b):
+        with self.cv:
+            while self.used > 0 and self.used + b > self.budget:
+                self.cv.wait()
+            self.used += b
+
+    def give(self, b):
+        with self.cv:
+            self.used -= b
+            self.cv.notify_all()
+
+
+def main_large():
+    import threading
+    sys.path.insert(0, ROOT)
+    from oracle import pyoracle as O
+    out_path = os.path.join(HERE, "large_cases.json")
+    part_path = out_path + ".partial"
+    done = {}
+    if os.path.exists(part_path):
+        for line in open(part_path):
+            r = json.loads(line)
+            done[(r["name"], json.dumps(r["args"]), r["op"])] = r
+    lock = threading.Lock()
+    gate = _MemGate(MEM_BUDGET)
+
+    def save(rec):
+        with lock:
+            done[(rec["name"], json.dumps(rec["args"]), rec["op"])] = rec
+            with open(part_path, "a") as f:
+                f.write(json.dumps(rec) + "\n")
+
+    def ref_job(cmd, est):
+        gate.take(est)
+        try:
+            return json.loads(subprocess.check_output([DRIVER] + cmd, timeout=14400))
+        finally:
+            gate.give(est)
+
+    def case_job(case):
+        name, args, op = case
+        if (name, json.dumps(args), op) in done:
+            return
+        est, inst = _estimate_bytes(args)
+        if est > REF_BYTES_LIMIT:
+            save({"name": name, "args": args, "op": op, "result": _oracle_case(args, op, inst)})
+            return
+        base = [str(a) for a in args]
+        if op != "verdicts":
+            res = ref_job(base + [op], est)
+            if "domains" in res:
+                res["domains_sha256"] = hashlib.sha256(res.pop("domains").encode()).hexdigest()
+            res["source"] = "reference"
+            save({"name": name, "args": args, "op": op, "result": res})
+            return
+        # Verdicts: slices of the live pairs of the root AC closure, whose size
+        # the oracle's AC3bit gives (it equals the reference's).
+        ok, d, _ = O.ac3bit(inst)
+        if not ok:
+            res = ref_job(base + ["verdicts", "0", "0"], est)
+            res["source"] = "reference"
+            save({"name": name, "args": args, "op": op, "result": res})
+            return
+        live = int(np.unpackbits(d.view(np.uint8)).sum())
+        k = max(1, min(16, int(MEM_BUDGET // est)))
+        cuts = [live * j // k for j in range(k + 1)]
+        parts = [None] * k
+
+        def one(j):
+            parts[j] = ref_job(base + ["verdicts", str(cuts[j]), str(cuts[j + 1] - cuts[j])], est)
+
+        ths = [threading.Thread(target=one, args=(j,)) for j in range(k)]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+        assert sum(p["tested"] for p in parts) == live and all(p["live"] == live for p in parts)
+        res = dict(parts[0], failed=[q for p in parts for q in p["failed"]], tested=live, source="reference")
+        save({"name": name, "args": args, "op": op, "result": res})
+
+    cs = large_cases()
+    # Longest first: the full-size SAC1 runs, then the rest.
+    order = sorted(cs, key=lambda c: (c[2] != "sac1", c[1][0] != "binary"))
+    with ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 4)) as ex:
+        list(ex.map(case_job, order))
+    results = [done[(n, json.dumps(a), o)] for n, a, o in cs]
+    with open(out_path, "w") as f:
+        json.dump({"generator": "cpim_gb300/csrc/cp_gen.h", "driver": "oracle/ref/ref_driver.cpp",
+                   "domains": "sha256 of the lowercase hex string of the n*W u64 domain words",
+                   "source": "reference: the reference's own code (oracle/ref); oracle: the restatement in oracle/, "
+                             "for networks whose tuple lists do not fit the reference's in-memory model here",
+                   "cases": results}, f, indent=0, separators=(",", ":"))
+        f.write("\n")
+    os.remove(part_path)
+    print("wrote %d cases to %s" % (len(results), out_path))
 
 
 def run(case):
@@ -108,45 +246,6 @@ def run(case):
     cmd = [DRIVER] + [str(a) for a in args] + [op]
     res = json.loads(subprocess.check_output(cmd, timeout=600))
     return {"name": name, "args": args, "op": op, "result": res}
-
-
-def run_large(case):
-    name, args, op = case
-    base = [DRIVER] + [str(a) for a in args]
-    if op != "verdicts":
-        res = json.loads(subprocess.check_output(base + [op], timeout=7200))
-        if "domains" in res:
-            res["domains_sha256"] = hashlib.sha256(res.pop("domains").encode()).hexdigest()
-        return {"name": name, "args": args, "op": op, "result": res}
-    head = json.loads(subprocess.check_output(base + ["verdicts", "0", "0"], timeout=600))
-    if not head["consistent"]:
-        return {"name": name, "args": args, "op": op, "result": head}
-    live, k = head["live"], 16
-    cuts = [live * j // k for j in range(k + 1)]
-    with ThreadPoolExecutor(max_workers=k) as ex:
-        parts = list(ex.map(lambda j: json.loads(subprocess.check_output(
-            base + ["verdicts", str(cuts[j]), str(cuts[j + 1] - cuts[j])], timeout=7200)), range(k)))
-    failed = [p for part in parts for p in part["failed"]]
-    assert sum(part["tested"] for part in parts) == live
-    res = dict(head, failed=failed, tested=live)
-    return {"name": name, "args": args, "op": op, "result": res}
-
-
-def main_large():
-    cs = large_cases()
-    # Verdict cases fan out over processes themselves; the others run
-    # single-threaded side by side, the longest first.
-    order = sorted(range(len(cs)), key=lambda j: (cs[j][2] != "sac1", cs[j][1][0] != "binary"))
-    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
-        done = dict(zip(order, ex.map(lambda j: run_large(cs[j]), order)))
-    results = [done[j] for j in range(len(cs))]
-    path = os.path.join(HERE, "large_cases.json")
-    with open(path, "w") as f:
-        json.dump({"generator": "cpim_gb300/csrc/cp_gen.h", "driver": "oracle/ref/ref_driver.cpp",
-                   "domains": "sha256 of the lowercase hex string of the n*W u64 domain words",
-                   "cases": results}, f, indent=0, separators=(",", ":"))
-        f.write("\n")
-    print("wrote %d cases to %s" % (len(results), path))
 
 
 def main():
