@@ -72,7 +72,6 @@ struct cp_engine {
   bool closed = false;
   int block_node = 256;
   int block_sac = 256;
-  int block_grid = 256;
   int chunk = 0;
   int ctas_per_sm = 0;
   int sac_mode = 0;  // 0: tiled sweep where eligible, 1: general kernel only
@@ -220,7 +219,7 @@ struct cp_net {
   int sac_grid = 0;
   int tile_grid = 0;   // persistent CTAs of the tiled sweep (0: not eligible)
   int slot_cap = 0;    // neighbours per tile held in shared memory
-  int grid_blocks = 0;
+  int front_blocks = 0;  // cooperative grid of the whole-grid fixpoint
   bool cta_in_smem = true;
   bool prefer_grid = false;
   int64_t device_bytes = 0;
@@ -325,12 +324,14 @@ int run_ac(cp_net* net, int level, const int* evt_dev, int nevt, int& launches, 
   if (!st) st = net->d_stats;
   if (net->prefer_grid) {
     cudaStream_t s = e->stream;
-    CP_CUDA(cudaMemsetAsync(net->G.qlen, 0, 12 * sizeof(int), s));  // qlen, failed, bar
-    const size_t nw = (static_cast<size_t>(net->n) + 31) / 32;
-    CP_CUDA(cudaMemsetAsync(net->G.fb[0], 0, 2 * nw * 4, s));  // both bitmaps
+    CP_CUDA(cudaMemsetAsync(net->G.flags, 0, net->G.ctl_words * sizeof(int), s));  // flags .. bitmaps
     net->G.wait_ns = e->wait_ns;
-    CP_CUDA(launch_ac_grid(net->dn, net->level_ptr(level), evt_dev, nevt_dev, evt_dev ? nevt : 0, net->G, st,
-                           e->block_grid, net->grid_blocks, s));
+    CP_CUDA(launch_ac_front(net->dn, net->level_ptr(level), evt_dev, nevt_dev, evt_dev ? nevt : 0, net->G, st,
+                            net->front_blocks, s));
+    if (!evt_dev) {  // round 0 ran as its own launch
+      ++launches;
+      ++e->launches;
+    }
   } else {
     const int op = evt_dev ? kOpEvents : kOpRoot;
     CP_CUDA(launch_node(net->dn, net->d_levels, level, level, op, 0, 0, evt_dev, nevt, st, nullptr,
@@ -443,7 +444,6 @@ int cp_engine_set_tuning(cp_engine* e, int block, int chunk, int ctas_per_sm) {
   if (block) {
     e->block_node = block;
     e->block_sac = std::min(block, 256);
-    e->block_grid = std::min(block, 512);
   }
   e->chunk = chunk;
   e->ctas_per_sm = ctas_per_sm;
@@ -562,9 +562,9 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
     for (int c = 0; c < n_bin; ++c) {
       const int x = net->bx[c], y = net->by[c];
       // Source y: revise x against y (x's rows are the A block).
-      arcs[fill[y]++] = Arc{x, static_cast<u32>(offA[c]), static_cast<u32>(offB[c]), 0};
+      arcs[fill[y]++] = Arc{x, static_cast<u32>(offA[c]), static_cast<u32>(offB[c]), y};
       // Source x: revise y against x (y's rows are the B block).
-      arcs[fill[x]++] = Arc{y, static_cast<u32>(offB[c]), static_cast<u32>(offA[c]), 0};
+      arcs[fill[x]++] = Arc{y, static_cast<u32>(offB[c]), static_cast<u32>(offA[c]), x};
     }
   }
   // Tables.
@@ -644,9 +644,6 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   int64_t max_items = 0;
   for (int x = 0; x < n; ++x) max_items += std::max(1, (arc_deg[x] + tab_deg[x] + chunk - 1) / chunk);
   if (max_items >= (int64_t(1) << 31)) return fail(CP_E_UNSUPPORTED, "too many work items");
-  // Queue offsets of every variable's items when all are seeded (root AC).
-  std::vector<int> root_base(n + 1, 0);
-  for (int x = 0; x < n; ++x) root_base[x + 1] = root_base[x] + std::max(1, (arc_deg[x] + tab_deg[x] + chunk - 1) / chunk);
   int64_t total_values = 0;
   for (int x = 0; x < n; ++x) total_values += dom[x];
 
@@ -680,8 +677,6 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   mp.add(&d_tnt, t_ntup.data(), n_tab);
   mp.add(&d_toff, t_off.data(), n_tab);
   mp.add(&d_ttup, t_tup.data(), t_tup.size());
-  int* d_root_base;
-  mp.add(&d_root_base, root_base.data(), n + 1);
   mp.add(&net->d_bx, net->bx.data(), n_bin);
   mp.add(&net->d_by, net->by.data(), n_bin);
   mp.add(&net->d_offA, offA.data(), n_bin);
@@ -708,26 +703,21 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   D.t_ntup = d_tnt;
   D.t_off = d_toff;
   D.t_tup = d_ttup;
-  net->G.root_base = d_root_base;
 
   // Scratch.
   const size_t nw = (static_cast<size_t>(n) + 31) / 32;
   GridScratch& G = net->G;
-  CP_TRY(net->alloc(&G.q[0], max_items));
-  CP_TRY(net->alloc(&G.q[1], max_items));
-  CP_TRY(net->alloc(&G.fb[0], 2 * nw));  // both bitmaps: cleared by one memset
-  G.fb[1] = G.fb[0] + nw;
   {
-    int* ctl;  // qlen[4] | failed[2] + pad | bar[2]: cleared by one memset
-    CP_TRY(net->alloc(&ctl, 12));
-    G.qlen = ctl;
+    // flags[3] + pad | failed[2] + pad | bar[2] + pad | three bitmaps:
+    // cleared by one memset before each launch.
+    G.ctl_words = 12 + 3 * nw;
+    int* ctl;
+    CP_TRY(net->alloc(&ctl, G.ctl_words));
+    G.flags = ctl;
     G.failed = ctl + 4;
     G.bar = reinterpret_cast<unsigned*>(ctl + 8);
+    G.bm = reinterpret_cast<u32*>(ctl + 12);
   }
-  CP_TRY(net->alloc(&G.tstamp, std::max(1, n_tab)));
-  CP_TRY(net->alloc(&G.epoch, 4));
-  CP_CUDA(cudaMemsetAsync(G.tstamp, 0, std::max(1, n_tab) * sizeof(int), s));
-  CP_CUDA(cudaMemsetAsync(G.epoch, 0, 4 * sizeof(int), s));
   SacScratch& S = net->S;
   CP_TRY(net->alloc(&S.work, total_values));
   CP_TRY(net->alloc(&S.ok, total_values));
@@ -786,8 +776,8 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
     CP_TRY(net->alloc(&p, net->sac_stride * net->sac_grid));
     net->d_sac_scratch = p;
   }
-  net->grid_blocks = ac_grid_max_blocks(D, e->block_grid, e->sm_count);
-  if (net->grid_blocks < 1) return fail(CP_E_UNSUPPORTED, "grid fixpoint kernel does not fit");
+  net->front_blocks = ac_front_blocks(D, static_cast<int>(arcs.size()), e->sm_count);
+  if (net->front_blocks < 1) return fail(CP_E_UNSUPPORTED, "grid fixpoint kernel does not fit");
   // Tiled SAC sweep (binary networks): shared memory holds the round-one
   // domains of up to slot_cap neighbours for 32 branches, plus a slot map.
   for (int x = 0; x < n; ++x) net->max_deg = std::max(net->max_deg, arc_deg[x]);
@@ -1059,8 +1049,8 @@ int sac_round(cp_net* net, int level, bool root, int& launches) {
   cudaStream_t s = e->stream;
   if (!e->sac_graphs || net->sac_graph_off || !(root || net->prefer_grid))
     return sac_round_launches(net, level, root, launches, false);
-  const std::array<int64_t, 10> key = {level, e->sac_mode, e->block_sac, e->block_grid, e->block_node,
-                                       net->sac_grid, net->tile_grid, net->slot_cap, net->grid_blocks, e->wait_ns};
+  const std::array<int64_t, 10> key = {level, e->sac_mode, e->block_sac, e->chunk, e->block_node,
+                                       net->sac_grid, net->tile_grid, net->slot_cap, net->front_blocks, e->wait_ns};
   if (key != net->sac_key) {
     net->drop_sac_graphs();
     net->sac_key = key;

@@ -42,7 +42,7 @@ struct Arc {
   int z;        // variable revised
   u32 zy;       // word offset of z's rows (value-wise revise)
   u32 yz;       // word offset of y's rows (union-of-supports revise)
-  int pad;
+  int src;      // y, the variable whose incidence list holds the arc
 };
 
 struct DevNet {
@@ -80,16 +80,14 @@ struct KStats {
   int pad[3];
 };
 
-// Global-memory state of the grid-wide fixpoint (one per network).
+// Global-memory state of the grid-wide fixpoint (one per network): one block
+// of ctl_words ints cleared by one memset before each launch.
 struct GridScratch {
-  u32* q[2];          // work queues, max_items each
-  u32* fb[2];         // dedupe bitmaps, ceil(n/32) words each (one block)
-  const int* root_base;  // [n+1] first work item of each variable when all are seeded
-  int* qlen;          // [3] rotating queue lengths; qlen, failed, bar share one block
-  int* tstamp;        // [nt] round stamp of the last table revision
-  int* epoch;         // [1] stamp base carried across calls
-  int* failed;        // [1]
+  int* flags;         // [3] bitmap i has a bit set
+  int* failed;        // [2] wipe-out seen, by round parity
   unsigned* bar;      // [2] grid barrier: count, generation
+  u32* bm;            // [3][ceil(n/32)] frontier bitmaps
+  size_t ctl_words;   // size of the block starting at flags
   long long wait_ns;  // longest wait of a block at the grid barrier
 };
 
@@ -216,11 +214,14 @@ size_t cta_state_bytes(const DevNet& N);
 cudaError_t launch_node(const DevNet& N, u64* levels, int src, int dst, int op, int var, int val,
                         const int* evt, int nevt, KStats* st, uint8_t* ok_out, int block, void* gscratch,
                         cudaStream_t s);
-// Grid-wide persistent fixpoint at level `level`, seeded with evt (or all
-// variables when evt == nullptr).
-cudaError_t launch_ac_grid(const DevNet& N, u64* level_dom, const int* evt, const int* nevt_dev, int nevt,
-                           GridScratch G, KStats* st, int block, int grid, cudaStream_t s);
-int ac_grid_max_blocks(const DevNet& N, int block, int sm_count);
+// Grid-wide fixpoint at level `level`, seeded with evt (or all variables when
+// evt == nullptr), the frontier kept in bitmaps (k_ac_front); the GridScratch
+// block must be zero on entry. Without evt, round 0 is a plain launch before
+// the cooperative one (two launches). ac_front_blocks: the cooperative grid
+// for a network with narcs binary incidences (0 if the kernel does not fit).
+cudaError_t launch_ac_front(const DevNet& N, u64* level_dom, const int* evt, const int* nevt_dev, int nevt,
+                            GridScratch G, KStats* st, int grid, cudaStream_t s);
+int ac_front_blocks(const DevNet& N, int narcs, int sm_count);
 // Persistent batched singleton tests: pairs work[0..*nwork), results in ok.
 // With idx != nullptr the tests are work[idx[i]] for i < *nidx.
 cudaError_t launch_sac_branches(const DevNet& N, const u64* root, const int2* work, const int* nwork, int* cursor,

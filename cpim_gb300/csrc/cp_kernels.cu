@@ -7,11 +7,13 @@
 //   - k_sac:   persistent CTAs pull SAC singleton branches (x, a) from a
 //              device work list; each branch gets its own domain copy in the
 //              CTA's shared memory, only a 1-byte verdict leaves the SM;
-//   - k_ac_grid: the whole grid runs one fixpoint on global-memory domains
-//              under a bounded grid barrier (cooperative launch).
+//   - k_ac_front: the whole grid runs one fixpoint on global-memory domains
+//              under a bounded grid barrier (cooperative launch), the
+//              frontier kept as bitmaps instead of a queue.
 //
-// Frontier: a queue of work items (variable y, chunk of y's incidences) plus a
-// bitmap that admits each changed variable once per round. Round r processes
+// Frontier of the CTA-local fixpoints: a queue of work items (variable y,
+// chunk of y's incidences) plus a bitmap that admits each changed variable
+// once per round. Round r processes
 // queue r&1 and appends to the other; a variable's bit in the current bitmap
 // is cleared by the warp that takes its first chunk, so both bitmaps are clean
 // at every round boundary without a clearing pass.
@@ -172,7 +174,7 @@ __device__ __forceinline__ void seed_var(const DevNet& N, const Fix& F, int z) {
 
 // Removes rm (warp-uniform) from D(z); on a change, checks for wipe-out and
 // admits z to the next round.
-template <int WT, bool kGlobal>
+template <int WT>
 __device__ __forceinline__ void commit(const DevNet& N, const Fix& F, u32* qn, u32* fbn, int* qlenn, int slot, int z,
                                        const u64 (&rm)[WT], Cnt& cn) {
   const int lane = threadIdx.x & 31;
@@ -190,10 +192,7 @@ __device__ __forceinline__ void commit(const DevNet& N, const Fix& F, u32* qn, u
   }
   if (__ballot_sync(kFull, newly != 0) == 0) return;
   cn.dels += __popcll(newly);
-  if (kGlobal)
-    __threadfence();
-  else
-    __threadfence_block();
+  __threadfence_block();
   const u64 cur = (lane < WT) ? vload(F.D + static_cast<size_t>(z) * WT + lane) : 0ull;
   const bool nonempty = __ballot_sync(kFull, cur != 0) != 0;
   if (lane == 0) {
@@ -204,9 +203,70 @@ __device__ __forceinline__ void commit(const DevNet& N, const Fix& F, u32* qn, u
   }
 }
 
-// Revises z against y along arc A; dy / cy: D(y) and its size, read by the
-// caller once per work item.
-template <int WT, bool kGlobal>
+// Values of D(z) without a support in D(y) along arc A (dy, dz warp-uniform),
+// from the union of the supports (in z) of the live values of y, 32 rows per
+// step; stops as soon as the union covers D(z) (nothing to remove). The side
+// to take when y has fewer live values than z.
+template <int WT>
+__device__ __forceinline__ void union_removals(const DevNet& N, const Arc A, const u64 (&dy)[WT], const u64 (&dz)[WT],
+                                               u64 (&rm)[WT], Cnt& cn) {
+  const int lane = threadIdx.x & 31;
+  u64 acc[WT], cov[WT];
+#pragma unroll
+  for (int w = 0; w < WT; ++w) acc[w] = cov[w] = 0;
+  int loaded = 0;
+  bool covered = false;
+#pragma unroll
+  for (int base = 0; base < 64 * WT; base += 32) {
+    if (covered) break;
+    const u32 bits = static_cast<u32>(dy[base >> 6] >> (base & 32));
+    if (bits == 0) continue;
+    if ((bits >> lane) & 1u) {
+      u64 r[WT];
+      load_row<WT>(N.rel, A.yz + static_cast<size_t>(base + lane) * WT, r);
+#pragma unroll
+      for (int w = 0; w < WT; ++w) acc[w] |= r[w];
+    }
+    loaded += __popc(bits);
+    u64 gap = 0;
+#pragma unroll
+    for (int w = 0; w < WT; ++w) {
+      cov[w] = warp_or64(acc[w]);
+      gap |= dz[w] & ~cov[w];
+    }
+    covered = gap == 0;
+  }
+#pragma unroll
+  for (int w = 0; w < WT; ++w) rm[w] = dz[w] & ~cov[w];
+  if (lane == 0) cn.rows += loaded;
+}
+
+// Value-wise removals: every live value of z tests its support row against
+// D(y), one group of 32 values at a time.
+template <int WT>
+__device__ __forceinline__ void valuewise_removals_seq(const DevNet& N, u32 zy, const u64 (&dy)[WT],
+                                                       const u64 (&dz)[WT], u64 (&rm)[WT]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int base = 0; base < 64 * WT; base += 32) {
+    const u32 bits = static_cast<u32>(dz[base >> 6] >> (base & 32));
+    if (bits == 0) continue;
+    bool unsup = false;
+    if ((bits >> lane) & 1u) {
+      u64 r[WT];
+      load_row<WT>(N.rel, zy + static_cast<size_t>(base + lane) * WT, r);
+      u64 hit = 0;
+#pragma unroll
+      for (int w = 0; w < WT; ++w) hit |= r[w] & dy[w];
+      unsup = hit == 0;
+    }
+    const u32 m = __ballot_sync(kFull, unsup);
+    rm[base >> 6] |= static_cast<u64>(m) << (base & 32);
+  }
+}
+
+// Revises z against y along arc A; dy / cy: D(y) and its size.
+template <int WT>
 __device__ __forceinline__ void revise_arc(const DevNet& N, const Fix& F, u32* qn, u32* fbn, int* qlenn, int slot,
                                            int y, const u64 (&dy)[WT], int cy, const Arc A, Cnt& cn) {
   const int lane = threadIdx.x & 31;
@@ -225,86 +285,12 @@ __device__ __forceinline__ void revise_arc(const DevNet& N, const Fix& F, u32* q
 #pragma unroll
   for (int w = 0; w < WT; ++w) rm[w] = 0;
   if (cy < cz) {
-    // Union of the supports (in z) of the live values of y, 32 rows per
-    // step; stops as soon as the union covers D(z) (nothing to remove).
-    u64 acc[WT], cov[WT];
-#pragma unroll
-    for (int w = 0; w < WT; ++w) acc[w] = cov[w] = 0;
-    int loaded = 0;
-    bool covered = false;
-#pragma unroll
-    for (int base = 0; base < 64 * WT; base += 32) {
-      if (covered) break;
-      const u32 bits = static_cast<u32>(dy[base >> 6] >> (base & 32));
-      if (bits == 0) continue;
-      if ((bits >> lane) & 1u) {
-        u64 r[WT];
-        load_row<WT>(N.rel, A.yz + static_cast<size_t>(base + lane) * WT, r);
-#pragma unroll
-        for (int w = 0; w < WT; ++w) acc[w] |= r[w];
-      }
-      loaded += __popc(bits);
-      u64 gap = 0;
-#pragma unroll
-      for (int w = 0; w < WT; ++w) {
-        cov[w] = warp_or64(acc[w]);
-        gap |= dz[w] & ~cov[w];
-      }
-      covered = gap == 0;
-    }
-#pragma unroll
-    for (int w = 0; w < WT; ++w) rm[w] = dz[w] & ~cov[w];
-    if (lane == 0) cn.rows += loaded;
+    union_removals<WT>(N, A, dy, dz, rm, cn);
   } else {
-    // Every live value of z tests its support row against D(y); in the
-    // global-memory fixpoint with domains up to 128 values all rows are loaded
-    // before any is tested (elsewhere group by group: the registers are
-    // needed).
-    constexpr int kVG = (kGlobal && WT <= 2) ? 2 * WT : 1;
-    if constexpr (kVG > 1) {
-      u64 r[kVG][WT];
-      bool live[kVG];
-#pragma unroll
-      for (int g = 0; g < kVG; ++g) {
-        const int base = g * 32;
-        live[g] = (dz[base >> 6] >> ((base & 32) + lane)) & 1ull;
-        if (live[g]) {
-          load_row<WT>(N.rel, A.zy + static_cast<size_t>(base + lane) * WT, r[g]);
-        } else {
-#pragma unroll
-          for (int w = 0; w < WT; ++w) r[g][w] = 0;
-        }
-      }
-#pragma unroll
-      for (int g = 0; g < kVG; ++g) {
-        const int base = g * 32;
-        u64 hit = 0;
-#pragma unroll
-        for (int w = 0; w < WT; ++w) hit |= r[g][w] & dy[w];
-        const u32 m = __ballot_sync(kFull, live[g] && hit == 0);
-        rm[base >> 6] |= static_cast<u64>(m) << (base & 32);
-      }
-    } else {
-#pragma unroll
-      for (int base = 0; base < 64 * WT; base += 32) {
-        const u32 bits = static_cast<u32>(dz[base >> 6] >> (base & 32));
-        if (bits == 0) continue;
-        bool unsup = false;
-        if ((bits >> lane) & 1u) {
-          u64 r[WT];
-          load_row<WT>(N.rel, A.zy + static_cast<size_t>(base + lane) * WT, r);
-          u64 hit = 0;
-#pragma unroll
-          for (int w = 0; w < WT; ++w) hit |= r[w] & dy[w];
-          unsup = hit == 0;
-        }
-        const u32 m = __ballot_sync(kFull, unsup);
-        rm[base >> 6] |= static_cast<u64>(m) << (base & 32);
-      }
-    }
+    valuewise_removals_seq<WT>(N, A.zy, dy, dz, rm);
     if (lane == 0) cn.rows += cz;
   }
-  commit<WT, kGlobal>(N, F, qn, fbn, qlenn, slot, z, rm, cn);
+  commit<WT>(N, F, qn, fbn, qlenn, slot, z, rm, cn);
 }
 
 // Table revision (GAC on a positive table, the definition of
@@ -312,72 +298,92 @@ __device__ __forceinline__ void revise_arc(const DevNet& N, const Fix& F, u32* q
 // in its variable's domain; each scope variable keeps exactly the values that
 // appear in a valid tuple. Lanes stride over tuples, projections are OR-reduced
 // across the warp.
-template <int WT, bool kGlobal>
+// Table t against the current domains D: rm[i] = the values of scope
+// position i that appear in no valid tuple (s[i]: the scope, r: the arity).
+// Returns a scope variable found empty (nothing computed then), or -1.
+template <int WT>
+__device__ __forceinline__ int table_removals(const DevNet& N, const u64* D, int t, int (&s)[kMaxArity], int& r,
+                                              u64 (&rm)[kMaxArity][WT], Cnt& cn) {
+  const int lane = threadIdx.x & 31;
+  r = N.t_arity[t];
+  u64 snap[kMaxArity][WT], proj[kMaxArity][WT];
+  int empty_var = -1;
+#pragma unroll
+  for (int i = 0; i < kMaxArity; ++i) {
+    s[i] = i < r ? N.t_scope[t * kMaxArity + i] : 0;
+    u64 any = 0;
+    if (i < r) {
+      load_dom_uniform<WT>(D + static_cast<size_t>(s[i]) * WT, snap[i]);
+    } else {
+#pragma unroll
+      for (int w = 0; w < WT; ++w) snap[i][w] = 0;
+    }
+#pragma unroll
+    for (int w = 0; w < WT; ++w) {
+      proj[i][w] = 0;
+      rm[i][w] = 0;
+      any |= snap[i][w];
+    }
+    if (i < r && any == 0) empty_var = s[i];
+  }
+  if (lane == 0) ++cn.rev;
+  if (empty_var >= 0) return empty_var;
+  const int nt = N.t_ntup[t];
+  const uint16_t* tp = N.t_tup + N.t_off[t];
+  // Four tuples per lane per step, all coordinates loaded before any test.
+  constexpr int kU = 4;
+  for (int k0 = lane; k0 < nt; k0 += 32 * kU) {
+    int v[kU][kMaxArity];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int k = k0 + 32 * u;
+#pragma unroll
+      for (int i = 0; i < kMaxArity; ++i) v[u][i] = (i < r && k < nt) ? tp[static_cast<size_t>(i) * nt + k] : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      bool valid = k0 + 32 * u < nt;
+#pragma unroll
+      for (int i = 0; i < kMaxArity; ++i)
+        if (i < r) valid = valid && ((sel<WT>(snap[i], v[u][i] >> 6) >> (v[u][i] & 63)) & 1ull);
+      if (valid) {
+#pragma unroll
+        for (int i = 0; i < kMaxArity; ++i)
+          if (i < r) or_at<WT>(proj[i], v[u][i] >> 6, 1ull << (v[u][i] & 63));
+      }
+    }
+  }
+  if (lane == 0) cn.tuples += nt;
+#pragma unroll
+  for (int i = 0; i < kMaxArity; ++i)
+    if (i < r) {
+#pragma unroll
+      for (int w = 0; w < WT; ++w) rm[i][w] = snap[i][w] & ~warp_or64(proj[i][w]);
+    }
+  return -1;
+}
+
+template <int WT>
 __device__ __forceinline__ void revise_table(const DevNet& N, const Fix& F, u32* qn, u32* fbn, int* qlenn, int slot,
                                              int t, Cnt& cn) {
   if constexpr (WT > 4) {
     return;  // tables are rejected at upload for domains wider than 256 values
   } else {
     const int lane = threadIdx.x & 31;
-    const int r = N.t_arity[t];
-    int s[kMaxArity];
-    u64 snap[kMaxArity][WT], proj[kMaxArity][WT];
-    int empty_var = -1;
-#pragma unroll
-    for (int i = 0; i < kMaxArity; ++i) {
-      s[i] = i < r ? N.t_scope[t * kMaxArity + i] : 0;
-      u64 any = 0;
-      if (i < r) {
-        load_dom_uniform<WT>(F.D + static_cast<size_t>(s[i]) * WT, snap[i]);
-      } else {
-#pragma unroll
-        for (int w = 0; w < WT; ++w) snap[i][w] = 0;
-      }
-#pragma unroll
-      for (int w = 0; w < WT; ++w) {
-        proj[i][w] = 0;
-        any |= snap[i][w];
-      }
-      if (i < r && any == 0) empty_var = s[i];
-    }
-    if (lane == 0) ++cn.rev;
+    int s[kMaxArity], r = 0;
+    u64 rm[kMaxArity][WT];
+    const int empty_var = table_removals<WT>(N, F.D, t, s, r, rm, cn);
     if (empty_var >= 0) {
       if (lane == 0) set_failed(F, slot, empty_var);
       return;
     }
-    const int nt = N.t_ntup[t];
-    const uint16_t* tp = N.t_tup + N.t_off[t];
-    for (int k = lane; k < nt; k += 32) {
-      int v[kMaxArity];
-      bool valid = true;
 #pragma unroll
-      for (int i = 0; i < kMaxArity; ++i) {
-        v[i] = 0;
-        if (i < r) {
-          v[i] = tp[static_cast<size_t>(i) * nt + k];
-          valid = valid && ((sel<WT>(snap[i], v[i] >> 6) >> (v[i] & 63)) & 1ull);
-        }
-      }
-      if (valid) {
-#pragma unroll
-        for (int i = 0; i < kMaxArity; ++i)
-          if (i < r) or_at<WT>(proj[i], v[i] >> 6, 1ull << (v[i] & 63));
-      }
-    }
-    if (lane == 0) cn.tuples += nt;
-#pragma unroll
-    for (int i = 0; i < kMaxArity; ++i) {
-      if (i < r) {
-        u64 rm[WT];
-#pragma unroll
-        for (int w = 0; w < WT; ++w) rm[w] = snap[i][w] & ~warp_or64(proj[i][w]);
-        commit<WT, kGlobal>(N, F, qn, fbn, qlenn, slot, s[i], rm, cn);
-      }
-    }
+    for (int i = 0; i < kMaxArity; ++i)
+      if (i < r) commit<WT>(N, F, qn, fbn, qlenn, slot, s[i], rm[i], cn);
   }
 }
 
-template <int WT, bool kTab, bool kGlobal>
+template <int WT, bool kTab>
 __device__ __forceinline__ void process_item(const DevNet& N, const Fix& F, u32 item, u32* fbc, u32* qn, u32* fbn,
                                              int* qlenn, int slot, int stamp, Cnt& cn) {
   const int lane = threadIdx.x & 31;
@@ -388,42 +394,16 @@ __device__ __forceinline__ void process_item(const DevNet& N, const Fix& F, u32 
   const int t0 = N.tinc_start[y], dt = N.tinc_start[y + 1] - t0;
   const int lo = c * N.chunk;
   const int hi = min(lo + N.chunk, da + dt);
-  const int hb = min(hi, da);  // binary arcs of this item: [lo, hb)
-  // Global-memory fixpoints with domains up to 256 values read D(y) once per
-  // item (these revisions change other variables only; a change of D(y) by
-  // another warp queues y again) and read the next arc's record while the
-  // current one is revised. The CTA-local fixpoints (shared-memory domains,
-  // short latencies) and the widest domains read both per arc and keep the
-  // registers.
-  constexpr bool kHoist = kGlobal && WT <= 4;
-  u64 dy[WT];
-  int cy = 0;
-  Arc nxt{};
-  if constexpr (kHoist) {
-    if (lo < hb) {
-      load_dom_uniform<WT>(F.D + static_cast<size_t>(y) * WT, dy);
-#pragma unroll
-      for (int w = 0; w < WT; ++w) cy += __popcll(dy[w]);
-      nxt = N.arcs[a0 + lo];
-    }
-  }
   for (int i = lo; i < hi; ++i) {
     if (i < da) {
-      if constexpr (kHoist) {
-        const Arc A = nxt;
-        if (i + 1 < hb) nxt = N.arcs[a0 + i + 1];
-        if (any_failed(F)) return;
-        revise_arc<WT, kGlobal>(N, F, qn, fbn, qlenn, slot, y, dy, cy, A, cn);
-      } else {
-        if (any_failed(F)) return;
-        const Arc A = N.arcs[a0 + i];
-        u64 dyl[WT];
-        load_dom_uniform<WT>(F.D + static_cast<size_t>(y) * WT, dyl);
-        int cyl = 0;
+      if (any_failed(F)) return;
+      const Arc A = N.arcs[a0 + i];
+      u64 dy[WT];
+      load_dom_uniform<WT>(F.D + static_cast<size_t>(y) * WT, dy);
+      int cy = 0;
 #pragma unroll
-        for (int w = 0; w < WT; ++w) cyl += __popcll(dyl[w]);
-        revise_arc<WT, kGlobal>(N, F, qn, fbn, qlenn, slot, y, dyl, cyl, A, cn);
-      }
+      for (int w = 0; w < WT; ++w) cy += __popcll(dy[w]);
+      revise_arc<WT>(N, F, qn, fbn, qlenn, slot, y, dy, cy, A, cn);
     } else if constexpr (kTab) {
       if (any_failed(F)) return;
       const int t = N.vtab[t0 + i - da];
@@ -431,7 +411,7 @@ __device__ __forceinline__ void process_item(const DevNet& N, const Fix& F, u32 
       if (lane == 0) prev = atomicMax(F.tstamp + t, stamp);
       prev = __shfl_sync(kFull, prev, 0);
       if (prev >= stamp) continue;
-      revise_table<WT, kGlobal>(N, F, qn, fbn, qlenn, slot, t, cn);
+      revise_table<WT>(N, F, qn, fbn, qlenn, slot, t, cn);
     }
   }
 }
@@ -459,7 +439,7 @@ __device__ int cta_fixpoint(const DevNet& N, const Fix& F, Cnt& cn, int* err) {
     u32* fbn = cur ? F.fb0 : F.fb1;
     int* qlenn = F.qlen + (r + 1) % 3;
     for (int j = warp; j < len; j += nwarps)
-      process_item<WT, kTab, false>(N, F, qc[j], fbc, qn, fbn, qlenn, cur ^ 1, F.stamp_base + r + 1, cn);
+      process_item<WT, kTab>(N, F, qc[j], fbc, qn, fbn, qlenn, cur ^ 1, F.stamp_base + r + 1, cn);
     __syncthreads();
   }
   return r;
@@ -1080,7 +1060,7 @@ __global__ void __launch_bounds__(256) k_sac(DevNet N, const u64* root, const in
 }
 
 // ---------------------------------------------------------------------------
-// k_ac_grid: whole-grid fixpoint with a bounded grid barrier.
+// Whole-grid fixpoints: a bounded grid barrier.
 // ---------------------------------------------------------------------------
 // Sense-free generation barrier; every block waits at most wait_ns, then
 // reports CP_E_TIMEOUT through *err and returns false (a block that sees
@@ -1118,62 +1098,348 @@ __device__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* err, long lon
   return s_ok != 0;
 }
 
-template <int WT, bool kTab>
-__global__ void __launch_bounds__(512) k_ac_grid(DevNet N, u64* D, const int* evt, const int* nevt_dev, int nevt,
-                                                 GridScratch G, KStats* st) {
+// ---------------------------------------------------------------------------
+// k_ac_front: the whole grid runs one fixpoint on global-memory domains, the
+// frontier kept as bitmaps of changed variables (no work queue, no appends).
+// Round r reads bitmap r%3 (the variables changed in round r-1), marks the
+// variables it changes in bitmap (r+1)%3 and clears bitmap (r+2)%3, which
+// round r+1 will write; flag[i] says that bitmap i has a bit set. A round's
+// work is static: the binary incidences (arcs out of y, CSR by y) in groups
+// of K, then the tables. A warp takes a group, tests the frontier bits of the
+// group's source variables (one ballot: the active arcs, compacted by their
+// rank in the ballot mask), reads D(y) and D(z) of all of them at once and
+// then the support rows of all active arcs in one wave before testing any,
+// so each warp keeps K revisions' loads in flight instead of one. A table is
+// revised once per round when any of its scope variables changed. Warp w
+// takes tasks w, w + W, ... and reads its next group's records while working
+// on the current one. Failures of round r go to failed[(r+1)&1], which nobody
+// writes during round r+1, so every block takes the same decision at the top
+// of a round. Round 0 of a root fixpoint, where every variable is in the
+// frontier, runs as a plain launch with one warp per task (k_front_first);
+// the cooperative kernel then starts at round 1 and ends at once if round 0
+// changed nothing.
+// ---------------------------------------------------------------------------
+template <int WT>
+struct FrontGroup {
+  static constexpr int K = WT == 1 ? 8 : (WT == 2 ? 4 : 1);
+};
+constexpr int kFrontBlock = 256;
+
+__device__ __forceinline__ bool front_bit(const u32* bm, int v) { return (__ldcg(bm + (v >> 5)) >> (v & 31)) & 1u; }
+
+// Removes rm (warp-uniform) from D(z); on a change, checks for wipe-out and
+// marks z in the next frontier bitmap.
+template <int WT>
+__device__ __forceinline__ void commit_front(const Fix& F, u32* bn, int* fn, int slot, int z, const u64 (&rm)[WT],
+                                             Cnt& cn) {
+  const int lane = threadIdx.x & 31;
+  bool any = false;
+#pragma unroll
+  for (int w = 0; w < WT; ++w) any |= rm[w] != 0;
+  if (!any) return;
+  bool emptied;
+  if constexpr (WT == 1) {
+    // One word: the atomic's old value says whether this removal emptied it.
+    u64 old = 0;
+    if (lane == 0) old = atomicAnd(F.D + z, ~rm[0]);
+    old = shfl64(old, 0);
+    const u64 newly = old & rm[0];
+    if (!newly) return;
+    if (lane == 0) cn.dels += __popcll(newly);
+    emptied = (old & ~rm[0]) == 0;
+  } else {
+    u64 newly = 0;
+    if (lane < WT) {
+      const u64 r = sel<WT>(rm, lane);
+      if (r) newly = atomicAnd(F.D + static_cast<size_t>(z) * WT + lane, ~r) & r;
+    }
+    if (__ballot_sync(kFull, newly != 0) == 0) return;
+    cn.dels += __popcll(newly);
+    __threadfence();
+    const u64 cur = (lane < WT) ? vload(F.D + static_cast<size_t>(z) * WT + lane) : 0ull;
+    emptied = __ballot_sync(kFull, cur != 0) == 0;
+  }
+  if (lane == 0) {
+    if (emptied) {
+      set_failed(F, slot, z);
+    } else {
+      const u32 bit = 1u << (z & 31);
+      if (!(atomicOr(bn + (z >> 5), bit) & bit)) atomicExch(fn, 1);
+    }
+  }
+}
+
+// One group of up to K binary incidences: lane k < cnt holds incidence k's
+// record A (read ahead by the caller). all: every variable is in the
+// frontier (round 0 of a root fixpoint), no bitmap test (bc unused).
+template <int WT>
+__device__ __forceinline__ void front_group(const DevNet& N, const Fix& F, const Arc A, int cnt, bool all,
+                                            const u32* bc, u32* bn, int* fn, int slot, Cnt& cn) {
+  constexpr int K = FrontGroup<WT>::K;
+  const int lane = threadIdx.x & 31;
+  // D(y) and D(z) of each active incidence, lane k holding incidence k's.
+  u64 dyL[WT], dzL[WT];
+#pragma unroll
+  for (int w = 0; w < WT; ++w) dyL[w] = dzL[w] = 0;
+  const bool act = lane < cnt && (all || front_bit(bc, A.src));
+  const u32 m = __ballot_sync(kFull, act);
+  if (!m || any_failed(F)) return;
+  if (act) {
+#pragma unroll
+    for (int w = 0; w < WT; ++w) {
+      dyL[w] = vload(F.D + static_cast<size_t>(A.src) * WT + w);
+      dzL[w] = vload(F.D + static_cast<size_t>(A.z) * WT + w);
+    }
+  }
+  if constexpr (WT <= 2) {
+    constexpr int kVG = 2 * WT;  // groups of 32 values of z
+    u64 rows[K][kVG][WT];
+    // The rows of z's live values of every active arc revised value-wise
+    // (y has at least as many live values as z), all issued before any test.
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      u64 dz[WT];
+      int cz = 0, cy = 0;
+#pragma unroll
+      for (int w = 0; w < WT; ++w) {
+        dz[w] = shfl64(dzL[w], k);
+        cz += __popcll(dz[w]);
+        cy += __popcll(shfl64(dyL[w], k));
+      }
+      const u32 zy = __shfl_sync(kFull, A.zy, k);
+      const bool vw = ((m >> k) & 1u) && cy >= cz && cz > 0;
+#pragma unroll
+      for (int g = 0; g < kVG; ++g) {
+        const bool live = vw && ((dz[g >> 1] >> ((g & 1) * 32 + lane)) & 1ull);
+        if (live) {
+          load_row<WT>(N.rel, zy + static_cast<size_t>(g * 32 + lane) * WT, rows[k][g]);
+        } else {
+#pragma unroll
+          for (int w = 0; w < WT; ++w) rows[k][g][w] = 0;
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      if (!((m >> k) & 1u)) continue;
+      u64 dz[WT], dy[WT], rm[WT];
+      int cz = 0, cy = 0;
+#pragma unroll
+      for (int w = 0; w < WT; ++w) {
+        dz[w] = shfl64(dzL[w], k);
+        dy[w] = shfl64(dyL[w], k);
+        cz += __popcll(dz[w]);
+        cy += __popcll(dy[w]);
+        rm[w] = 0;
+      }
+      const Arc Ak{__shfl_sync(kFull, A.z, k), __shfl_sync(kFull, A.zy, k), __shfl_sync(kFull, A.yz, k),
+                   __shfl_sync(kFull, A.src, k)};
+      if (lane == 0) ++cn.rev;
+      if (cy == 0 || cz == 0) {
+        if (lane == 0) set_failed(F, slot, cy == 0 ? Ak.src : Ak.z);
+        return;
+      }
+      if (cy >= cz) {
+#pragma unroll
+        for (int g = 0; g < kVG; ++g) {
+          const bool live = (dz[g >> 1] >> ((g & 1) * 32 + lane)) & 1ull;
+          u64 hit = 0;
+#pragma unroll
+          for (int w = 0; w < WT; ++w) hit |= rows[k][g][w] & dy[w];
+          const u32 um = __ballot_sync(kFull, live && hit == 0);
+          rm[g >> 1] |= static_cast<u64>(um) << ((g & 1) * 32);
+        }
+        if (lane == 0) cn.rows += cz;
+      } else {
+        union_removals<WT>(N, Ak, dy, dz, rm, cn);
+      }
+      commit_front<WT>(F, bn, fn, slot, Ak.z, rm, cn);
+    }
+  } else {
+    for (int k = 0; k < K; ++k) {
+      if (!((m >> k) & 1u)) continue;
+      u64 dz[WT], dy[WT], rm[WT];
+      int cz = 0, cy = 0;
+#pragma unroll
+      for (int w = 0; w < WT; ++w) {
+        dz[w] = shfl64(dzL[w], k);
+        dy[w] = shfl64(dyL[w], k);
+        cz += __popcll(dz[w]);
+        cy += __popcll(dy[w]);
+        rm[w] = 0;
+      }
+      const Arc Ak{__shfl_sync(kFull, A.z, k), __shfl_sync(kFull, A.zy, k), __shfl_sync(kFull, A.yz, k),
+                   __shfl_sync(kFull, A.src, k)};
+      if (lane == 0) ++cn.rev;
+      if (cy == 0 || cz == 0) {
+        if (lane == 0) set_failed(F, slot, cy == 0 ? Ak.src : Ak.z);
+        return;
+      }
+      if (cy >= cz) {
+        valuewise_removals_seq<WT>(N, Ak.zy, dy, dz, rm);
+        if (lane == 0) cn.rows += cz;
+      } else {
+        union_removals<WT>(N, Ak, dy, dz, rm, cn);
+      }
+      commit_front<WT>(F, bn, fn, slot, Ak.z, rm, cn);
+    }
+  }
+}
+
+// Table t, if one of its scope variables is in the frontier.
+template <int WT>
+__device__ __forceinline__ void front_table(const DevNet& N, const Fix& F, int t, bool all, const u32* bc, u32* bn,
+                                            int* fn, int slot, Cnt& cn) {
+  if constexpr (WT > 4) {
+    return;  // tables are rejected at upload for domains wider than 256 values
+  } else {
+    const int lane = threadIdx.x & 31;
+    const int ar = N.t_arity[t];
+    const bool act = lane < ar && (all || front_bit(bc, N.t_scope[t * kMaxArity + lane]));
+    if (!__any_sync(kFull, act) || any_failed(F)) return;
+    int s[kMaxArity], r = 0;
+    u64 rm[kMaxArity][WT];
+    const int empty_var = table_removals<WT>(N, F.D, t, s, r, rm, cn);
+    if (empty_var >= 0) {
+      if (lane == 0) set_failed(F, slot, empty_var);
+      return;
+    }
+#pragma unroll
+    for (int i = 0; i < kMaxArity; ++i)
+      if (i < r) commit_front<WT>(F, bn, fn, slot, s[i], rm[i], cn);
+  }
+}
+
+// Counters of the warps of one block summed in shared memory, then one global
+// atomic per counter and block (every thread of the block must call it).
+__device__ __forceinline__ void flush_counts_block(KStats* st, const Cnt& cn) {
+  __shared__ unsigned long long s_c[4];
+  if (threadIdx.x < 4) s_c[threadIdx.x] = 0;
+  __syncthreads();
+  u64 c[4] = {cn.rev, cn.rows, cn.tuples, cn.dels};
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c[i] += __shfl_xor_sync(kFull, c[i], o);
+    if ((threadIdx.x & 31) == 0 && c[i]) atomicAdd(&s_c[i], c[i]);
+  }
+  __syncthreads();
+  // revisions, rows, tuples, deletions are consecutive fields of KStats.
+  if (threadIdx.x < 4 && s_c[threadIdx.x]) atomicAdd(&st->revisions + threadIdx.x, s_c[threadIdx.x]);
+}
+
+__device__ __forceinline__ Fix make_front_fix(u64* D, const GridScratch& G, KStats* st) {
   Fix F;
   F.D = D;
-  F.q0 = G.q[0];
-  F.q1 = G.q[1];
-  F.fb0 = G.fb[0];
-  F.fb1 = G.fb[1];
-  F.qlen = G.qlen;
-  F.tstamp = G.tstamp;
+  F.q0 = F.q1 = nullptr;
+  F.fb0 = F.fb1 = nullptr;
+  F.qlen = nullptr;
+  F.tstamp = nullptr;
   F.failed = G.failed;
   F.fail_var = &st->fail_var;
-  F.stamp_base = vloadi(G.epoch);
-  const unsigned nblocks = gridDim.x;
+  F.stamp_base = 0;
+  return F;
+}
+
+// Round 0 of a root fixpoint: one warp per task, every variable in the
+// frontier; changes go to bitmap 1 and flag 1, wipe-outs to failed[1] (an
+// empty domain at the start too), where k_ac_front's round 1 reads them.
+template <int WT, bool kTab>
+__global__ void __launch_bounds__(kFrontBlock, WT <= 2 ? 2 : 1) k_front_first(DevNet N, u64* D, GridScratch G,
+                                                                              KStats* st) {
+  const Fix F = make_front_fix(D, G, st);
+  const int nw = (N.n + 31) >> 5;
+  const int lane = threadIdx.x & 31;
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const int gthreads = gridDim.x * blockDim.x;
-  if (evt) {
+  for (int z = gtid; z < N.n; z += gthreads) {
+    u64 any = 0;
+#pragma unroll
+    for (int w = 0; w < WT; ++w) any |= vload(D + static_cast<size_t>(z) * WT + w);
+    if (!any) set_failed(F, 1, z);
+  }
+  constexpr int K = FrontGroup<WT>::K;
+  const int narcs = N.arc_start[N.n];
+  const int ngroups = (narcs + K - 1) / K;
+  const int task = gtid >> 5;
+  Cnt cn;
+  if (task < ngroups) {
+    const int cnt = min(K, narcs - task * K);
+    Arc a{0, 0, 0, 0};
+    if (lane < cnt) a = N.arcs[task * K + lane];
+    front_group<WT>(N, F, a, cnt, true, nullptr, G.bm + nw, G.flags + 1, 1, cn);
+  } else if constexpr (kTab) {
+    if (task < ngroups + N.nt) front_table<WT>(N, F, task - ngroups, true, nullptr, G.bm + nw, G.flags + 1, 1, cn);
+  }
+  flush_counts_block(st, cn);
+  if (gtid == 0) atomicMax(&st->rounds_max, 1);
+}
+
+// Rounds from `first` on: first = 0 seeds the frontier with evt (the
+// variables whose domains changed), first = 1 continues after k_front_first.
+template <int WT, bool kTab>
+__global__ void __launch_bounds__(kFrontBlock, WT <= 2 ? 2 : 1) k_ac_front(DevNet N, u64* D, const int* evt,
+                                                                           const int* nevt_dev, int nevt, int first,
+                                                                           GridScratch G, KStats* st) {
+  const Fix F = make_front_fix(D, G, st);
+  const int nw = (N.n + 31) >> 5;
+  u32* B = G.bm;        // three bitmaps of nw words
+  int* flag = G.flags;  // [3]
+  const unsigned nblocks = gridDim.x;
+  const int lane = threadIdx.x & 31;
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gthreads = gridDim.x * blockDim.x;
+  int* err = &st->grid_err;
+  bool ok = true;
+  if (first == 0) {
     const int ne = nevt_dev ? vloadi(nevt_dev) : nevt;
-    for (int i = gtid; i < ne; i += gthreads) seed_var<WT>(N, F, evt[i]);
-  } else {
-    // Root: every variable, its items written at precomputed queue offsets
-    // (no appends); an empty domain is a wipe-out.
-    for (int z = gtid; z < N.n; z += gthreads) {
+    for (int i = gtid; i < ne; i += gthreads) {
+      const int z = evt[i];
       u64 any = 0;
 #pragma unroll
-      for (int w = 0; w < WT; ++w) any |= vload(F.D + static_cast<size_t>(z) * WT + w);
-      if (!any) set_failed(F, 0, z);
-      const int b0 = G.root_base[z], nch = G.root_base[z + 1] - b0;
-      for (int c = 0; c < nch; ++c) F.q0[b0 + c] = (static_cast<u32>(z) << kItemVarShift) | static_cast<u32>(c);
+      for (int w = 0; w < WT; ++w) any |= vload(D + static_cast<size_t>(z) * WT + w);
+      if (!any) {
+        set_failed(F, 0, z);
+      } else {
+        atomicOr(B + (z >> 5), 1u << (z & 31));
+        atomicExch(flag, 1);
+      }
     }
-    if (gtid == 0) F.qlen[0] = G.root_base[N.n];
+    ok = grid_barrier(G.bar, nblocks, err, G.wait_ns);
   }
-  int* err = &st->grid_err;
   Cnt cn;
   const long long max_rounds = N.total_values + 2;
-  int r = 0;
-  bool ok = grid_barrier(G.bar, nblocks, err, G.wait_ns);
+  constexpr int K = FrontGroup<WT>::K;
+  const int narcs = N.arc_start[N.n];
+  const int ngroups = (narcs + K - 1) / K;
+  const int ntasks = ngroups + (kTab ? N.nt : 0);
   const int gwarp = gtid >> 5, nwarps = gthreads >> 5;
+  int r = first;
   for (; ok; ++r) {
-    const int cur = r & 1;
-    const int len = vloadi(F.qlen + r % 3);
-    const int fl = vloadi(F.failed + cur);
-    if (len == 0 || fl) break;
+    const int cur = r % 3, nxt = (r + 1) % 3, clr = (r + 2) % 3;
+    if (!vloadi(flag + cur) || vloadi(F.failed + (r & 1))) break;
     if (r > max_rounds) {
       if (gtid == 0) st->error = -4;
       break;
     }
-    if (gtid == 0) F.qlen[(r + 2) % 3] = 0;
-    const u32* qc = cur ? F.q1 : F.q0;
-    u32* qn = cur ? F.q0 : F.q1;
-    u32* fbc = cur ? F.fb1 : F.fb0;
-    u32* fbn = cur ? F.fb0 : F.fb1;
-    int* qlenn = F.qlen + (r + 1) % 3;
-    for (int j = gwarp; j < len; j += nwarps)
-      process_item<WT, kTab, true>(N, F, qc[j], fbc, qn, fbn, qlenn, cur ^ 1, F.stamp_base + r + 1, cn);
+    const u32* bc = B + static_cast<size_t>(cur) * nw;
+    u32* bn = B + static_cast<size_t>(nxt) * nw;
+    u32* bz = B + static_cast<size_t>(clr) * nw;
+    for (int w = gtid; w < nw; w += gthreads) bz[w] = 0;
+    if (gtid == 0) flag[clr] = 0;
+    const int slot = (r + 1) & 1;
+    Arc an{0, 0, 0, 0};
+    if (gwarp < ngroups && lane < min(K, narcs - gwarp * K)) an = N.arcs[gwarp * K + lane];
+    for (int t = gwarp; t < ntasks; t += nwarps) {
+      const int tn = t + nwarps;
+      if (t < ngroups) {
+        const Arc a = an;
+        if (tn < ngroups && lane < min(K, narcs - tn * K)) an = N.arcs[tn * K + lane];
+        front_group<WT>(N, F, a, min(K, narcs - t * K), false, bc, bn, flag + nxt, slot, cn);
+      } else if constexpr (kTab) {
+        front_table<WT>(N, F, t - ngroups, false, bc, bn, flag + nxt, slot, cn);
+      }
+    }
     ok = grid_barrier(G.bar, nblocks, err, G.wait_ns);
   }
   flush_counts(st, cn);
@@ -1181,7 +1447,6 @@ __global__ void __launch_bounds__(512) k_ac_grid(DevNet N, u64* D, const int* ev
     st->inconsistent = (vloadi(F.failed) | vloadi(F.failed + 1)) ? 1 : 0;
     atomicMax(&st->rounds_max, r);
     atomicAdd(&st->fixpoints, 1ull);
-    *G.epoch = F.stamp_base + r + 2;
   }
 }
 
@@ -2170,26 +2435,53 @@ cudaError_t launch_mac(const DevNet* nets, const MacJob* jobs, int njobs, int* c
   return cudaGetLastError();
 }
 
-int ac_grid_max_blocks(const DevNet& N, int block, int sm_count) {
+int ac_front_max_blocks(const DevNet& N, int sm_count) {
   int per_sm = 0;
   cudaError_t e = dispatch_wt(N, [&](auto wt, auto tab) -> cudaError_t {
     constexpr int WT = decltype(wt)::value;
     constexpr bool TB = decltype(tab)::value;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ac_grid<WT, TB>, block, 0);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ac_front<WT, TB>, kFrontBlock, 0);
   });
   if (e != cudaSuccess || per_sm < 1) return 0;
   return per_sm * sm_count;
 }
 
-cudaError_t launch_ac_grid(const DevNet& N, u64* level_dom, const int* evt, const int* nevt_dev, int nevt,
-                           GridScratch G, KStats* st, int block, int grid, cudaStream_t s) {
+static int front_tasks(const DevNet& N, int narcs) {
+  int K = 1;
+  dispatch_wt(N, [&](auto wt, auto) -> cudaError_t {
+    K = FrontGroup<decltype(wt)::value>::K;
+    return cudaSuccess;
+  });
+  return (narcs + K - 1) / K + N.nt;
+}
+
+int ac_front_blocks(const DevNet& N, int narcs, int sm_count) {
+  const int most = ac_front_max_blocks(N, sm_count);
+  if (most < 1) return 0;
+  // One warp per task of a full round, at most every co-resident CTA.
+  const int warps = kFrontBlock / 32;
+  return std::max(1, std::min(most, (front_tasks(N, narcs) + warps - 1) / warps));
+}
+
+cudaError_t launch_ac_front(const DevNet& N, u64* level_dom, const int* evt, const int* nevt_dev, int nevt,
+                            GridScratch G, KStats* st, int grid, cudaStream_t s) {
   return dispatch_wt(N, [&](auto wt, auto tab) -> cudaError_t {
     constexpr int WT = decltype(wt)::value;
     constexpr bool TB = decltype(tab)::value;
+    int first = 0;
+    if (!evt) {
+      // Round 0 as a plain launch, one warp per task.
+      const int warps = kFrontBlock / 32;
+      const int blocks = std::max(1, (front_tasks(N, 2 * N.nb) + warps - 1) / warps);
+      k_front_first<WT, TB><<<blocks, kFrontBlock, 0, s>>>(N, level_dom, G, st);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+      first = 1;
+    }
     DevNet n2 = N;
-    void* args[] = {&n2, &level_dom, &evt, &nevt_dev, &nevt, &G, &st};
-    return cudaLaunchCooperativeKernel(reinterpret_cast<void*>(k_ac_grid<WT, TB>), dim3(grid), dim3(block), args, 0,
-                                       s);
+    void* args[] = {&n2, &level_dom, &evt, &nevt_dev, &nevt, &first, &G, &st};
+    return cudaLaunchCooperativeKernel(reinterpret_cast<void*>(k_ac_front<WT, TB>), dim3(grid), dim3(kFrontBlock),
+                                       args, 0, s);
   });
 }
 

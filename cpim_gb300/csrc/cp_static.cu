@@ -170,8 +170,8 @@ __global__ void k_static_prep(int n, int W, int nb, const int* dsize, const int*
   __syncthreads();
   for (int c = threadIdx.x; c < nb; c += blockDim.x) {
     const int x = bx[c], y = by[c];
-    arcs[arc_start[y] + atomicAdd(&fill[y], 1)] = Arc{x, static_cast<u32>(offA[c]), static_cast<u32>(offB[c]), 0};
-    arcs[arc_start[x] + atomicAdd(&fill[x], 1)] = Arc{y, static_cast<u32>(offB[c]), static_cast<u32>(offA[c]), 0};
+    arcs[arc_start[y] + atomicAdd(&fill[y], 1)] = Arc{x, static_cast<u32>(offA[c]), static_cast<u32>(offB[c]), y};
+    arcs[arc_start[x] + atomicAdd(&fill[x], 1)] = Arc{y, static_cast<u32>(offB[c]), static_cast<u32>(offA[c]), x};
   }
   // A blocks are the caller's rows in constraint order; B blocks start zeroed.
   const int64_t b_end = nb ? offB[nb - 1] + int64_t(dsize[by[nb - 1]]) * W : 0;

@@ -14,9 +14,12 @@ pytestmark = pytest.mark.gpu
 
 def test_grid_wait_runs_out_then_recovers():
     # Over 8192 arc incidences: the fixpoint runs on the whole grid with a
-    # bounded barrier. A zero budget makes the first wait of some CTA run out.
+    # bounded barrier. A fixpoint seeded with changed variables always passes
+    # the barrier after the seeding; a zero budget makes the wait of some CTA
+    # there run out.
     inst = cp.gen_binary(2000, 64, 30000, 0.2, 0.5, 0.2, 3)
     ok, d, dels = O.ac3bit(oracle_view_of(inst))
+    every = np.arange(inst.n, dtype=np.int32)
     with cp.Engine(0) as eng:
         net = eng.upload(inst)
         eng.set_wait_budget(0)
@@ -24,7 +27,7 @@ def test_grid_wait_runs_out_then_recovers():
         for _ in range(3):
             net.dom_set(0, inst.init)
             try:
-                net.enforce_ac(0)
+                net.enforce_ac(0, evt=every)
                 codes.append(0)
             except cp.CPError as ex:
                 codes.append(ex.code)
