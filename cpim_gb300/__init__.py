@@ -104,6 +104,7 @@ def lib():
         "cp_enforce_sac1": ([vp, i, C.POINTER(Stats)], i),
         "cp_singletons": ([vp, i, i, PI, PI, PU8, i, C.POINTER(Stats)], i),
         "cp_sac_sweep": ([vp, i, P64, C.POINTER(C.c_int64), C.POINTER(Stats)], i),
+        "cp_sac_tiles": ([vp, i, i, PI, PI, PI, i, P64, C.POINTER(C.c_double)], i),
         "cp_mac_solve": ([vp, i, i, i64, C.POINTER(SearchResult), PI], i),
         "cp_gsolver_solve": ([vp, i64, C.POINTER(SearchResult), PI], i),
         "cp_gen_binary": ([i, i, i64, d, d, d, u64, PV], i),
@@ -385,6 +386,18 @@ class Net:
         _check(lib().cp_sac_sweep(self._h, level, _p(out, C.c_uint64), C.byref(deep), C.byref(st)))
         return out, deep.value, st
 
+    def sac_tiles(self, xs, c1s, c2s, mode=0, level=0):
+        """Support-count tiles (x, c1, c2): (removal words [ntiles, 128, 2],
+        kernel ms). mode 0 bitwise, 1 tensor cores."""
+        x = np.ascontiguousarray(xs, dtype=np.int32)
+        a = np.ascontiguousarray(c1s, dtype=np.int32)
+        b = np.ascontiguousarray(c2s, dtype=np.int32)
+        out = np.zeros((len(x), 128, 2), np.uint64)
+        ms = C.c_double()
+        _check(lib().cp_sac_tiles(self._h, level, len(x), _p(x, C.c_int), _p(a, C.c_int), _p(b, C.c_int), mode,
+                                  _p(out, C.c_uint64), C.byref(ms)))
+        return out, ms.value
+
     # -- search --
     def mac_solve(self, var_h=VarHeuristic.VRH_DOM_MIN, val_h=ValHeuristic.VLH_MIN, time_limit_ms=600000):
         res = SearchResult()
@@ -401,6 +414,30 @@ class Net:
         return {"status": res.status, "num_positive": res.num_positive, "num_negative": res.num_negative,
                 "propagations": res.propagations, "solve_ms": res.solve_ms,
                 "solution": sol.tolist() if res.status == 1 else []}
+
+
+def sac_tile_list(inst: Instance, xs, limit=None):
+    """SAC support-count tiles (x, c1, c2) of a binary network: for every x in
+    xs, every constraint c1 on x (joining y) and every other constraint c2 on
+    y; at most `limit` tiles."""
+    bx, by = inst.bin_scope[0::2], inst.bin_scope[1::2]
+    inc = [[] for _ in range(inst.n)]
+    for c, (a, b) in enumerate(zip(bx.tolist(), by.tolist())):
+        inc[a].append(c)
+        inc[b].append(c)
+    tx, t1, t2 = [], [], []
+    for x in xs:
+        for c1 in inc[x]:
+            y = int(by[c1]) if int(bx[c1]) == x else int(bx[c1])
+            for c2 in inc[y]:
+                if c2 == c1:
+                    continue
+                tx.append(x)
+                t1.append(c1)
+                t2.append(c2)
+                if limit is not None and len(tx) >= limit:
+                    return (np.array(tx, np.int32), np.array(t1, np.int32), np.array(t2, np.int32))
+    return np.array(tx, np.int32), np.array(t1, np.int32), np.array(t2, np.int32)
 
 
 class Batch:

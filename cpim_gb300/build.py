@@ -16,7 +16,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libcpgpu.so")
-SOURCES = ["cp_kernels.cu", "cp_engine.cu", "cp_static.cu", "cp_server.cpp"]
+SOURCES = ["cp_kernels.cu", "cp_engine.cu", "cp_static.cu", "cp_tensor.cu", "cp_server.cpp"]
 HEADERS = ["cp_internal.h", "cp_gen.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")

@@ -203,6 +203,7 @@ struct cp_net {
   int* d_by = nullptr;
   int64_t* d_offA = nullptr;
   int64_t* d_offB = nullptr;
+  std::vector<int64_t> offA, offB;  // host copies: word offsets of each constraint's A / B rows
   int64_t relA_words = 0, relB_words = 0;
   GridScratch G{};
   SacScratch S{};
@@ -681,6 +682,8 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   mp.add(&net->d_by, net->by.data(), n_bin);
   mp.add(&net->d_offA, offA.data(), n_bin);
   mp.add(&net->d_offB, offB.data(), n_bin);
+  net->offA = offA;
+  net->offB = offB;
   char* d_meta = nullptr;
   CP_TRY(net->alloc(&d_meta, mp.total));
   PinnedLease stage(e);
@@ -1203,6 +1206,74 @@ int cp_sac_sweep(cp_net* net, int level, uint64_t* verdict, int64_t* deep, cp_st
     a.s.kernel_bytes = alg_bytes(net, ka, static_cast<int64_t>(k.branches));
     *st = a.s;
   }
+  return CP_OK;
+}
+
+int cp_sac_tiles(cp_net* net, int level, int ntiles, const int* tile_x, const int* tile_c1, const int* tile_c2,
+                 int mode, uint64_t* out, double* ms) {
+  if (!net || ntiles < 0 || (ntiles > 0 && (!tile_x || !tile_c1 || !tile_c2 || !out)))
+    return fail(CP_E_ARG, "null argument");
+  CP_TRY(check_level(net, level));
+  if (mode != 0 && mode != 1) return fail(CP_E_ARG, "mode must be 0 (bitwise) or 1 (tensor cores)");
+  if (net->W > 2 || net->dn.nt != 0) return fail(CP_E_UNSUPPORTED, "tiles need a binary network of at most 128 values");
+  const int nb = static_cast<int>(net->bx.size());
+  std::vector<SacTile> tiles(ntiles);
+  for (int t = 0; t < ntiles; ++t) {
+    const int x = tile_x[t], c1 = tile_c1[t], c2 = tile_c2[t];
+    if (c1 < 0 || c1 >= nb || c2 < 0 || c2 >= nb) return fail(CP_E_ARG, "constraint out of range");
+    const bool x_first = net->bx[c1] == x;
+    if (!x_first && net->by[c1] != x) return fail(CP_E_ARG, "constraint c1 does not contain x");
+    const int y = x_first ? net->by[c1] : net->bx[c1];
+    const bool y_first = net->bx[c2] == y;
+    if (!y_first && net->by[c2] != y) return fail(CP_E_ARG, "constraint c2 does not contain y");
+    const int z = y_first ? net->by[c2] : net->bx[c2];
+    SacTile& T = tiles[t];
+    // Rows of x over y: the A block when x is the first variable of c1, else
+    // the B block; likewise rows of z over y in c2.
+    T.xy = static_cast<u32>(x_first ? net->offA[c1] : net->offB[c1]);
+    T.zy = static_cast<u32>(y_first ? net->offB[c2] : net->offA[c2]);
+    T.y = y;
+    T.z = z;
+    T.dx = net->dom[x];
+    T.dz = net->dom[z];
+    T.pad0 = T.pad1 = 0;
+  }
+  if (ntiles == 0) {
+    if (ms) *ms = 0.0;
+    return CP_OK;
+  }
+  cp_engine* e = net->e;
+  cudaStream_t s = e->stream;
+  const size_t out_words = static_cast<size_t>(ntiles) * 128 * 2;
+  void *d_tiles = nullptr, *d_out = nullptr, *d_err = nullptr;
+  int rc = e->dev_alloc(&d_tiles, tiles.size() * sizeof(SacTile));
+  if (rc == CP_OK) rc = e->dev_alloc(&d_out, out_words * 8);
+  if (rc == CP_OK) rc = e->dev_alloc(&d_err, sizeof(int));
+  int h_err = 0;
+  float kms = 0;
+  if (rc == CP_OK) {
+    cudaError_t ce = cudaMemcpyAsync(d_tiles, tiles.data(), tiles.size() * sizeof(SacTile), cudaMemcpyHostToDevice, s);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(d_err, 0, sizeof(int), s);
+    if (ce == cudaSuccess) ce = cudaEventRecord(e->evk0, s);
+    if (ce == cudaSuccess)
+      ce = mode == 0 ? launch_tiles_bitwise(net->W, net->d_rel, net->level_ptr(level),
+                                            static_cast<const SacTile*>(d_tiles), ntiles, static_cast<u64*>(d_out),
+                                            e->sm_count, s)
+                     : launch_tiles_tc(net->W, net->d_rel, net->level_ptr(level), static_cast<const SacTile*>(d_tiles),
+                                       ntiles, static_cast<u64*>(d_out), static_cast<int*>(d_err), e->sm_count, s);
+    if (ce == cudaSuccess) ce = cudaEventRecord(e->evk1, s);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(out, d_out, out_words * 8, cudaMemcpyDeviceToHost, s);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+    if (ce == cudaSuccess) ce = cudaEventElapsedTime(&kms, e->evk0, e->evk1);
+    if (ce != cudaSuccess) rc = fail(CP_E_CUDA, std::string("cp_sac_tiles: ") + cudaGetErrorString(ce));
+  }
+  ++e->launches;
+  for (void* p : {d_tiles, d_out, d_err})
+    if (p) e->dev_free(p);
+  if (rc != CP_OK) return rc;
+  if (h_err) return fail(CP_E_TIMEOUT, "tensor-core product did not complete within the bounded wait");
+  if (ms) *ms = kms;
   return CP_OK;
 }
 

@@ -222,6 +222,20 @@ cudaError_t launch_node(const DevNet& N, u64* levels, int src, int dst, int op, 
 cudaError_t launch_ac_front(const DevNet& N, u64* level_dom, const int* evt, const int* nevt_dev, int nevt,
                             GridScratch G, KStats* st, int grid, cudaStream_t s);
 int ac_front_blocks(const DevNet& N, int narcs, int sm_count);
+// One SAC support-count tile (cp_tensor.cu): branches x = a for a < dx, rows of
+// x over y at word offset xy; values of z (dz of them) with rows over y at zy.
+struct SacTile {
+  u32 xy, zy;
+  int y, z, dx, dz, pad0, pad1;
+};
+// out[t][a] (two words): values of z in D(z) that lose every support in
+// D(y) & row_xy(a); W (internal words per domain) 1 or 2.
+cudaError_t launch_tiles_bitwise(int W, const u64* rel, const u64* dom, const SacTile* tiles, int ntiles, u64* out,
+                                 int sm_count, cudaStream_t s);
+// The same on the tensor cores; *err set to 1 if a product did not complete
+// within the bounded wait.
+cudaError_t launch_tiles_tc(int W, const u64* rel, const u64* dom, const SacTile* tiles, int ntiles, u64* out,
+                            int* err, int sm_count, cudaStream_t s);
 // Persistent batched singleton tests: pairs work[0..*nwork), results in ok.
 // With idx != nullptr the tests are work[idx[i]] for i < *nidx.
 cudaError_t launch_sac_branches(const DevNet& N, const u64* root, const int2* work, const int* nwork, int* cursor,

@@ -163,6 +163,20 @@ int cp_singletons(cp_net* net, int level, int count, const int* vars, const int*
  * two-round tiled kernel passed on to the general fixpoint kernel (0 where
  * the tiled kernel does not run). */
 int cp_sac_sweep(cp_net* net, int level, uint64_t* verdict, int64_t* deep, cp_stats* st);
+/* Support counting of SAC tiles, bitwise or on the tensor cores: the
+ * support-count form of a singleton test's round two that the reference only
+ * projects (docs/tensor_core_vs_cuda_core_gac.md), measured beside the
+ * bitwise form on the same tiles. Tile t is (x, c1, c2): constraint c1 joins
+ * x and y, constraint c2 joins y and z. Its 128 branches are x = a for
+ * a < dom(x), with D_a(y) = D(y) & R_c1(x = a) at `level`; out (ntiles * 128 * 2
+ * words) gets, per tile and branch a, the values v in D(z) with no support in
+ * D_a(y) (the AND-then-any of AC3bit::seek_support, src/AC3bit.cpp:29-38),
+ * zero for a >= dom(x). mode 0: bitwise (AND and ballot per branch); mode 1:
+ * the 0/1 product D_a(y) x R_c2 on the 5th-generation tensor cores (bf16
+ * operands, fp32 counts in tensor memory; exact). Both modes give the same
+ * words. Binary networks of at most 128 values. ms: kernel time (CUDA events). */
+int cp_sac_tiles(cp_net* net, int level, int ntiles, const int* tile_x, const int* tile_c1, const int* tile_c2,
+                 int mode, uint64_t* out, double* ms);
 
 /* ---- multi-instance batches ----------------------------------------------
  * Many independent networks (each uploaded with cp_net_upload, of any sizes)
