@@ -778,6 +778,31 @@ def run_gac(args):
     return 0
 
 
+def run_tensor(args):
+    """The tensor-core support-count tiles against the bitwise test on the
+    benchmark network (see tensor_variant); `steps` timed repetitions."""
+    import torch
+    import cpim_gb300 as cp
+    torch.cuda.set_device(0)
+    inst = cp.gen_binary(N, D, E, P, P, 0.0, SEED)
+    with cp.Engine(0) as eng:
+        net = eng.upload(inst, max_levels=2)
+        sweep_ms = None
+        for _ in range(max(1, args.warmup)):
+            st = net.enforce_sac1(0)
+            sweep_ms = st.kernel_ms / max(1, st.sweeps)
+        net.dom_set(0, inst.init)
+        res = tensor_variant(inst, net, sweep_ms, reps=max(1, args.steps))
+        net.close()
+    line = {"metric": "SAC support-count tiles/s, tensor cores vs bitwise (bit-exact)",
+            "value": res["tensor_cores"]["tiles_per_s"], "unit": "tiles/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16 (0/1 operands, fp32 counts)", "data": "synthetic (seeded generator)",
+            "config": bench_config(), **res}
+    print(json.dumps(line))
+    return 0
+
+
 def run_mac(args):
     """Config-1 measurement: MAC (dom/min, min value) to the first solution on
     the plain CPU-runnable shape, seeds 1..10: the device search (one CTA per
@@ -852,10 +877,11 @@ def main():
                     help="SAC closures per timed step of the default workload")
     ap.add_argument("--no-extras", action="store_true",
                     help="default workload without the GAC and uneven-batch samples")
-    ap.add_argument("--workload", default="sac", choices=["sac", "uneven", "serving", "gac", "mac"],
+    ap.add_argument("--workload", default="sac", choices=["sac", "uneven", "serving", "gac", "mac", "tensor"],
                     help="sac: the batched SAC sweep (headline); uneven: the uneven multi-instance batch; "
                          "serving: the request server under Poisson load; gac: the large GAC fixpoint; "
-                         "mac: MAC searches on the plain shape")
+                         "mac: MAC searches on the plain shape; tensor: support-count tiles on the tensor cores "
+                         "against the bitwise test")
     ap.add_argument("--instances", type=int, default=4096, help="uneven workload: instances")
     ap.add_argument("--per-instance-sample", type=int, default=256, help="uneven workload: one-by-one sample")
     ap.add_argument("--networks", type=int, default=64, help="serving: resident networks")
@@ -879,6 +905,8 @@ def main():
         return run_gac(args)
     if args.workload == "mac":
         return run_mac(args)
+    if args.workload == "tensor":
+        return run_tensor(args)
     return run_ours(args)
 
 
