@@ -638,13 +638,7 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
       for (int i = 0; i < t_arity[t]; ++i) vtab[fill[t_scope[static_cast<size_t>(t) * kMaxArity + i]]++] = t;
   }
   // Work-item chunking.
-  int max_deg = 0;
-  for (int x = 0; x < n; ++x) max_deg = std::max(max_deg, arc_deg[x] + tab_deg[x]);
-  int chunk = e->chunk > 0 ? e->chunk : 8;
-  chunk = std::max(chunk, (max_deg + kMaxChunksPerVar - 1) / kMaxChunksPerVar);
-  int64_t max_items = 0;
-  for (int x = 0; x < n; ++x) max_items += std::max(1, (arc_deg[x] + tab_deg[x] + chunk - 1) / chunk);
-  if (max_items >= (int64_t(1) << 31)) return fail(CP_E_UNSUPPORTED, "too many work items");
+  const int chunk = e->chunk > 0 ? e->chunk : 8;
   int64_t total_values = 0;
   for (int x = 0; x < n; ++x) total_values += dom[x];
 
@@ -656,7 +650,6 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   D.nb = n_bin;
   D.nt = n_tab;
   D.chunk = chunk;
-  D.max_items = static_cast<int>(max_items);
   D.total_values = total_values;
   int* d_dsize;
   int* d_arc_start;

@@ -34,9 +34,7 @@ constexpr int kMaxArity = 4;
 // fewest supports, then padding.
 constexpr int kWeakK = 16;
 constexpr int kWeakStride = 20;
-constexpr int kItemVarShift = 12;             // work item = (var << 12) | chunk
-constexpr int kMaxChunksPerVar = 1 << kItemVarShift;
-constexpr int kMaxVars = 1 << (32 - kItemVarShift);
+constexpr int kMaxVars = 1 << 20;             // variables per network
 
 struct Arc {
   int z;        // variable revised
@@ -48,7 +46,6 @@ struct Arc {
 struct DevNet {
   int n = 0, W = 1, nb = 0, nt = 0;
   int chunk = 8;          // incidences per work item
-  int max_items = 0;      // capacity of one work queue
   int64_t total_values = 0;
   const int* dsize = nullptr;       // [n]
   const int* arc_start = nullptr;   // [n+1]

@@ -11,12 +11,12 @@
 //              under a bounded grid barrier (cooperative launch), the
 //              frontier kept as bitmaps instead of a queue.
 //
-// Frontier of the CTA-local fixpoints: a queue of work items (variable y,
-// chunk of y's incidences) plus a bitmap that admits each changed variable
-// once per round. Round r processes
-// queue r&1 and appends to the other; a variable's bit in the current bitmap
-// is cleared by the warp that takes its first chunk, so both bitmaps are clean
-// at every round boundary without a clearing pass.
+// Frontier of the CTA-local fixpoints: a queue of the changed variables plus
+// a bitmap that admits each once per round; a round's work items are the
+// chunks of the queued variables' incidences, numbered by a CTA-wide scan.
+// Round r processes queue r&1 and appends to the other; a variable's bit in
+// the current bitmap is cleared by the warp that takes its first chunk, so
+// both bitmaps are clean at every round boundary without a clearing pass.
 //
 // Revise of arc (z <- y) by one warp (the AND-then-any of AC3bit::seek_support,
 // src/AC3bit.cpp:29-38, over all values of z at once): the warp either tests
@@ -106,8 +106,9 @@ __device__ __forceinline__ long long globaltimer_ns() {
 // State of one fixpoint; pointers are shared or global memory.
 struct Fix {
   u64* D;
-  u32* q0;
+  u32* q0;       // queued variables of the even / odd rounds (n each)
   u32* q1;
+  int* pre;      // [n+1] first work item of each queued variable this round
   u32* fb0;
   u32* fb1;
   int* qlen;     // [3]
@@ -147,15 +148,17 @@ __device__ __forceinline__ int incidences(const DevNet& N, int z) {
   return (N.arc_start[z + 1] - N.arc_start[z]) + (N.tinc_start[z + 1] - N.tinc_start[z]);
 }
 
-// Admits z to the next round once (bitmap), appending all its work items.
-__device__ __forceinline__ void append_var(const DevNet& N, u32* q, u32* fb, int* qlen, int z) {
+// Work items of variable z: its incidences in chunks of N.chunk (at least one).
+__device__ __forceinline__ int var_chunks(const DevNet& N, int z) {
+  return max(1, (incidences(N, z) + N.chunk - 1) / N.chunk);
+}
+
+// Admits z to the next round once (bitmap): one queue entry per variable.
+__device__ __forceinline__ void append_var(u32* q, u32* fb, int* qlen, int z) {
   const u32 bit = 1u << (z & 31);
   const u32 old = atomicOr(fb + (z >> 5), bit);
   if (old & bit) return;
-  int nch = (incidences(N, z) + N.chunk - 1) / N.chunk;
-  if (nch < 1) nch = 1;
-  const int base = atomicAdd(qlen, nch);
-  for (int c = 0; c < nch; ++c) q[base + c] = (static_cast<u32>(z) << kItemVarShift) | static_cast<u32>(c);
+  q[atomicAdd(qlen, 1)] = static_cast<u32>(z);
 }
 
 // Seeds variable z (single thread): a seeded variable with an empty domain is
@@ -169,7 +172,7 @@ __device__ __forceinline__ void seed_var(const DevNet& N, const Fix& F, int z) {
     set_failed(F, 0, z);
     return;
   }
-  append_var(N, F.q0, F.fb0, F.qlen, z);
+  append_var(F.q0, F.fb0, F.qlen, z);
 }
 
 // Removes rm (warp-uniform) from D(z); on a change, checks for wipe-out and
@@ -199,7 +202,7 @@ __device__ __forceinline__ void commit(const DevNet& N, const Fix& F, u32* qn, u
     if (!nonempty)
       set_failed(F, slot, z);
     else
-      append_var(N, qn, fbn, qlenn, z);
+      append_var(qn, fbn, qlenn, z);
   }
 }
 
@@ -383,12 +386,11 @@ __device__ __forceinline__ void revise_table(const DevNet& N, const Fix& F, u32*
   }
 }
 
+// Work item c (chunk of incidences) of variable y.
 template <int WT, bool kTab>
-__device__ __forceinline__ void process_item(const DevNet& N, const Fix& F, u32 item, u32* fbc, u32* qn, u32* fbn,
+__device__ __forceinline__ void process_item(const DevNet& N, const Fix& F, int y, int c, u32* fbc, u32* qn, u32* fbn,
                                              int* qlenn, int slot, int stamp, Cnt& cn) {
   const int lane = threadIdx.x & 31;
-  const int y = static_cast<int>(item >> kItemVarShift);
-  const int c = static_cast<int>(item & (kMaxChunksPerVar - 1));
   if (c == 0 && lane == 0) atomicAnd(fbc + (y >> 5), ~(1u << (y & 31)));
   const int a0 = N.arc_start[y], da = N.arc_start[y + 1] - a0;
   const int t0 = N.tinc_start[y], dt = N.tinc_start[y + 1] - t0;
@@ -416,6 +418,48 @@ __device__ __forceinline__ void process_item(const DevNet& N, const Fix& F, u32 
   }
 }
 
+// The round's work items: pre[i] = work items of the queued variables before
+// q[i] (a CTA-wide exclusive scan of their chunk counts), pre[len] = all of
+// them. Every thread of the CTA calls it; ends with the CTA synchronised.
+__device__ __forceinline__ int cta_round_items(const DevNet& N, const u32* q, int len, int* pre) {
+  __shared__ int s_w[32];
+  __shared__ int s_carry;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (threadIdx.x == 0) s_carry = 0;
+  __syncthreads();
+  for (int base = 0; base < len; base += blockDim.x) {
+    const int i = base + threadIdx.x;
+    const int v = i < len ? var_chunks(N, static_cast<int>(q[i])) : 0;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(kFull, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) s_w[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      int w = lane < nw ? s_w[lane] : 0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(kFull, w, o);
+        if (lane >= o) w += y;
+      }
+      s_w[lane] = w;
+    }
+    __syncthreads();
+    const int carry = s_carry;
+    if (i < len) pre[i] = carry + (warp ? s_w[warp - 1] : 0) + x - v;
+    __syncthreads();
+    if (threadIdx.x == 0) s_carry = carry + s_w[nw - 1];
+    __syncthreads();
+  }
+  const int total = s_carry;
+  if (threadIdx.x == 0) pre[len] = total;
+  __syncthreads();
+  return total;
+}
+
 // CTA-local fixpoint; the caller has seeded queue 0 and synchronised.
 // Returns the number of rounds; sets *err on a round-count overrun.
 template <int WT, bool kTab>
@@ -438,8 +482,15 @@ __device__ int cta_fixpoint(const DevNet& N, const Fix& F, Cnt& cn, int* err) {
     u32* fbc = cur ? F.fb1 : F.fb0;
     u32* fbn = cur ? F.fb0 : F.fb1;
     int* qlenn = F.qlen + (r + 1) % 3;
-    for (int j = warp; j < len; j += nwarps)
-      process_item<WT, kTab>(N, F, qc[j], fbc, qn, fbn, qlenn, cur ^ 1, F.stamp_base + r + 1, cn);
+    const int items = cta_round_items(N, qc, len, F.pre);
+    // Warp w takes items w, w + W, ...; its cursor into the queue only moves
+    // forward (pre is increasing).
+    int i = 0;
+    for (int j = warp; j < items; j += nwarps) {
+      while (F.pre[i + 1] <= j) ++i;
+      process_item<WT, kTab>(N, F, static_cast<int>(qc[i]), j - F.pre[i], fbc, qn, fbn, qlenn, cur ^ 1,
+                             F.stamp_base + r + 1, cn);
+    }
     __syncthreads();
   }
   return r;
@@ -447,7 +498,7 @@ __device__ int cta_fixpoint(const DevNet& N, const Fix& F, Cnt& cn, int* err) {
 
 // Layout of the CTA-local state inside a byte buffer.
 struct CtaLayout {
-  size_t d, q0, q1, fb0, fb1, ts, total;
+  size_t d, q0, q1, pre, fb0, fb1, ts, total;
 };
 
 __host__ __device__ inline CtaLayout cta_layout(const DevNet& N) {
@@ -456,8 +507,9 @@ __host__ __device__ inline CtaLayout cta_layout(const DevNet& N) {
   const size_t nw = (static_cast<size_t>(N.n) + 31) / 32;
   L.d = 0;
   L.q0 = up(L.d + static_cast<size_t>(N.n) * N.W * 8);
-  L.q1 = up(L.q0 + static_cast<size_t>(N.max_items) * 4);
-  L.fb0 = up(L.q1 + static_cast<size_t>(N.max_items) * 4);
+  L.q1 = up(L.q0 + static_cast<size_t>(N.n) * 4);
+  L.pre = up(L.q1 + static_cast<size_t>(N.n) * 4);
+  L.fb0 = up(L.pre + (static_cast<size_t>(N.n) + 1) * 4);
   L.fb1 = up(L.fb0 + nw * 4);
   L.ts = up(L.fb1 + nw * 4);
   L.total = up(L.ts + static_cast<size_t>(N.nt) * 4);
@@ -470,6 +522,7 @@ __device__ __forceinline__ Fix make_cta_fix(const DevNet& N, char* base, int* ql
   F.D = reinterpret_cast<u64*>(base + L.d);
   F.q0 = reinterpret_cast<u32*>(base + L.q0);
   F.q1 = reinterpret_cast<u32*>(base + L.q1);
+  F.pre = reinterpret_cast<int*>(base + L.pre);
   F.fb0 = reinterpret_cast<u32*>(base + L.fb0);
   F.fb1 = reinterpret_cast<u32*>(base + L.fb1);
   F.tstamp = N.nt ? reinterpret_cast<int*>(base + L.ts) : nullptr;
@@ -1035,7 +1088,7 @@ __global__ void __launch_bounds__(256) k_sac(DevNet N, const u64* root, const in
     if (threadIdx.x == 0) {
       u64* dv = F.D + static_cast<size_t>(xa.x) * WT;
       for (int w = 0; w < WT; ++w) dv[w] = (w == (xa.y >> 6)) ? (1ull << (xa.y & 63)) : 0ull;
-      append_var(N, F.q0, F.fb0, F.qlen, xa.x);
+      append_var(F.q0, F.fb0, F.qlen, xa.x);
     }
     __syncthreads();
     const int rounds = cta_fixpoint<WT, kTab>(N, F, cn, &s_err);
@@ -1332,6 +1385,7 @@ __device__ __forceinline__ Fix make_front_fix(u64* D, const GridScratch& G, KSta
   Fix F;
   F.D = D;
   F.q0 = F.q1 = nullptr;
+  F.pre = nullptr;
   F.fb0 = F.fb1 = nullptr;
   F.qlen = nullptr;
   F.tstamp = nullptr;
@@ -2237,7 +2291,7 @@ __global__ void __launch_bounds__(256) k_batch_sac(BatchDev B, int deep_only, KS
     if (threadIdx.x == 0) {
       u64* dv = F.D + static_cast<size_t>(x) * WT;
       for (int w = 0; w < WT; ++w) dv[w] = (w == (a >> 6)) ? (1ull << (a & 63)) : 0ull;
-      append_var(N, F.q0, F.fb0, F.qlen, x);
+      append_var(F.q0, F.fb0, F.qlen, x);
     }
     __syncthreads();
     const int rounds = cta_fixpoint<WT, kTab>(N, F, cn, &s_err);

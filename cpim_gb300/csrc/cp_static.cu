@@ -309,7 +309,6 @@ extern "C" int cp_enforce_ac_static(int n, int W, const int* d_dom_size, uint64_
   N.nb = n_bin;
   N.nt = 0;
   N.chunk = kStaticChunk;
-  N.max_items = n + (2 * n_bin + kStaticChunk - 1) / kStaticChunk + 1;
   N.total_values = int64_t(n) * 64 * W;
   const size_t cta_bytes = cta_state_bytes(N);
   const StaticLayout L = static_layout(n, W, n_bin, cta_bytes);

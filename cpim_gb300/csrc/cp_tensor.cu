@@ -298,6 +298,9 @@ cudaError_t launch_tiles_tc(int W, const u64* rel, const u64* dom, const SacTile
   if (W != 1 && W != 2) return cudaErrorInvalidValue;
   auto kern = W == 1 ? k_tiles_tc<1> : k_tiles_tc<2>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+  // All of the unified L1 as shared memory, so that three CTAs fit per SM
+  // from the first launch on.
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTcThreads, kTcSmem);
