@@ -131,9 +131,30 @@ class ModelBuilder {
 
 // The network: device-resident domains (a level stack) and relations
 // (Network, include/Network.h:324-380).
+// A variable of the network, with the reference's id() (IntVar,
+// include/Network.h:142-193). Domains stay on the device; read them through
+// Network::Domains / Sizes.
+class IntVar {
+ public:
+  explicit IntVar(int id) : id_(id) {}
+  int id() const { return id_; }
+
+ private:
+  int id_;
+};
+
 class Network {
  public:
+  // Network::vars (include/Network.h:127): the variables in id order, so that
+  // reference code such as ac->enforce(net.vars, level) compiles unchanged.
+  std::vector<IntVar*> vars;
+
   Network(Engine& engine, const ModelBuilder& model, int max_levels = 0) : n_(model.num_variables()) {
+    var_store_.reserve(n_);
+    for (int x = 0; x < n_; ++x) {
+      var_store_.emplace_back(x);
+      vars.push_back(&var_store_.back());
+    }
     int maxd = 1;
     for (int d : model.dom_) maxd = d > maxd ? d : maxd;
     W_ = (maxd + 63) / 64;
@@ -212,7 +233,15 @@ class Network {
   cp_net* net_ = nullptr;
   int n_ = 0, W_ = 1;
   std::vector<int> dom_;
+  std::vector<IntVar> var_store_;
 };
+
+inline std::vector<int> var_ids(const std::vector<IntVar*>& vs) {
+  std::vector<int> ids;
+  ids.reserve(vs.size());
+  for (const IntVar* v : vs) ids.push_back(v->id());
+  return ids;
+}
 
 // AC::enforce(x_evt, level) (include/Solver.h:315): AC_3bit on binary
 // networks, GAC with tables.
@@ -231,6 +260,8 @@ class AC {
     last_ = st;
     return cs;
   }
+  // The reference's signature (include/Solver.h:315).
+  virtual ConsistencyState enforce(std::vector<IntVar*>& x_evt, int level) { return enforce(var_ids(x_evt), level); }
   int del() const { return delete_; }
   const cp_stats& last_stats() const { return last_; }
   ConsistencyState cs;
@@ -259,6 +290,8 @@ class SAC1 {
     last_ = st;
     return st.inconsistent == 0;
   }
+  // The reference's signature (SAC1::enforce, include/Solver.h:425).
+  bool enforce(std::vector<IntVar*> x_evt, int level) { return enforce(var_ids(x_evt), level); }
   int del() const { return del_; }
   const cp_stats& last_stats() const { return last_; }
 

@@ -73,9 +73,7 @@ int main(int argc, char** argv) {
     Network net(engine, model);
     apply_init(net);
     AC3bit ac(&net);
-    std::vector<int> all;
-    for (int x = 0; x < n; ++x) all.push_back(x);
-    ConsistencyState cs = ac.enforce(all, 0);
+    ConsistencyState cs = ac.enforce(net.vars, 0);  // AC::enforce(vector<IntVar*>&, int)
     std::printf("{\"op\": \"ac3bit\", \"consistent\": %s, \"deletions\": %d, \"domains\": \"%s\"}\n",
                 cs.state ? "true" : "false", cs.num_delete, hex(net.Domains(0)).c_str());
   }
@@ -83,7 +81,7 @@ int main(int argc, char** argv) {
     Network net(engine, model);
     apply_init(net);
     SAC1 sac(&net, AC_3bit);
-    const bool ok = sac.enforce({}, 0);
+    const bool ok = sac.enforce(net.vars, 0);  // SAC1::enforce(vector<IntVar*>, int)
     std::printf("{\"op\": \"sac1\", \"consistent\": %s, \"deletions\": %d, \"domains\": \"%s\"}\n",
                 ok ? "true" : "false", sac.del(), hex(net.Domains(0)).c_str());
   }
