@@ -803,6 +803,66 @@ def run_tensor(args):
     return 0
 
 
+def run_xcsp(args):
+    """The reference's own XCSP benchmark instances (a copy of its
+    samples/bench directory given by --samples): MAC with dom/min and min
+    value order to the first solution on the GPU (one device-resident search
+    per instance, and all solved instances as one batched launch), checked
+    against the reference's node counts (tests/golden/xcsp_reference_cases.json),
+    beside the oracle's MAC on one host core and the reference's own solve
+    time from that file (measured where the reference builds)."""
+    import numpy as np
+    import cpim_gb300 as cp
+    from cpim_gb300.xcsp import read_xcsp
+    from oracle import pyoracle as O
+    with open(os.path.join(ROOT, "tests", "golden", "xcsp_reference_cases.json")) as f:
+        cases = json.load(f)["cases"]
+    rows = []
+    with cp.Engine(0) as eng:
+        solved_nets = []
+        for c in cases:
+            m = read_xcsp(os.path.join(args.samples, c["file"]))
+            ref = c["mac"]
+            if ref["time_out"]:
+                rows.append({"file": c["file"], "reference": "time out at %d ms" % ref["solve_ms"]})
+                continue
+            net = eng.upload(m.inst)
+            reps = 3 if ref["num_positive"] < 5000 else 1
+            best = 1e30
+            for _ in range(reps):
+                t0 = time.perf_counter()
+                r = net.mac_solve(time_limit_ms=300000)
+                best = min(best, time.perf_counter() - t0)
+            assert (r["num_positive"], r["num_negative"]) == (ref["num_positive"], ref["num_negative"]), c["file"]
+            solved_nets.append((net, m))
+            row = {"file": c["file"], "n": m.inst.n, "constraints": m.inst.n_bin,
+                   "nodes": ref["num_positive"] + ref["num_negative"], "solution": r["status"] == 1,
+                   "gpu_ms": best * 1e3, "reference_cpu_ms": ref["solve_ms"]}
+            if ref["num_positive"] < 50000:
+                from tests.golden_cases import oracle_view_of
+                t0 = time.perf_counter()
+                O.mac(oracle_view_of(m.inst))
+                row["oracle_cpu_ms"] = (time.perf_counter() - t0) * 1e3
+            rows.append(row)
+        t0 = time.perf_counter()
+        mb = cp.MacBatch(eng, [(n, []) for n, _ in solved_nets], time_limit_ms=300000)
+        res = mb.wait()
+        batch_s = time.perf_counter() - t0
+        mb.close()
+        for n, _ in solved_nets:
+            n.close()
+    nodes = sum(r["num_positive"] + r["num_negative"] for r in res)
+    line = {"metric": "MAC first-solution searches on the reference's XCSP instances (node counts bit-exact)",
+            "value": len(res) / batch_s, "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "the reference's samples/bench XCSP files",
+            "config": {"workload": "MAC(AC_3bit, dom/min, min value) on samples/bench (queens, composed-25-1-2, "
+                                   "rand-2-23; haystacks-11 exceeds the reference's 60 s limit)"},
+            "batch": {"searches": len(res), "wall_s": batch_s, "nodes_per_s": nodes / batch_s},
+            "instances": rows}
+    print(json.dumps(line))
+    return 0
+
+
 def run_mac(args):
     """Config-1 measurement: MAC (dom/min, min value) to the first solution on
     the plain CPU-runnable shape, seeds 1..10: the device search (one CTA per
@@ -877,12 +937,13 @@ def main():
                     help="SAC closures per timed step of the default workload")
     ap.add_argument("--no-extras", action="store_true",
                     help="default workload without the GAC and uneven-batch samples")
-    ap.add_argument("--workload", default="sac", choices=["sac", "uneven", "serving", "gac", "mac", "tensor"],
+    ap.add_argument("--workload", default="sac", choices=["sac", "uneven", "serving", "gac", "mac", "tensor", "xcsp"],
                     help="sac: the batched SAC sweep (headline); uneven: the uneven multi-instance batch; "
                          "serving: the request server under Poisson load; gac: the large GAC fixpoint; "
                          "mac: MAC searches on the plain shape; tensor: support-count tiles on the tensor cores "
-                         "against the bitwise test")
+                         "against the bitwise test; xcsp: MAC on the reference's XCSP instances (--samples)")
     ap.add_argument("--instances", type=int, default=4096, help="uneven workload: instances")
+    ap.add_argument("--samples", default="", help="xcsp workload: a copy of the reference's samples/bench directory")
     ap.add_argument("--per-instance-sample", type=int, default=256, help="uneven workload: one-by-one sample")
     ap.add_argument("--networks", type=int, default=64, help="serving: resident networks")
     ap.add_argument("--slots", type=int, default=16, help="serving: working levels per resident network")
@@ -907,6 +968,8 @@ def main():
         return run_mac(args)
     if args.workload == "tensor":
         return run_tensor(args)
+    if args.workload == "xcsp":
+        return run_xcsp(args)
     return run_ours(args)
 
 

@@ -121,3 +121,39 @@ def read_xcsp(source, max_table=200000) -> XcspModel:
                     tab_arity=np.array(t_ar, np.int32), tab_scope=np.array(t_sc, np.int32),
                     tab_ntup=np.array(t_nt, np.int32), tab_tuples=np.array(t_tu, np.int32))
     return XcspModel(inst=inst, names=names, values=values)
+
+
+def read_benchmark_list(path):
+    """The instance files a reference benchmark list names (<BenchMark>
+    <BMFiles><BMFile>path</BMFile>..., the list the reference's driver reads;
+    commented entries are not elements): each path as given, else resolved
+    against the list's own directory, else its file name in that directory;
+    type="dir" entries expand to the .xml files of the directory."""
+    import os
+    base = os.path.dirname(os.path.abspath(path))
+    out = []
+    for f in ET.parse(path).getroot().iter("BMFile"):
+        raw = (f.text or "").strip()
+        cands = [raw, os.path.join(base, raw), os.path.join(base, os.path.basename(raw))]
+        hit = next((c for c in cands if os.path.exists(c)), None)
+        if hit is None:
+            raise FileNotFoundError(raw)
+        if f.get("type") == "dir" or os.path.isdir(hit):
+            out.extend(sorted(os.path.join(hit, n) for n in os.listdir(hit) if n.endswith(".xml")))
+        else:
+            out.append(hit)
+    return out
+
+
+def dump_network(inst, path):
+    """A binary network as the text format of the reference driver's `file`
+    mode: "n W", domain sizes, initial words, "nb", scope pairs, rows."""
+    if inst.n_tab:
+        raise ValueError("binary networks only")
+    with open(path, "w") as f:
+        f.write("%d %d\n" % (inst.n, inst.W))
+        f.write(" ".join(str(int(d)) for d in inst.dom) + "\n")
+        f.write(" ".join(str(int(w)) for w in inst.init) + "\n")
+        f.write("%d\n" % inst.n_bin)
+        f.write(" ".join(str(int(v)) for v in inst.bin_scope) + "\n")
+        f.write(" ".join(str(int(w)) for w in inst.bin_rows) + "\n")

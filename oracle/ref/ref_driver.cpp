@@ -10,6 +10,9 @@
 //   ref_driver mixed  N D E P_LO P_HI K3 NTUP REMOVE SEED  OP [ARG]
 //   ref_driver mixedbin (same arguments as mixed; tables dropped)
 //   ref_driver uneven SEED N_LO N_HI D_CAP  OP [ARG]
+//   ref_driver file PATH  OP [ARG]     (a binary network dumped as text:
+//       "n W", n domain sizes, n*W initial words, "nb", nb scope pairs,
+//       then every constraint's dom(x)*W support-row words, decimal)
 // OP: ac3bit | ac3 | sac1 | mac | mac_domdeg | time_ac REPS | time_branches K |
 //     verdicts [FIRST [COUNT]]
 #include <chrono>
@@ -90,6 +93,37 @@ int main(int argc, char** argv) {
     I.ttup_off.clear();
     I.ttup.clear();
     i = 11;
+  } else if (kind == "file" && argc >= 4) {
+    // A dumped network (for instances read elsewhere, e.g. from XCSP files).
+    std::ifstream in(argv[2]);
+    if (!in) {
+      std::cerr << "cannot open " << argv[2] << std::endl;
+      return 2;
+    }
+    in >> I.n >> I.W;
+    I.dom.resize(I.n);
+    for (auto& d : I.dom) in >> d;
+    I.init.resize(size_t(I.n) * I.W);
+    for (auto& w : I.init) in >> w;
+    int nb = 0;
+    in >> nb;
+    I.bx.resize(nb);
+    I.by.resize(nb);
+    for (int c = 0; c < nb; ++c) in >> I.bx[c] >> I.by[c];
+    I.brow_off.resize(nb);
+    for (int c = 0; c < nb; ++c) {
+      I.brow_off[c] = int64_t(I.brows.size());
+      for (int64_t k = 0; k < int64_t(I.dom[I.bx[c]]) * I.W; ++k) {
+        uint64_t w = 0;
+        in >> w;
+        I.brows.push_back(w);
+      }
+    }
+    if (!in) {
+      std::cerr << "truncated network file" << std::endl;
+      return 2;
+    }
+    i = 3;
   } else if (kind == "uneven" && argc >= 7) {
     I = cpgen::uneven_instance(std::strtoull(argv[2], nullptr, 10), std::atoi(argv[3]), std::atoi(argv[4]),
                                std::atoi(argv[5]));
@@ -132,12 +166,15 @@ int main(int argc, char** argv) {
   } else if (op == "mac" || op == "mac_domdeg") {
     MAC mac(&net, AC_3bit, op == "mac" ? Heuristic::VRH_DOM_MIN : Heuristic::VRH_DOM_DEG_MIN, Heuristic::VLH_MIN);
     SearchStatistics st;
+    const double t0 = now_s();
     {
       Silence s;
       st = mac.enforce(arg > 0 ? int(arg) : 600000);
     }
+    const double t1 = now_s();
     out << ", \"num_positive\": " << st.num_positive << ", \"num_negative\": " << st.num_negative
         << ", \"num_sol\": " << st.num_sol << ", \"time_out\": " << (st.time_out ? "true" : "false")
+        << ", \"solve_ms\": " << (t1 - t0) * 1e3
         << ", \"solution\": [";
     for (size_t k = 0; k < mac.solution.size(); ++k) out << (k ? ", " : "") << mac.solution[k];
     out << "]";
