@@ -826,15 +826,16 @@ def run_xcsp(args):
             if ref["time_out"]:
                 rows.append({"file": c["file"], "reference": "time out at %d ms" % ref["solve_ms"]})
                 continue
-            net = eng.upload(m.inst)
             reps = 3 if ref["num_positive"] < 5000 else 1
             best = 1e30
             for _ in range(reps):
+                net = eng.upload(m.inst)  # a search leaves its levels changed
                 t0 = time.perf_counter()
                 r = net.mac_solve(time_limit_ms=300000)
                 best = min(best, time.perf_counter() - t0)
+                net.close()
             assert (r["num_positive"], r["num_negative"]) == (ref["num_positive"], ref["num_negative"]), c["file"]
-            solved_nets.append((net, m))
+            solved_nets.append((eng.upload(m.inst), m))
             row = {"file": c["file"], "n": m.inst.n, "constraints": m.inst.n_bin,
                    "nodes": ref["num_positive"] + ref["num_negative"], "solution": r["status"] == 1,
                    "gpu_ms": best * 1e3, "reference_cpu_ms": ref["solve_ms"]}
