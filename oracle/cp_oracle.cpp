@@ -115,6 +115,7 @@ struct AC3bit {
   size_t qh = 0, qt = 0;
   u64 t = 0;
   int64_t num_delete = 0;
+  int fail_c = -1;  // the constraint whose revision emptied a domain (cs.tab)
   explicit AC3bit(const Net& net) : N(net), stamp_var(net.n), stamp_tab(net.nc), q(net.n + 1), inq(net.n) {}
 
   void insert(int v) {
@@ -159,6 +160,7 @@ struct AC3bit {
     t = 0;
     qh = qt = 0;
     num_delete = 0;
+    fail_c = -1;
     for (int v : evt) insert(v);
     while (qh != qt) {
       const int x = pop();
@@ -171,7 +173,10 @@ struct AC3bit {
               if (z != x && stamp_var[z] > stamp_tab[c]) aa = true;
             if (y != x || aa) {
               if (revise(D, c, y)) {
-                if (dsize(D, N.W, y) == 0) return false;
+                if (dsize(D, N.W, y) == 0) {
+                  fail_c = c;
+                  return false;
+                }
                 insert(y);
               }
             }
@@ -420,7 +425,13 @@ std::vector<int> neighbour_counts(const Net& N) {
   return cnt;
 }
 
-// varh: 1 = VRH_DOM_MIN, 4 = VRH_DOM_DEG_MIN (Heuristic::Var, include/Solver.h:55-63).
+// varh: 1 = VRH_DOM_MIN, 4 = VRH_DOM_DEG_MIN, 6 = VRH_DOM_WDEG_MIN
+// (Heuristic::Var, include/Solver.h:55-63). dom/wdeg: every AC call that
+// wipes a domain out adds 1 to the weight (initially 1, src/Network.cpp:303)
+// of the constraint whose revision emptied it first in AC3::enforce's order
+// (src/AC3.cpp:122-128); a variable's score is |D(x)| over the summed weights
+// of its constraints with another unassigned variable, -1 when |D(x)| = 1 or
+// the sum is 0 (src/MAC.cpp:387-408).
 int mac(const Net& N, const u64* d0, int64_t time_limit_ms, int varh, int64_t* npos, int64_t* nneg, int* solution) {
   const auto t0 = std::chrono::steady_clock::now();
   auto elapsed_ms = [&]() {
@@ -429,8 +440,14 @@ int mac(const Net& N, const u64* d0, int64_t time_limit_ms, int varh, int64_t* n
   MacState S(N, d0);
   Prop P(N);
   const std::vector<int> deg = varh == 4 ? neighbour_counts(N) : std::vector<int>();
+  std::vector<double> weight(varh == 6 ? N.nc : 0, 1.0);
+  auto propagate = [&](u64* D, const std::vector<int>& evt, const char* A) {
+    const bool ok = P.enforce(D, evt, A, nullptr);
+    if (!ok && varh == 6 && P.ac.fail_c >= 0) weight[P.ac.fail_c] += 1.0;
+    return ok;
+  };
   *npos = *nneg = 0;
-  if (!P.enforce(S.D(0), all_vars(N.n), S.A(0), nullptr)) return 0;
+  if (!propagate(S.D(0), all_vars(N.n), S.A(0))) return 0;
   for (;;) {
     if (elapsed_ms() > double(time_limit_ms)) return 2;
     const int p = int(S.I.size());
@@ -439,8 +456,20 @@ int mac(const Net& N, const u64* d0, int64_t time_limit_ms, int varh, int64_t* n
     for (int v = 0; v < N.n; ++v) {
       if (S.A(p)[v]) continue;
       // dom/deg: integer size / |neighbourhood|, -1 for a variable without
-      // neighbours; both orders take the first strict minimum.
-      const int key = varh == 4 ? (deg[v] == 0 ? -1 : dsize(S.D(p), N.W, v) / deg[v]) : dsize(S.D(p), N.W, v);
+      // neighbours; every order takes the first strict minimum.
+      double key;
+      if (varh == 6) {
+        double w = 0.0;
+        for (int c : N.subs[v]) {
+          int free = 0;
+          for (int y : N.scope[c]) free += S.A(p)[y] ? 0 : 1;
+          if (free > 1) w += weight[c];
+        }
+        const int sz = dsize(S.D(p), N.W, v);
+        key = (sz == 1 || w == 0.0) ? -1.0 : sz / w;
+      } else {
+        key = varh == 4 ? (deg[v] == 0 ? -1 : dsize(S.D(p), N.W, v) / deg[v]) : dsize(S.D(p), N.W, v);
+      }
       if (key < min_size) {
         min_size = key;
         var = v;
@@ -453,7 +482,7 @@ int mac(const Net& N, const u64* d0, int64_t time_limit_ms, int varh, int64_t* n
     const int lv = int(S.I.size());
     reduce_to(S.D(lv), N.W, var, a);
     S.A(lv)[var] = 1;
-    bool consistent = P.enforce(S.D(lv), {var}, S.A(lv), nullptr);
+    bool consistent = propagate(S.D(lv), {var}, S.A(lv));
     if (consistent && int(S.I.size()) == N.n) {
       for (int v = 0; v < N.n; ++v) solution[v] = head(S.D(lv), N.W, v);
       return 1;
@@ -464,7 +493,7 @@ int mac(const Net& N, const u64* d0, int64_t time_limit_ms, int varh, int64_t* n
       S.back_to(q);
       del_bit(S.D(q), N.W, va.first, va.second);
       ++*nneg;
-      consistent = dsize(S.D(q), N.W, va.first) > 0 && P.enforce(S.D(q), {va.first}, S.A(q), nullptr);
+      consistent = dsize(S.D(q), N.W, va.first) > 0 && propagate(S.D(q), {va.first}, S.A(q));
       S.update_model_assigned();
     }
     if (!consistent) return 0;
@@ -657,8 +686,9 @@ int orc_mac(const OrcNet* v, const uint64_t* dom0, int64_t time_limit_ms, int64_
 
 int orc_mac_h(const OrcNet* v, const uint64_t* dom0, int64_t time_limit_ms, int varh, int64_t* num_positive,
               int64_t* num_negative, int* solution) {
-  if (varh != 1 && varh != 4) return -1;
+  if (varh != 1 && varh != 4 && varh != 6) return -1;
   Net N = build_net(v);
+  if (varh == 6 && N.nt) return -1;  // weights follow the binary AC3bit order only
   return mac(N, dom0, time_limit_ms, varh, num_positive, num_negative, solution);
 }
 

@@ -49,8 +49,8 @@ int orc_sac1(const OrcNet* net, uint64_t* dom, int64_t* deletions);
 /* status: 1 solution, 0 proved unsat, 2 time out. */
 int orc_mac(const OrcNet* net, const uint64_t* dom0, int64_t time_limit_ms, int64_t* num_positive,
             int64_t* num_negative, int* solution);
-/* The same with variable heuristic varh: 1 = VRH_DOM_MIN, 4 = VRH_DOM_DEG_MIN
- * (-1 for any other). */
+/* The same with variable heuristic varh: 1 = VRH_DOM_MIN, 4 = VRH_DOM_DEG_MIN,
+ * 6 = VRH_DOM_WDEG_MIN (binary networks) (-1 for any other). */
 int orc_mac_h(const OrcNet* net, const uint64_t* dom0, int64_t time_limit_ms, int varh, int64_t* num_positive,
               int64_t* num_negative, int* solution);
 /* The d-way search of GModelSolver (smallest domain above one value first,

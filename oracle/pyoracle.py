@@ -183,13 +183,13 @@ def sac1(inst: Instance, dom=None):
 
 
 def mac(inst: Instance, time_limit_ms=600000, varh=1):
-    """varh: 1 = VRH_DOM_MIN, 4 = VRH_DOM_DEG_MIN."""
+    """varh: 1 = VRH_DOM_MIN, 4 = VRH_DOM_DEG_MIN, 6 = VRH_DOM_WDEG_MIN."""
     npos, nneg = C.c_int64(), C.c_int64()
     sol = np.full(inst.n, -1, dtype=np.int32)
     st = lib().orc_mac_h(C.byref(inst.view()), _ptr(inst.init, C.c_uint64), time_limit_ms, varh, C.byref(npos),
                          C.byref(nneg), _ptr(sol, C.c_int))
     if st < 0:
-        raise ValueError("variable heuristic must be 1 (dom/min) or 4 (dom/deg)")
+        raise ValueError("variable heuristic must be 1 (dom/min), 4 (dom/deg) or 6 (dom/wdeg, binary networks)")
     return {"status": st, "num_positive": npos.value, "num_negative": nneg.value,
             "solution": sol.tolist() if st == 1 else []}
 

@@ -13,7 +13,7 @@
 //   ref_driver file PATH  OP [ARG]     (a binary network dumped as text:
 //       "n W", n domain sizes, n*W initial words, "nb", nb scope pairs,
 //       then every constraint's dom(x)*W support-row words, decimal)
-// OP: ac3bit | ac3 | sac1 | mac | mac_domdeg | time_ac REPS | time_branches K |
+// OP: ac3bit | ac3 | sac1 | mac | mac_domdeg | mac_domwdeg | time_ac REPS | time_branches K |
 //     verdicts [FIRST [COUNT]]
 #include <chrono>
 #include <cstdio>
@@ -163,8 +163,11 @@ int main(int argc, char** argv) {
     }
     out << ", \"consistent\": " << (ok ? "true" : "false") << ", \"deletions\": " << sac.del();
     if (ok) out << ", \"domains\": \"" << domains_hex(net, I, 0) << "\"";
-  } else if (op == "mac" || op == "mac_domdeg") {
-    MAC mac(&net, AC_3bit, op == "mac" ? Heuristic::VRH_DOM_MIN : Heuristic::VRH_DOM_DEG_MIN, Heuristic::VLH_MIN);
+  } else if (op == "mac" || op == "mac_domdeg" || op == "mac_domwdeg") {
+    const Heuristic::Var vh = op == "mac" ? Heuristic::VRH_DOM_MIN
+                              : op == "mac_domdeg" ? Heuristic::VRH_DOM_DEG_MIN
+                                                   : Heuristic::VRH_DOM_WDEG_MIN;
+    MAC mac(&net, AC_3bit, vh, Heuristic::VLH_MIN);
     SearchStatistics st;
     const double t0 = now_s();
     {

@@ -45,6 +45,10 @@ def cases():
     for s in range(1, 11):
         out.append(("cfg1", ["binary", 50, 16, 250, 0.3, 0.3, 0.0, s], "mac_domdeg"))
         out.append(("tight", ["binary", 30, 8, 120, 0.35, 0.35, 0.1, s], "mac_domdeg"))
+    # MAC with the dom/wdeg variable order (VRH_DOM_WDEG_MIN), same networks.
+    for s in range(1, 11):
+        out.append(("cfg1", ["binary", 50, 16, 250, 0.3, 0.3, 0.0, s], "mac_domwdeg"))
+        out.append(("tight", ["binary", 30, 8, 120, 0.35, 0.35, 0.1, s], "mac_domwdeg"))
     # Tight small networks: AC and SAC delete values, MAC backtracks.
     for s in range(1, 11):
         for op in ("ac3bit", "sac1", "mac"):
@@ -245,6 +249,7 @@ def run(case):
     name, args, op = case
     cmd = [DRIVER] + [str(a) for a in args] + [op]
     res = json.loads(subprocess.check_output(cmd, timeout=600))
+    res.pop("solve_ms", None)  # timings are not fixtures
     return {"name": name, "args": args, "op": op, "result": res}
 
 

@@ -197,9 +197,9 @@ def test_xcsp_instances_on_the_device(which):
 
 @pytest.mark.parametrize("mode", [0, 1])
 def test_mac_domdeg_matches_reference(golden, mode):
-    # VRH_DOM_DEG_MIN (src/MAC.cpp:371-386): the variable is chosen on the host
-    # from the device's domain sizes in either search mode; decision counts and
-    # first solutions equal the reference's own MAC runs.
+    # VRH_DOM_DEG_MIN (src/MAC.cpp:371-386): chosen inside the device search
+    # (mode 0) or on the host from the device's domain sizes (mode 1);
+    # decision counts and first solutions equal the reference's own MAC runs.
     cases = [c for c in golden if c["op"] == "mac_domdeg"]
     assert len(cases) >= 20
     with cp.Engine(0) as e:
@@ -213,3 +213,20 @@ def test_mac_domdeg_matches_reference(golden, mode):
             if m["status"] == 1:
                 assert m["solution"] == r["solution"], c["args"]
             net.close()
+
+
+def test_mac_domdeg_batched_matches_reference(golden):
+    """All dom/deg golden networks as one batched device search."""
+    cases = [c for c in golden if c["op"] == "mac_domdeg"]
+    with cp.Engine(0) as e:
+        nets = [e.upload(make_engine_instance(c["args"])) for c in cases]
+        mb = cp.MacBatch(e, [(n, []) for n in nets], var_h=cp.VarHeuristic.VRH_DOM_DEG_MIN, time_limit_ms=120000)
+        res = mb.wait()
+        mb.close()
+        for c, m in zip(cases, res):
+            r = c["result"]
+            assert (m["num_positive"], m["num_negative"]) == (r["num_positive"], r["num_negative"]), c["args"]
+            if r["num_sol"] == 1:
+                assert m["solution"] == r["solution"], c["args"]
+        for n in nets:
+            n.close()

@@ -84,10 +84,26 @@ def test_mac_domdeg_matches_reference(golden):
             assert O.check_solution(inst, m["solution"])
 
 
+def test_mac_domwdeg_matches_reference(golden):
+    # VRH_DOM_WDEG_MIN (src/MAC.cpp:387-408) with the weights AC3::enforce
+    # raises on the constraint whose revision wipes a domain out first
+    # (src/AC3.cpp:122-128): decision counts and first solution exact.
+    cases = _cases(golden, "mac_domwdeg")
+    assert len(cases) >= 20
+    for c in cases:
+        inst = make_oracle_instance(c["args"])
+        m = O.mac(inst, varh=6)
+        r = c["result"]
+        assert (m["num_positive"], m["num_negative"]) == (r["num_positive"], r["num_negative"]), c["args"]
+        assert (m["status"] == 1) == (r["num_sol"] == 1), c["args"]
+        if m["status"] == 1:
+            assert m["solution"] == r["solution"], c["args"]
+
+
 def test_mac_rejects_unknown_heuristic(golden):
     inst = make_oracle_instance(_cases(golden, "mac")[0]["args"])
     with pytest.raises(ValueError):
-        O.mac(inst, varh=6)
+        O.mac(inst, varh=5)
 
 
 def test_gac_equals_ac3bit_on_binary(golden):
