@@ -45,6 +45,7 @@ class VarHeuristic(enum.IntEnum):
     VRH_LEX = 0
     VRH_DOM_MIN = 1
     VRH_DOM_DEG_MIN = 4
+    VRH_DOM_WDEG_MIN = 6
 
 
 class ValHeuristic(enum.IntEnum):

@@ -200,6 +200,13 @@ struct cp_net {
   u64* d_levels = nullptr;
   u64* d_rel = nullptr;
   int* d_bx = nullptr;
+  int* d_nbr = nullptr;  // nbr_count on the device (dom/deg in the device search)
+  int* d_arc_con = nullptr;  // constraint id of every binary incidence (CSR order)
+  // dom/wdeg: scratch of the sequential replay (allocated on first use).
+  ReplayScratch replay{};
+  u64* d_replay_dom = nullptr;
+  uint8_t* d_replay_assigned = nullptr;
+  int* d_replay_out = nullptr;
   int* d_by = nullptr;
   int64_t* d_offA = nullptr;
   int64_t* d_offB = nullptr;
@@ -558,13 +565,18 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   std::vector<int> arc_start(n + 1, 0);
   for (int x = 0; x < n; ++x) arc_start[x + 1] = arc_start[x] + arc_deg[x];
   std::vector<Arc> arcs(static_cast<size_t>(2) * n_bin);
+  std::vector<int> arc_con(static_cast<size_t>(2) * n_bin);
   {
+    // One pass over the constraints in order: every variable's incidences are
+    // in increasing constraint order (the reference's subscription order).
     std::vector<int> fill(arc_start.begin(), arc_start.end() - 1);
     for (int c = 0; c < n_bin; ++c) {
       const int x = net->bx[c], y = net->by[c];
       // Source y: revise x against y (x's rows are the A block).
+      arc_con[fill[y]] = c;
       arcs[fill[y]++] = Arc{x, static_cast<u32>(offA[c]), static_cast<u32>(offB[c]), y};
       // Source x: revise y against x (y's rows are the B block).
+      arc_con[fill[x]] = c;
       arcs[fill[x]++] = Arc{y, static_cast<u32>(offB[c]), static_cast<u32>(offA[c]), x};
     }
   }
@@ -672,6 +684,8 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   mp.add(&d_toff, t_off.data(), n_tab);
   mp.add(&d_ttup, t_tup.data(), t_tup.size());
   mp.add(&net->d_bx, net->bx.data(), n_bin);
+  mp.add(&net->d_nbr, net->nbr_count.data(), n);
+  mp.add(&net->d_arc_con, arc_con.data(), arc_con.size());
   mp.add(&net->d_by, net->by.data(), n_bin);
   mp.add(&net->d_offA, offA.data(), n_bin);
   mp.add(&net->d_offB, offB.data(), n_bin);
@@ -1397,6 +1411,14 @@ class DeviceMAC {
   DeviceMAC(cp_net* net, int varh, int valh) : R{net}, n_(net->n), L_(net->levels), varh_(varh), valh_(valh) {
     assigned_.assign(static_cast<size_t>(L_) * n_, 0);
     top_.assign(n_, 0);
+    if (varh_ == 6) {
+      weight_.assign(net->bx.size(), 1.0);  // Tabular::weight starts at 1 (src/Network.cpp:303)
+      cons_of_.resize(n_);
+      for (size_t c = 0; c < net->bx.size(); ++c) {
+        cons_of_[net->bx[c]].push_back(static_cast<int>(c));
+        cons_of_[net->by[c]].push_back(static_cast<int>(c));
+      }
+    }
   }
 
   int solve(int64_t time_limit_ms, cp_search_result* res, int* solution) {
@@ -1406,7 +1428,7 @@ class DeviceMAC {
     };
     *res = cp_search_result{};
     bool consistent = false;
-    CP_TRY(R.node(kOpRoot, 0, 0, 0, 0, consistent));
+    CP_TRY(node(kOpRoot, 0, 0, 0, 0, consistent));
     if (!consistent) return finish(res, 0, elapsed());
     for (;;) {
       if (elapsed() > double(time_limit_ms)) return finish(res, 2, elapsed());
@@ -1420,7 +1442,7 @@ class DeviceMAC {
       ++res->num_positive;
       const int lv = static_cast<int>(I_.size());
       A(lv)[var] = 1;  // IntVar::ReduceTo marks the variable assigned
-      CP_TRY(R.node(kOpAssign, p, lv, var, val, consistent));
+      CP_TRY(node(kOpAssign, p, lv, var, val, consistent));
       if (consistent && lv == n_) {
         for (int x = 0; x < n_; ++x) solution[x] = R.head(x);
         return finish(res, 1, elapsed());
@@ -1430,7 +1452,7 @@ class DeviceMAC {
         const int q = static_cast<int>(I_.size());
         back_to(q);
         ++res->num_negative;
-        CP_TRY(R.node(kOpRefute, q, q, va.first, va.second, consistent));
+        CP_TRY(node(kOpRefute, q, q, va.first, va.second, consistent));
         update_model_assigned();
       }
       if (!consistent) return finish(res, 0, elapsed());
@@ -1443,8 +1465,53 @@ class DeviceMAC {
   std::vector<char> assigned_;
   std::vector<int> top_;
   std::vector<std::pair<int, int>> I_;
+  std::vector<double> weight_;           // dom/wdeg constraint weights
+  std::vector<std::vector<int>> cons_of_;  // dom/wdeg: constraints of each variable
 
   char* A(int p) { return &assigned_[static_cast<size_t>(p) * n_]; }
+
+  // One node (the AC call of MAC::enforce); under dom/wdeg a failing node's
+  // propagation is replayed in the reference's sequential order on the
+  // node's starting domains (copied before the node runs) to find the
+  // constraint whose weight rises.
+  int node(int op, int src, int dst, int var, int val, bool& consistent) {
+    cp_net* net = R.net;
+    cudaStream_t s = net->e->stream;
+    const size_t words = static_cast<size_t>(n_) * net->W;
+    if (varh_ == 6) {
+      CP_TRY(replay_scratch());
+      CP_CUDA(cudaMemcpyAsync(net->d_replay_dom, net->level_ptr(src), words * 8, cudaMemcpyDeviceToDevice, s));
+    }
+    CP_TRY(R.node(op, src, dst, var, val, consistent));
+    if (varh_ == 6 && !consistent) {
+      // The flags the AC call sees: the level it runs at.
+      const int lv = op == kOpAssign ? dst : src;
+      std::memcpy(net->h_sizes, A(lv), static_cast<size_t>(n_));
+      CP_CUDA(cudaMemcpyAsync(net->d_replay_assigned, net->h_sizes, static_cast<size_t>(n_), cudaMemcpyHostToDevice, s));
+      CP_CUDA(launch_ac3_replay(net->dn, net->d_arc_con, net->d_bx, net->d_by, net->d_replay_dom,
+                                net->d_replay_assigned, op, var, val, net->replay, net->d_replay_out, s));
+      ++net->e->launches;
+      int c = -1;
+      CP_CUDA(cudaMemcpyAsync(&net->h_sizes[0], net->d_replay_out, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CP_CUDA(cudaStreamSynchronize(s));
+      c = net->h_sizes[0];
+      if (c >= 0 && c < static_cast<int>(weight_.size())) weight_[c] += 1.0;
+    }
+    return CP_OK;
+  }
+  int replay_scratch() {
+    cp_net* net = R.net;
+    if (net->d_replay_out) return CP_OK;
+    const size_t nb = std::max<size_t>(1, net->bx.size());
+    CP_TRY(net->alloc(&net->replay.stamp_var, static_cast<size_t>(n_)));
+    CP_TRY(net->alloc(&net->replay.stamp_tab, nb));
+    CP_TRY(net->alloc(&net->replay.q, static_cast<size_t>(n_) + 1));
+    CP_TRY(net->alloc(&net->replay.inq, static_cast<size_t>(n_)));
+    CP_TRY(net->alloc(&net->d_replay_dom, static_cast<size_t>(n_) * net->W));
+    CP_TRY(net->alloc(&net->d_replay_assigned, static_cast<size_t>(n_)));
+    CP_TRY(net->alloc(&net->d_replay_out, 1));
+    return CP_OK;
+  }
   int finish(cp_search_result* res, int status, double ms) {
     res->status = status;
     res->propagations = R.propagations;
@@ -1454,14 +1521,28 @@ class DeviceMAC {
   // VRH_DOM_MIN (src/MAC.cpp:357-365): first unassigned variable of strictly
   // smaller size; VRH_LEX (:366-368); VRH_DOM_DEG_MIN (:371-386): the same
   // with the integer key size / |neighbourhood| (-1 without neighbours).
+  // VRH_DOM_WDEG_MIN (:387-408): |D(v)| over the summed weights of v's
+  // constraints that have another unassigned variable, -1 when |D(v)| = 1 or
+  // the sum is 0; the first strict minimum, in doubles as the reference.
   int select_var(int p) {
     if (varh_ == 0) return static_cast<int>(I_.size()) + 1 < n_ ? static_cast<int>(I_.size()) + 1 : -1;
     int var = -1;
     double min_size = 1e300;
     for (int v = 0; v < n_; ++v) {
       if (A(p)[v]) continue;
-      const int deg = R.net->nbr_count[v];
-      const int key = varh_ == 4 ? (deg == 0 ? -1 : R.size(v) / deg) : R.size(v);
+      double key;
+      if (varh_ == 6) {
+        double w = 0.0;
+        for (int c : cons_of_[v]) {
+          const int free = (A(p)[R.net->bx[c]] ? 0 : 1) + (A(p)[R.net->by[c]] ? 0 : 1);
+          if (free > 1) w += weight_[c];
+        }
+        const int sz = R.size(v);
+        key = (sz == 1 || w == 0.0) ? -1.0 : sz / w;
+      } else {
+        const int deg = R.net->nbr_count[v];
+        key = varh_ == 4 ? (deg == 0 ? -1 : R.size(v) / deg) : R.size(v);
+      }
       if (key < min_size) {
         min_size = key;
         var = v;
@@ -1746,6 +1827,7 @@ int mac_start(cp_engine* e, std::vector<MacSpec>& specs, int varh, int64_t time_
     J.net = i;
     J.levels = specs[i].levels;
     J.varh = varh;
+    J.nbr = specs[i].net->d_nbr;
     J.n_choice = static_cast<int>(ch_off[i + 1] - ch_off[i]);
     J.init = specs[i].init;
     J.stack_dom = specs[i].stack ? specs[i].stack : reinterpret_cast<u64*>(d_scratch + off_stack[i]);
@@ -1785,11 +1867,14 @@ extern "C" {
 int cp_mac_solve(cp_net* net, int var_heuristic, int val_heuristic, int64_t time_limit_ms, cp_search_result* res,
                  int* solution) {
   if (!net || !res || !solution) return fail(CP_E_ARG, "null argument");
-  if (var_heuristic != 0 && var_heuristic != 1 && var_heuristic != 4)
-    return fail(CP_E_UNSUPPORTED, "variable heuristic: 0 (VRH_LEX), 1 (VRH_DOM_MIN) or 4 (VRH_DOM_DEG_MIN)");
+  if (var_heuristic != 0 && var_heuristic != 1 && var_heuristic != 4 && var_heuristic != 6)
+    return fail(CP_E_UNSUPPORTED,
+                "variable heuristic: 0 (VRH_LEX), 1 (VRH_DOM_MIN), 4 (VRH_DOM_DEG_MIN) or 6 (VRH_DOM_WDEG_MIN)");
   if (val_heuristic != 0) return fail(CP_E_UNSUPPORTED, "value heuristic: 0 (VLH_MIN)");
-  // dom/deg is chosen on the host (the device search has the dom/min key only).
-  if (net->e->search_mode == 0 && !net->prefer_grid && var_heuristic != 4) {
+  if (var_heuristic == 6 && net->dn.nt != 0)
+    return fail(CP_E_UNSUPPORTED, "VRH_DOM_WDEG_MIN follows the binary AC3bit order: binary networks only");
+  // dom/wdeg runs host-driven: its weights come from replays of failing nodes.
+  if (net->e->search_mode == 0 && !net->prefer_grid && var_heuristic != 6) {
     // The whole search in one CTA, on the network's own level stack.
     std::vector<MacSpec> spec(1);
     spec[0].net = net;
@@ -1816,8 +1901,8 @@ int cp_mac_batch_start(cp_engine* e, int k, cp_net* const* nets, const int* n_ch
                        const int* choice_val, int var_heuristic, int val_heuristic, int64_t time_limit_ms,
                        cp_mac_batch** out) {
   if (!e || !out || k < 1 || !nets) return fail(CP_E_ARG, "bad MAC batch arguments");
-  if (var_heuristic != 0 && var_heuristic != 1)
-    return fail(CP_E_UNSUPPORTED, "variable heuristic: 0 (VRH_LEX) or 1 (VRH_DOM_MIN)");
+  if (var_heuristic != 0 && var_heuristic != 1 && var_heuristic != 4)
+    return fail(CP_E_UNSUPPORTED, "variable heuristic: 0 (VRH_LEX), 1 (VRH_DOM_MIN) or 4 (VRH_DOM_DEG_MIN)");
   if (val_heuristic != 0) return fail(CP_E_UNSUPPORTED, "value heuristic: 0 (VLH_MIN)");
   std::vector<MacSpec> spec(static_cast<size_t>(k));
   int64_t c = 0;

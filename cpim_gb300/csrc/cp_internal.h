@@ -123,7 +123,8 @@ struct MacJob {
   MacState* state;       // device memory, zeroed before the first launch
   int net;               // index into the launch's network array
   int levels;            // depth of the level stack
-  int varh;              // MAC order 1: dom/min, 0: lex; 2: the d-way search of GModelSolver
+  int varh;              // MAC order 1: dom/min, 0: lex, 4: dom/deg; 2: the d-way search of GModelSolver
+  const int* nbr;        // n neighbour counts (dom/deg), else null
   int n_choice;
   const u64* init;       // n*W words: domains before the choices
   u64* stack_dom;        // levels * n * W words
@@ -219,6 +220,20 @@ cudaError_t launch_node(const DevNet& N, u64* levels, int src, int dst, int op, 
 cudaError_t launch_ac_front(const DevNet& N, u64* level_dom, const int* evt, const int* nevt_dev, int nevt,
                             GridScratch G, KStats* st, int grid, cudaStream_t s);
 int ac_front_blocks(const DevNet& N, int narcs, int sm_count);
+// Scratch of the sequential AC3 replay (dom/wdeg weights).
+struct ReplayScratch {
+  unsigned long long* stamp_var;  // [n]
+  unsigned long long* stamp_tab;  // [nb]
+  int* q;                         // [n + 1] ring
+  uint8_t* inq;                   // [n]
+};
+// The constraint whose revision first empties a domain when AC3 runs in the
+// reference's sequential order on D (the node's domains before the edit
+// op/var/val; overwritten) with the level's assigned flags: out[0], -1 if
+// none. One warp.
+cudaError_t launch_ac3_replay(const DevNet& N, const int* arc_con, const int* bx, const int* by, u64* D,
+                              const uint8_t* assigned, int op, int var, int val, ReplayScratch R, int* out,
+                              cudaStream_t s);
 // One SAC support-count tile (cp_tensor.cu): branches x = a for a < dx, rows of
 // x over y at word offset xy; values of z (dz of them) with rows over y at zy.
 struct SacTile {

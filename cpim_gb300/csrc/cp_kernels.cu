@@ -677,8 +677,11 @@ __device__ __forceinline__ int dom_head(const u64* D, int x) {
 // (smallest size, ties to the smallest index). Block-wide. With A_p null the
 // candidates are the variables with more than one value instead
 // (GModel::GetMinDomainVar, src/GModel.cu:1553-1572).
+// With nbr (dom/deg, src/MAC.cpp:371-386) the key is |D(v)| / |neighbourhood(v)|
+// in integers, -1 for a variable without neighbours; the first strict
+// minimum in variable order either way (keys packed with the index).
 template <int WT>
-__device__ int mac_select(const u64* D, const uint8_t* A_p, int n, MacShared& sh) {
+__device__ int mac_select(const u64* D, const uint8_t* A_p, int n, MacShared& sh, const int* nbr = nullptr) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   unsigned long long best = ~0ull;
   for (int v = threadIdx.x; v < n; v += blockDim.x) {
@@ -687,7 +690,9 @@ __device__ int mac_select(const u64* D, const uint8_t* A_p, int n, MacShared& sh
 #pragma unroll
     for (int w = 0; w < WT; ++w) sz += __popcll(D[static_cast<size_t>(v) * WT + w]);
     if (!A_p && sz <= 1) continue;
-    const unsigned long long key = (static_cast<unsigned long long>(sz) << 32) | static_cast<unsigned>(v);
+    // Keys offset by one so that dom/deg's -1 sorts first as an unsigned.
+    const int k = nbr ? (nbr[v] == 0 ? -1 : sz / nbr[v]) : sz;
+    const unsigned long long key = (static_cast<unsigned long long>(k + 1) << 32) | static_cast<unsigned>(v);
     best = key < best ? key : best;
   }
 #pragma unroll
@@ -779,7 +784,8 @@ __device__ void mac_one(const DevNet& N, const MacJob& J, MacOut* out, char* bas
       status = -1;  // level stack too shallow
       break;
     }
-    const int var = J.varh == 0 ? (p + 1 < n ? p + 1 : -1) : mac_select<WT>(F.D, A + static_cast<size_t>(p) * n, n, sh);
+    const int var = J.varh == 0 ? (p + 1 < n ? p + 1 : -1)
+                                : mac_select<WT>(F.D, A + static_cast<size_t>(p) * n, n, sh, J.varh == 4 ? J.nbr : nullptr);
     if (var < 0) {
       status = -6;  // no variable to branch on
       break;
@@ -1501,6 +1507,128 @@ __global__ void __launch_bounds__(kFrontBlock, WT <= 2 ? 2 : 1) k_ac_front(DevNe
     st->inconsistent = (vloadi(F.failed) | vloadi(F.failed + 1)) ? 1 : 0;
     atomicMax(&st->rounds_max, r);
     atomicAdd(&st->fixpoints, 1ull);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_ac3_replay: AC3::enforce (src/AC3.cpp:99-141, with AC3bit's seek_support,
+// src/AC3bit.cpp:29-38, and the FIFO var_que, src/Solver.cpp:180-214) run
+// sequentially by one warp in the reference's order, only to learn which
+// constraint's revision empties a domain first: the constraint whose weight
+// the dom/wdeg order raises (src/AC3.cpp:122-128). Used for the nodes whose
+// parallel fixpoint failed. Binary networks: variable x's incidences in the
+// CSR are in increasing constraint order (the reference's subscription
+// order, src/Network.cpp:402-403), arc_con[j] their constraint ids; a
+// constraint's scope is (bx, by). D: the node's domains before its edit
+// (overwritten); assigned: the level's flags. op / var / val: the node's
+// edit (root: every variable is an event; assign: D(var) = {val}; refute:
+// val removed, no AC when D(var) empties). out[0]: the constraint, or -1.
+// ---------------------------------------------------------------------------
+// Every lane runs the same control flow on warp-uniform values (queue
+// positions, stamps, the counter t); lane 0 writes the queue, flags and
+// stamps, __syncwarp orders those writes before the next reads; a revision
+// tests 32 values of y per ballot.
+template <int WT>
+__global__ void k_ac3_replay(DevNet N, const int* arc_con, const int* bx, const int* by, u64* D,
+                             const uint8_t* assigned, int op, int var, int val, ReplayScratch R, int* out) {
+  const int lane = threadIdx.x & 31;
+  if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+  for (int i = lane; i < N.n; i += 32) {
+    R.stamp_var[i] = 0;
+    R.inq[i] = 0;
+  }
+  for (int i = lane; i < N.nb; i += 32) R.stamp_tab[i] = 0;
+  // The node's edit.
+  if (op != kOpRoot && lane < WT) {
+    u64& w = D[static_cast<size_t>(var) * WT + lane];
+    if (op == kOpRefute)
+      w &= ~((lane == (val >> 6)) ? (1ull << (val & 63)) : 0ull);
+    else
+      w = (lane == (val >> 6)) ? (1ull << (val & 63)) : 0ull;
+  }
+  __syncwarp();
+  if (lane == 0) *out = -1;
+  if (op == kOpRefute) {
+    u64 dv[WT];
+    load_dom_uniform<WT>(D + static_cast<size_t>(var) * WT, dv);
+    u64 any = 0;
+#pragma unroll
+    for (int w = 0; w < WT; ++w) any |= dv[w];
+    if (!any) return;  // MAC::enforce does not call AC on an emptied domain (src/MAC.cpp:153-154)
+  }
+  const int qcap = N.n + 1;
+  int qh = 0, qt = 0;
+  unsigned long long t = 0;
+  auto insert = [&](int v) {
+    const bool fresh = !R.inq[v];  // uniform: read after the last __syncwarp
+    __syncwarp();
+    if (lane == 0) {
+      if (fresh) {
+        R.q[qt] = v;
+        R.inq[v] = 1;
+      }
+      R.stamp_var[v] = t + 1;
+    }
+    if (fresh) qt = (qt + 1) % qcap;
+    ++t;
+    __syncwarp();
+  };
+  if (op == kOpRoot) {
+    for (int v = 0; v < N.n; ++v) insert(v);
+  } else {
+    insert(var);
+  }
+  // Each pop follows an insert, and every insert after the events follows a
+  // removal, so the loop ends; the cap only guards against a broken network.
+  long long guard = N.total_values + N.n + 2;
+  while (qh != qt && guard-- > 0) {
+    const int x = R.q[qh];
+    qh = (qh + 1) % qcap;
+    __syncwarp();
+    if (lane == 0) R.inq[x] = 0;
+    __syncwarp();
+    const int a0 = N.arc_start[x], a1 = N.arc_start[x + 1];
+    for (int j = a0; j < a1; ++j) {
+      const int c = arc_con[j];
+      if (!(R.stamp_var[x] > R.stamp_tab[c])) continue;
+      const Arc A = N.arcs[j];  // out of x: A.z the other variable
+      const int sc[2] = {bx[c], by[c]};
+      const int not_x = sc[0] == x ? sc[1] : sc[0];
+      for (int k = 0; k < 2; ++k) {
+        const int y = sc[k];
+        if (assigned[y]) continue;
+        const int other = sc[1 - k];
+        // Read now: revising the first scope variable may have stamped it.
+        const bool aa = R.stamp_var[not_x] > R.stamp_tab[c];
+        if (y == x && !aa) continue;
+        // revise(arc(c, y)): the values of y without a support in D(other).
+        const u32 rows = (y == x) ? A.yz : A.zy;
+        u64 dy[WT], dw[WT], rm[WT];
+        load_dom_uniform<WT>(D + static_cast<size_t>(y) * WT, dy);
+        load_dom_uniform<WT>(D + static_cast<size_t>(other) * WT, dw);
+#pragma unroll
+        for (int w = 0; w < WT; ++w) rm[w] = 0;
+        valuewise_removals_seq<WT>(N, rows, dw, dy, rm);
+        bool changed = false, empty = true;
+#pragma unroll
+        for (int w = 0; w < WT; ++w) {
+          changed |= rm[w] != 0;
+          empty &= (dy[w] & ~rm[w]) == 0;
+        }
+        if (!changed) continue;
+        if (lane < WT) D[static_cast<size_t>(y) * WT + lane] = sel<WT>(dy, lane) & ~sel<WT>(rm, lane);
+        __syncwarp();
+        if (empty) {
+          if (lane == 0) *out = c;
+          return;
+        }
+        insert(y);
+      }
+      ++t;
+      __syncwarp();
+      if (lane == 0) R.stamp_tab[c] = t;
+      __syncwarp();
+    }
   }
 }
 
@@ -2487,6 +2615,16 @@ cudaError_t launch_mac(const DevNet* nets, const MacJob* jobs, int njobs, int* c
   if (e != cudaSuccess) return e;
   k_mac<<<grid, block, dyn, s>>>(nets, jobs, njobs, cursor, outs, static_cast<char*>(gscratch), gstride, slice_ns);
   return cudaGetLastError();
+}
+
+cudaError_t launch_ac3_replay(const DevNet& N, const int* arc_con, const int* bx, const int* by, u64* D,
+                              const uint8_t* assigned, int op, int var, int val, ReplayScratch R, int* out,
+                              cudaStream_t s) {
+  return dispatch_w(N.W, [&](auto wt) -> cudaError_t {
+    constexpr int WT = decltype(wt)::value;
+    k_ac3_replay<WT><<<1, 32, 0, s>>>(N, arc_con, bx, by, D, assigned, op, var, val, R, out);
+    return cudaGetLastError();
+  });
 }
 
 int ac_front_max_blocks(const DevNet& N, int sm_count) {

@@ -299,8 +299,14 @@ int cp_server_run_trace(cp_server* s, int k, const double* t_arrival_s, const cp
  * heuristics (include/Solver.h:55-66: var 0 = VRH_LEX, 1 = VRH_DOM_MIN,
  * 4 = VRH_DOM_DEG_MIN; value 0 = VLH_MIN); the host keeps the reference's
  * control flow, the level stack and every propagation stay on the device.
- * VRH_DOM_DEG_MIN always runs host-driven (the variable is chosen on the host
- * from the device's domain sizes); batches take 0 and 1 only. */
+ * In the device search, dom/min and dom/deg are one block-wide minimum of
+ * (key, variable) over the unassigned variables (dom/deg: integer |D(v)| over
+ * the number of distinct neighbour variables, -1 without neighbours).
+ * 6 = VRH_DOM_WDEG_MIN (binary networks) runs host-driven: constraint weights
+ * start at 1 and rise by one for the constraint whose revision first empties
+ * a domain in the reference's sequential AC3 order (src/AC3.cpp:122-128),
+ * found by replaying each failing node's propagation in that order on the
+ * device; the variable is chosen on the host (src/MAC.cpp:387-408). */
 typedef struct cp_search_result {
   int32_t status;        /* 1 solution, 0 proved unsatisfiable, 2 time out */
   int32_t pad;

@@ -230,3 +230,24 @@ def test_mac_domdeg_batched_matches_reference(golden):
                 assert m["solution"] == r["solution"], c["args"]
         for n in nets:
             n.close()
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_mac_domwdeg_matches_reference(golden, mode):
+    # VRH_DOM_WDEG_MIN (src/MAC.cpp:387-408): weights from replays of the
+    # failing nodes in the reference's AC3 order; decision counts and first
+    # solutions equal the reference's own MAC runs (search mode does not
+    # matter: dom/wdeg always runs host-driven).
+    cases = [c for c in golden if c["op"] == "mac_domwdeg"]
+    assert len(cases) >= 20
+    with cp.Engine(0) as e:
+        e.set_search_mode(mode)
+        for c in cases:
+            net = e.upload(make_engine_instance(c["args"]))
+            m = net.mac_solve(cp.VarHeuristic.VRH_DOM_WDEG_MIN, cp.ValHeuristic.VLH_MIN, time_limit_ms=120000)
+            r = c["result"]
+            assert (m["status"] == 1) == (r["num_sol"] == 1), c["args"]
+            assert (m["num_positive"], m["num_negative"]) == (r["num_positive"], r["num_negative"]), c["args"]
+            if m["status"] == 1:
+                assert m["solution"] == r["solution"], c["args"]
+            net.close()
