@@ -523,7 +523,6 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   if (n_tab > 0 && (!tab_arity || !tab_scope || !tab_ntup || !tab_tuples)) return fail(CP_E_ARG, "null table arrays");
   const int Wi = internal_words(W);
   if (W < 1 || Wi < 0) return fail(CP_E_UNSUPPORTED, "domains wider than 512 values are not supported");
-  if (n_tab > 0 && Wi > 4) return fail(CP_E_UNSUPPORTED, "tables need domains of at most 256 values");
   for (int x = 0; x < n; ++x)
     if (dom[x] < 1 || dom[x] > 64 * W) return fail(CP_E_ARG, "domain size of variable " + std::to_string(x));
   CP_CUDA(cudaSetDevice(e->device));
@@ -581,22 +580,24 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
     }
   }
   // Tables.
-  std::vector<int> t_arity(n_tab), t_scope(static_cast<size_t>(n_tab) * kMaxArity, 0), t_ntup(n_tab);
+  std::vector<int> t_arity(n_tab), t_soff(n_tab), t_scope, t_ntup(n_tab);
   std::vector<int64_t> t_off(n_tab);
   int64_t total_tup = 0;
   {
     int64_t so = 0;
+    std::vector<int> seen(n, -1);
     for (int t = 0; t < n_tab; ++t) {
       const int r = tab_arity[t];
-      if (r < 2 || r > kMaxArity) return fail(CP_E_UNSUPPORTED, "table arity must be 2..4");
+      if (r < 2 || r > n) return fail(CP_E_ARG, "table arity must be 2..n");
       if (tab_ntup[t] < 0) return fail(CP_E_ARG, "negative tuple count");
       t_arity[t] = r;
+      t_soff[t] = static_cast<int>(t_scope.size());
       for (int i = 0; i < r; ++i) {
         const int v = tab_scope[so + i];
         if (v < 0 || v >= n) return fail(CP_E_ARG, "bad table scope " + std::to_string(t));
-        for (int j = 0; j < i; ++j)
-          if (t_scope[static_cast<size_t>(t) * kMaxArity + j] == v) return fail(CP_E_ARG, "repeated variable in table");
-        t_scope[static_cast<size_t>(t) * kMaxArity + i] = v;
+        if (seen[v] == t) return fail(CP_E_ARG, "repeated variable in table");
+        seen[v] = t;
+        t_scope.push_back(v);
         ++tab_deg[v];
       }
       so += r;
@@ -604,6 +605,7 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
       t_off[t] = total_tup;
       total_tup += static_cast<int64_t>(tab_ntup[t]) * r;
     }
+    if (so > INT32_MAX) return fail(CP_E_UNSUPPORTED, "table scopes too long");
   }
   std::vector<uint16_t> t_tup(static_cast<size_t>(total_tup));
   {
@@ -613,7 +615,7 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
       for (int j = 0; j < k; ++j)
         for (int i = 0; i < r; ++i) {
           const int v = tab_tuples[src + static_cast<int64_t>(j) * r + i];
-          const int var = t_scope[static_cast<size_t>(t) * kMaxArity + i];
+          const int var = t_scope[t_soff[t] + i];
           if (v < 0 || v >= dom[var]) return fail(CP_E_ARG, "tuple value out of range in table " + std::to_string(t));
           t_tup[t_off[t] + static_cast<int64_t>(i) * k + j] = static_cast<uint16_t>(v);
         }
@@ -633,8 +635,7 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
       for (int i = 0; i < t_arity[t]; ++i)
         for (int j = 0; j < t_arity[t]; ++j)
           if (i != j)
-            adj[t_scope[static_cast<size_t>(t) * kMaxArity + i]].push_back(
-                t_scope[static_cast<size_t>(t) * kMaxArity + j]);
+            adj[t_scope[t_soff[t] + i]].push_back(t_scope[t_soff[t] + j]);
     net->nbr_count.resize(n);
     for (int x = 0; x < n; ++x) {
       std::sort(adj[x].begin(), adj[x].end());
@@ -647,7 +648,7 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   {
     std::vector<int> fill(tinc_start.begin(), tinc_start.end() - 1);
     for (int t = 0; t < n_tab; ++t)
-      for (int i = 0; i < t_arity[t]; ++i) vtab[fill[t_scope[static_cast<size_t>(t) * kMaxArity + i]]++] = t;
+      for (int i = 0; i < t_arity[t]; ++i) vtab[fill[t_scope[t_soff[t] + i]]++] = t;
   }
   // Work-item chunking.
   const int chunk = e->chunk > 0 ? e->chunk : 8;
@@ -668,7 +669,7 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   Arc* d_arcs;
   int* d_tinc;
   int* d_vtab;
-  int *d_tar, *d_tsc, *d_tnt;
+  int *d_tar, *d_tsc, *d_tso, *d_tnt;
   int64_t* d_toff;
   uint16_t* d_ttup;
   // Metadata arrays: one device block, filled by one copy from pinned staging.
@@ -680,6 +681,7 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   mp.add(&d_vtab, vtab.data(), vtab.size());
   mp.add(&d_tar, t_arity.data(), n_tab);
   mp.add(&d_tsc, t_scope.data(), t_scope.size());
+  mp.add(&d_tso, t_soff.data(), n_tab);
   mp.add(&d_tnt, t_ntup.data(), n_tab);
   mp.add(&d_toff, t_off.data(), n_tab);
   mp.add(&d_ttup, t_tup.data(), t_tup.size());
@@ -710,6 +712,7 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   D.rel = net->d_rel;
   D.t_arity = d_tar;
   D.t_scope = d_tsc;
+  D.t_soff = d_tso;
   D.t_ntup = d_tnt;
   D.t_off = d_toff;
   D.t_tup = d_ttup;

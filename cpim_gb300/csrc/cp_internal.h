@@ -27,6 +27,9 @@ namespace cpgpu {
 using u64 = unsigned long long;
 using u32 = unsigned int;
 
+// Tables up to this arity (and at most 256 values per domain) are revised with
+// every scope position's domain and projection in registers; wider ones a few
+// positions at a time.
 constexpr int kMaxArity = 4;
 // Weak-support lists of the tiled SAC sweep: per directional arc, kWeakStride
 // words (80 bytes, 16-byte aligned): the support count of the (kWeakK+1)-th
@@ -54,7 +57,8 @@ struct DevNet {
   const int* vtab = nullptr;        // table ids per variable
   const u64* rel = nullptr;
   const int* t_arity = nullptr;
-  const int* t_scope = nullptr;     // [nt * kMaxArity]
+  const int* t_scope = nullptr;     // scopes of all tables, concatenated
+  const int* t_soff = nullptr;      // [nt] start of table t's scope in t_scope
   const int* t_ntup = nullptr;
   const int64_t* t_off = nullptr;   // offset of table t's tuples in t_tup
   const uint16_t* t_tup = nullptr;

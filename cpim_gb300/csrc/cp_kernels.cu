@@ -313,7 +313,7 @@ __device__ __forceinline__ int table_removals(const DevNet& N, const u64* D, int
   int empty_var = -1;
 #pragma unroll
   for (int i = 0; i < kMaxArity; ++i) {
-    s[i] = i < r ? N.t_scope[t * kMaxArity + i] : 0;
+    s[i] = i < r ? N.t_scope[N.t_soff[t] + i] : 0;
     u64 any = 0;
     if (i < r) {
       load_dom_uniform<WT>(D + static_cast<size_t>(s[i]) * WT, snap[i]);
@@ -366,24 +366,109 @@ __device__ __forceinline__ int table_removals(const DevNet& N, const u64* D, int
   return -1;
 }
 
+// Tables the register path above does not take (arity above kMaxArity, or
+// domains of more than 256 values): the scope positions are revised kG at a
+// time. A group's domains are snapshot in registers and its projections built
+// from the tuples valid against that snapshot and, at the other positions,
+// against the domains in memory; the group's removals are committed
+// (commit_fn(z, rm)) before the next group is computed. Domains only shrink,
+// so a tuple found invalid against a later state is invalid in every later
+// one and each removal is sound; a tuple counted valid on an earlier state of
+// another scope variable is looked at again when that variable's change
+// re-admits the table. Returns a scope variable found empty, or -1. Kept out
+// of line: its registers would otherwise count against every fixpoint kernel
+// that can meet a table.
+template <int WT, int kG, class CommitFn>
+__device__ __noinline__ int table_wide(const DevNet& N, const Fix& F, int t, Cnt& cn, CommitFn&& commit_fn) {
+  const int lane = threadIdx.x & 31;
+  const int r = N.t_arity[t];
+  const int* sc = N.t_scope + N.t_soff[t];
+  const int nt = N.t_ntup[t];
+  const uint16_t* tp = N.t_tup + N.t_off[t];
+  if (lane == 0) ++cn.rev;
+  for (int g0 = 0; g0 < r; g0 += kG) {
+    if (g0 > 0 && any_failed(F)) return -1;
+    int s[kG];
+    u64 snap[kG][WT], proj[kG][WT];
+    int empty_var = -1;
+#pragma unroll
+    for (int i = 0; i < kG; ++i) {
+      const bool in = g0 + i < r;
+      s[i] = in ? sc[g0 + i] : 0;
+      if (in) {
+        load_dom_uniform<WT>(F.D + static_cast<size_t>(s[i]) * WT, snap[i]);
+      } else {
+#pragma unroll
+        for (int w = 0; w < WT; ++w) snap[i][w] = 0;
+      }
+      u64 any = 0;
+#pragma unroll
+      for (int w = 0; w < WT; ++w) {
+        proj[i][w] = 0;
+        any |= snap[i][w];
+      }
+      if (in && any == 0) empty_var = s[i];
+    }
+    if (empty_var >= 0) return empty_var;
+    for (int k = lane; k < nt; k += 32) {
+      int v[kG];
+      bool valid = true;
+#pragma unroll
+      for (int i = 0; i < kG; ++i) {
+        v[i] = g0 + i < r ? tp[static_cast<size_t>(g0 + i) * nt + k] : 0;
+        if (g0 + i < r) valid = valid && ((sel<WT>(snap[i], v[i] >> 6) >> (v[i] & 63)) & 1ull);
+      }
+      for (int j = 0; j < r && valid; ++j) {
+        if (j >= g0 && j < g0 + kG) continue;
+        const int u = tp[static_cast<size_t>(j) * nt + k];
+        valid = (vload(F.D + static_cast<size_t>(__ldg(sc + j)) * WT + (u >> 6)) >> (u & 63)) & 1ull;
+      }
+      if (valid) {
+#pragma unroll
+        for (int i = 0; i < kG; ++i)
+          if (g0 + i < r) or_at<WT>(proj[i], v[i] >> 6, 1ull << (v[i] & 63));
+      }
+    }
+    if (lane == 0) cn.tuples += nt;
+#pragma unroll
+    for (int i = 0; i < kG; ++i)
+      if (g0 + i < r) {
+        u64 rm[WT];
+#pragma unroll
+        for (int w = 0; w < WT; ++w) rm[w] = snap[i][w] & ~warp_or64(proj[i][w]);
+        commit_fn(s[i], rm);
+      }
+  }
+  return -1;
+}
+
+// Positions a table of the given arity and domain width is revised in at a
+// time by table_wide (the register path takes the rest).
+template <int WT>
+constexpr int kWideGroup = WT <= 4 ? kMaxArity : 1;
+
 template <int WT>
 __device__ __forceinline__ void revise_table(const DevNet& N, const Fix& F, u32* qn, u32* fbn, int* qlenn, int slot,
                                              int t, Cnt& cn) {
-  if constexpr (WT > 4) {
-    return;  // tables are rejected at upload for domains wider than 256 values
-  } else {
-    const int lane = threadIdx.x & 31;
-    int s[kMaxArity], r = 0;
-    u64 rm[kMaxArity][WT];
-    const int empty_var = table_removals<WT>(N, F.D, t, s, r, rm, cn);
-    if (empty_var >= 0) {
-      if (lane == 0) set_failed(F, slot, empty_var);
+  const int lane = threadIdx.x & 31;
+  if constexpr (WT <= 4) {
+    if (N.t_arity[t] <= kMaxArity) {
+      int s[kMaxArity], r = 0;
+      u64 rm[kMaxArity][WT];
+      const int empty_var = table_removals<WT>(N, F.D, t, s, r, rm, cn);
+      if (empty_var >= 0) {
+        if (lane == 0) set_failed(F, slot, empty_var);
+        return;
+      }
+#pragma unroll
+      for (int i = 0; i < kMaxArity; ++i)
+        if (i < r) commit<WT>(N, F, qn, fbn, qlenn, slot, s[i], rm[i], cn);
       return;
     }
-#pragma unroll
-    for (int i = 0; i < kMaxArity; ++i)
-      if (i < r) commit<WT>(N, F, qn, fbn, qlenn, slot, s[i], rm[i], cn);
   }
+  const int empty_var = table_wide<WT, kWideGroup<WT>>(
+      N, F, t, cn, [&](int z, const u64 (&rm)[WT]) { commit<WT>(N, F, qn, fbn, qlenn, slot, z, rm, cn); });
+  if (empty_var >= 0 && lane == 0) set_failed(F, slot, empty_var);
 }
 
 // Work item c (chunk of incidences) of variable y.
@@ -1049,7 +1134,7 @@ __global__ void __launch_bounds__(512) k_mac(const DevNet* nets, const MacJob* j
         tab ? search_one<4, true>(sN, J, o, base, sh, slice_ns) : search_one<4, false>(sN, J, o, base, sh, slice_ns);
         break;
       default:
-        search_one<8, false>(sN, J, o, base, sh, slice_ns);
+        tab ? search_one<8, true>(sN, J, o, base, sh, slice_ns) : search_one<8, false>(sN, J, o, base, sh, slice_ns);
         break;
     }
     __syncthreads();
@@ -1349,24 +1434,30 @@ __device__ __forceinline__ void front_group(const DevNet& N, const Fix& F, const
 template <int WT>
 __device__ __forceinline__ void front_table(const DevNet& N, const Fix& F, int t, bool all, const u32* bc, u32* bn,
                                             int* fn, int slot, Cnt& cn) {
-  if constexpr (WT > 4) {
-    return;  // tables are rejected at upload for domains wider than 256 values
-  } else {
-    const int lane = threadIdx.x & 31;
-    const int ar = N.t_arity[t];
-    const bool act = lane < ar && (all || front_bit(bc, N.t_scope[t * kMaxArity + lane]));
-    if (!__any_sync(kFull, act) || any_failed(F)) return;
-    int s[kMaxArity], r = 0;
-    u64 rm[kMaxArity][WT];
-    const int empty_var = table_removals<WT>(N, F.D, t, s, r, rm, cn);
-    if (empty_var >= 0) {
-      if (lane == 0) set_failed(F, slot, empty_var);
+  const int lane = threadIdx.x & 31;
+  const int ar = N.t_arity[t];
+  const int* sc = N.t_scope + N.t_soff[t];
+  bool act = false;
+  for (int p = lane; p < ar && !act; p += 32) act = all || front_bit(bc, sc[p]);
+  if (!__any_sync(kFull, act) || any_failed(F)) return;
+  if constexpr (WT <= 4) {
+    if (ar <= kMaxArity) {
+      int s[kMaxArity], r = 0;
+      u64 rm[kMaxArity][WT];
+      const int empty_var = table_removals<WT>(N, F.D, t, s, r, rm, cn);
+      if (empty_var >= 0) {
+        if (lane == 0) set_failed(F, slot, empty_var);
+        return;
+      }
+#pragma unroll
+      for (int i = 0; i < kMaxArity; ++i)
+        if (i < r) commit_front<WT>(F, bn, fn, slot, s[i], rm[i], cn);
       return;
     }
-#pragma unroll
-    for (int i = 0; i < kMaxArity; ++i)
-      if (i < r) commit_front<WT>(F, bn, fn, slot, s[i], rm[i], cn);
   }
+  const int empty_var = table_wide<WT, kWideGroup<WT>>(
+      N, F, t, cn, [&](int z, const u64 (&rm)[WT]) { commit_front<WT>(F, bn, fn, slot, z, rm, cn); });
+  if (empty_var >= 0 && lane == 0) set_failed(F, slot, empty_var);
 }
 
 // Counters of the warps of one block summed in shared memory, then one global
@@ -2563,6 +2654,7 @@ cudaError_t dispatch_wt(const DevNet& N, F&& f) {
       case 1: return f(std::integral_constant<int, 1>{}, std::true_type{});
       case 2: return f(std::integral_constant<int, 2>{}, std::true_type{});
       case 4: return f(std::integral_constant<int, 4>{}, std::true_type{});
+      case 8: return f(std::integral_constant<int, 8>{}, std::true_type{});
       default: return cudaErrorInvalidValue;
     }
   }

@@ -7,9 +7,9 @@ walks, include/model/libxml2_parser.h:57-76): <domain> value lists with
 `v1 v2|v3 v4` with `supports` or `conflicts` semantics, and <constraint> with
 a scope and a relation reference. Values are mapped to indices 0..d-1 per
 variable in increasing order. Unary constraints filter the initial domains;
-binary ones become support rows; arity 3..4 become positive tables (a
-`conflicts` table is turned into the supports of the rest of its Cartesian
-product, which must stay below `max_table`)."""
+binary ones become support rows; those of higher arity become positive
+tables (a `conflicts` table is turned into the supports of the rest of its
+Cartesian product, which must stay below `max_table`)."""
 from __future__ import annotations
 
 import itertools
@@ -103,7 +103,7 @@ def read_xcsp(source, max_table=200000) -> XcspModel:
                         r[a * W + b // 64] |= np.uint64(1 << (b % 64))
             scopes += [x, y]
             rows.append(r)
-        elif arity <= 4:
+        else:
             if sem == "conflicts":
                 size = int(np.prod([dom[x] for x in scope]))
                 if size > max_table:
@@ -114,8 +114,6 @@ def read_xcsp(source, max_table=200000) -> XcspModel:
             t_sc += scope
             t_nt.append(len(tuples))
             t_tu += [v for t in tuples for v in t]
-        else:
-            raise ValueError("constraints of arity above 4 are not supported")
     inst = Instance(n=n, W=W, dom=dom, init=init, bin_scope=np.array(scopes, np.int32),
                     bin_rows=np.concatenate(rows) if rows else np.zeros(0, np.uint64),
                     tab_arity=np.array(t_ar, np.int32), tab_scope=np.array(t_sc, np.int32),

@@ -17,10 +17,11 @@
  *     and dom[x] support rows of W words, concatenated over c in bin_rows: row
  *     a has bit b set iff (x=a, y=b) is allowed (the rows of AC3bit::bitSup_,
  *     src/AC3bit.cpp:3-27, for the x side; the y side is derived on upload);
- *   - table t has arity tab_arity[t] (2..4), its scope in tab_scope and
- *     tab_ntup[t] tuples of positive (support) semantics in tab_tuples,
- *     arity ints per tuple, both concatenated over t (the kSupports
- *     ExtensionConstraint of include/model/types.h:148-161).
+ *   - table t has arity tab_arity[t] (2..n, distinct variables), its scope
+ *     in tab_scope and tab_ntup[t] tuples of positive (support) semantics in
+ *     tab_tuples, arity ints per tuple, both concatenated over t (the
+ *     kSupports ExtensionConstraint of include/model/types.h:148-161; any
+ *     arity, like the generic table revise of src/AC3.cpp:195-209).
  */
 #ifndef CPGPU_H
 #define CPGPU_H

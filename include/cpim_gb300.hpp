@@ -13,7 +13,7 @@
 // The model is described with ModelBuilder (a small stand-in for the
 // reference's model::ModelBuilder, include/model/model_builder.h:101-172):
 // variables with domain sizes, extension constraints with support or conflict
-// tuples. Binary constraints become support bit-rows, arity 3..4 tables stay
+// tuples. Binary constraints become support bit-rows, higher-arity tables stay
 // tuple lists. Every propagation runs in the engine; there is no CPU path.
 //
 // Header-only; link with cpim_gb300/_build/libcpgpu.so.

@@ -8,7 +8,9 @@
 //
 // It needs the reference's headers (Solver.h, Network.h) and this
 // repository's include/cpgpu.h, and links libcpgpu.so; it has no CUDA code.
-// Binary networks only, like AC3bit (src/AC3bit.cpp:3-6).
+// Constraints of any arity: binary ones become support rows (AC3bit's,
+// src/AC3bit.cpp:3-27), wider ones positive tables revised like the generic
+// AC3 (src/AC3.cpp:195-209).
 //
 // Level protocol: the reference keeps n + 3 domain levels per IntVar
 // (src/Network.cpp:78); the device network is uploaded with the same number
@@ -39,13 +41,20 @@ class GpuAC : public AC {
       dom[x] = m->vars[x]->capacity();
       pack_var(x, 0, init.data());
     }
-    // Support rows of each constraint's first variable over its second: row a,
-    // bit b set iff (a, b) is an allowed tuple (the bitSup_ rows of
-    // src/AC3bit.cpp:11-26 for scope[0]; the device derives the other side).
-    std::vector<int> scope;
+    // Support rows of each binary constraint's first variable over its
+    // second: row a, bit b set iff (a, b) is an allowed tuple (the bitSup_
+    // rows of src/AC3bit.cpp:11-26 for scope[0]; the device derives the other
+    // side). Wider constraints keep their tuple lists.
+    std::vector<int> scope, t_arity, t_scope, t_ntup, t_tuples;
     std::vector<uint64_t> rows;
     for (Tabular* c : m->tabs) {
-      if (c->scope.size() != 2) throw std::invalid_argument("GpuAC: binary constraints only");
+      if (c->scope.size() != 2) {
+        t_arity.push_back(static_cast<int>(c->scope.size()));
+        for (IntVar* v : c->scope) t_scope.push_back(v->id());
+        t_ntup.push_back(static_cast<int>(c->tuples().size()));
+        for (const auto& t : c->tuples()) t_tuples.insert(t_tuples.end(), t.begin(), t.end());
+        continue;
+      }
       IntVar* x = c->scope[0];
       IntVar* y = c->scope[1];
       scope.push_back(x->id());
@@ -55,7 +64,8 @@ class GpuAC : public AC {
       for (const auto& t : c->tuples()) rows[base + static_cast<size_t>(t[0]) * W_ + (t[1] >> 6)] |= 1ull << (t[1] & 63);
     }
     check(cp_net_upload(e_, n_, dom.data(), W_, init.data(), static_cast<int>(scope.size() / 2), scope.data(),
-                        rows.data(), 0, nullptr, nullptr, nullptr, nullptr, n_ + 3, &net_),
+                        rows.data(), static_cast<int>(t_arity.size()), t_arity.data(), t_scope.data(), t_ntup.data(),
+                        t_tuples.data(), n_ + 3, &net_),
           "cp_net_upload");
     buf_.resize(static_cast<size_t>(n_) * W_);
   }

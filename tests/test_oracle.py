@@ -154,7 +154,7 @@ def _nary_instance(seed, n=14, d=4, n_tab=5, arities=(5, 6), ntup=(14, 48)):
 
 @pytest.mark.parametrize("seed", range(1, 9))
 def test_gac_nary_matches_definition(seed):
-    # Tables beyond arity 4 (the device table revise stops at 4): the oracle's
+    # Tables beyond arity 4 (the device's wide-table path): the oracle's
     # worklist GAC equals the literal definition of samples/verify_gac.cpp,
     # every solution's values survive it, and a wipe-out has no solution.
     inst = _nary_instance(seed)
@@ -280,3 +280,25 @@ def test_singleton_verdicts_match_reference(golden):
                     got.add((x, a))
         assert got == set(map(tuple, c["result"]["failed"])), c["args"]
         assert failed == len(got)
+
+
+def test_nary_cases_pinned_by_definition():
+    # Every n-ary case the GPU tests compare against (tables of arity up to
+    # 40, domains up to 512 values, grid-sized networks of 8 values): the
+    # oracle's worklist GAC equals the literal definition, and its SAC1
+    # closure only removes more. (The literal definition takes minutes on the
+    # grid-sized network of 400 values, which is left out here.)
+    from tests.nary_cases import CASES, GRID_CASES, SEEDS, nary_arrays, to_oracle
+    cases = [(name, kw, SEEDS) for name, kw in CASES] + \
+            [(name, kw, (1, 2)) for name, kw in GRID_CASES if kw["d"] <= 64]
+    for name, kw, seeds in cases:
+        for seed in seeds:
+            inst = to_oracle(nary_arrays(seed, **kw))
+            ok1, d1, _ = O.gac(inst)
+            ok2, d2 = O.gac_definitional(inst)
+            assert ok1 == ok2, (name, seed)
+            if ok1:
+                assert np.array_equal(d1, d2), (name, seed)
+                if inst.n <= 48:
+                    oks, ds, _ = O.sac1(inst)
+                    assert not oks or np.all((ds & ~d1) == 0), (name, seed)

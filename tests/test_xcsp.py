@@ -113,6 +113,42 @@ def test_mixed_arity_unary_and_conflicts():
                 assert (int(d[x * m.inst.W + a // 64]) >> (a % 64)) & 1
 
 
+WIDE = """<instance><presentation format="XCSP 2.1"/>
+<domains><domain name="D">1..3</domain></domains>
+<variables><variable name="a" domain="D"/><variable name="b" domain="D"/><variable name="c" domain="D"/>
+<variable name="d" domain="D"/><variable name="e" domain="D"/><variable name="f" domain="D"/></variables>
+<relations>
+<relation name="S" arity="5" nbTuples="6" semantics="supports">1 2 3 1 2|2 2 2 2 2|3 1 2 3 1|1 1 1 1 1|2 3 1 3 2|3 3 3 1 1</relation>
+<relation name="K" arity="5" nbTuples="3" semantics="conflicts">2 2 2 2 2|1 1 1 1 1|3 3 3 1 1</relation>
+<relation name="L" arity="2" nbTuples="2" semantics="conflicts">1 1|2 3</relation>
+</relations>
+<constraints>
+<constraint name="c0" arity="5" scope="a b c d e" reference="S"/>
+<constraint name="c1" arity="5" scope="b c d e f" reference="K"/>
+<constraint name="c2" arity="2" scope="a f" reference="L"/>
+</constraints></instance>"""
+
+
+def test_arity_five_supports_and_conflicts():
+    # Constraints above arity 4 become positive tables (a conflicts relation
+    # as the rest of its Cartesian product); the oracle's MAC on them agrees
+    # with brute force over the XCSP semantics.
+    m = read_xcsp(WIDE)
+    assert m.inst.n_bin == 1 and m.inst.tab_arity.tolist() == [5, 5]
+    assert m.inst.tab_ntup.tolist() == [6, 3 ** 5 - 3]
+    sols, ok = _brute(WIDE)
+    r = O.mac(oracle_view_of(m.inst))
+    assert (r["status"] == 1) == bool(sols)
+    if sols:
+        assert ok(m.solution_values(r["solution"]))
+    okg, d, _ = O.gac(oracle_view_of(m.inst))
+    assert okg == bool(sols) or okg
+    for sol in sols:
+        for x, nm in enumerate(m.names):
+            a = m.values[x].index(sol[nm])
+            assert (int(d[x * m.inst.W + a // 64]) >> (a % 64)) & 1
+
+
 _REF = reference_root()
 SAMPLES = os.path.join(_REF, "samples", "bench") if _REF else ""
 
