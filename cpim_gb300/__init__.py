@@ -136,6 +136,7 @@ def lib():
         "cp_engine_device": ([vp], i),
         "cp_engine_set_priority": ([vp, i], i),
         "cp_engine_set_search_mode": ([vp, i], i),
+        "cp_engine_set_search_block": ([vp, i], i),
         "cp_engine_set_wait_budget": ([vp, i64], i),
         "cp_engine_inject_alloc_failure": ([vp, i64], i),
         "cp_mac_batch_start": ([vp, i, PV, PI, PI, PI, i, i, i64, PV], i),
@@ -281,6 +282,10 @@ class Engine:
     def set_search_mode(self, mode: int):
         """0: MAC searches run whole on the device (one CTA); 1: host-driven."""
         _check(lib().cp_engine_set_search_mode(self._h, int(mode)))
+
+    def set_search_block(self, block: int):
+        """Threads per CTA of the device searches (0: automatic)."""
+        _check(lib().cp_engine_set_search_block(self._h, int(block)))
 
     def set_cta_quota(self, quota: int):
         """Batch sweep CTAs retire after `quota` units (0: persistent)."""

@@ -78,6 +78,7 @@ struct cp_engine {
   bool sac_graphs = true;  // single-network SAC1 rounds replayed as CUDA graphs
   int cta_quota = 0;  // batch sweep CTAs retire after this many units (0: persistent)
   int search_mode = 0;  // 0: MAC searches run on the device where they fit one CTA; 1: host-driven nodes
+  int search_block = 0;  // threads per search CTA, 0: chosen per launch
   long long wait_ns = 2000000000ll;  // longest grid-barrier wait of a block (then CP_E_TIMEOUT)
   int64_t fail_alloc_after = -1;     // test hook: device allocations left before one fails (-1: off)
   std::multimap<size_t, void*> mapped_free;  // host-mapped pinned blocks (device-written results)
@@ -1770,8 +1771,18 @@ int mac_start(cp_engine* e, std::vector<MacSpec>& specs, int varh, int64_t time_
   std::vector<MacJob> jobs(k);
   std::vector<int2> ch;
   std::vector<int64_t> ch_off(k + 1, 0);
+  // Small work items when the searches leave SMs idle (unless a chunk was
+  // set with cp_engine_set_tuning): a node's fixpoint then spreads the arcs
+  // of a changed variable over the CTA's warps instead of walking chunk of
+  // them in one warp. One arc per item on networks of up to 1024 arcs (one
+  // 500-arc cfg1 search on one GB300: 0.41 ms vs 0.45 ms at four arcs and
+  // 0.65 ms at eight), one grouped pass (four arcs of one-word domains, two
+  // of two-word ones) on larger ones (46 k vs 42 k nodes/s at 1600 arcs,
+  // 18.3 k vs 16.2 k at 4000).
+  const bool spread = k < e->sm_count && e->chunk == 0;
   for (int i = 0; i < k; ++i) {
     dn[i] = specs[i].net->dn;
+    if (spread) dn[i].chunk = 2 * dn[i].nb <= 1024 ? 1 : 32 / arc_group_lanes(dn[i].W);
     ch.insert(ch.end(), specs[i].choices.begin(), specs[i].choices.end());
     ch_off[i + 1] = static_cast<int64_t>(ch.size());
   }
@@ -1808,7 +1819,7 @@ int mac_start(cp_engine* e, std::vector<MacSpec>& specs, int varh, int64_t time_
   // 1.65x the node rate of 256 on networks of a few thousand arcs).
   int max_inc = 0;
   for (const MacSpec& sp : specs) max_inc = std::max(max_inc, 2 * sp.net->nb + sp.net->nt);
-  const int block = (max_inc <= 2048 && k >= 2 * e->sm_count) ? 64 : 512;
+  const int block = e->search_block > 0 ? e->search_block : (max_inc <= 2048 && k >= 2 * e->sm_count) ? 64 : 512;
   const int per_sm = mac_blocks_per_sm(block, smem_mode ? max_state : 0);
   if (per_sm < 1) return fail(CP_E_UNSUPPORTED, "MAC kernel does not fit on an SM");
   const int grid = std::min(k, per_sm * e->sm_count);
@@ -1897,6 +1908,13 @@ int cp_engine_set_search_mode(cp_engine* e, int mode) {
   if (!e) return fail(CP_E_ARG, "null engine");
   if (mode != 0 && mode != 1) return fail(CP_E_ARG, "search mode must be 0 (device) or 1 (host-driven)");
   e->search_mode = mode;
+  return CP_OK;
+}
+
+int cp_engine_set_search_block(cp_engine* e, int block) {
+  if (!e) return fail(CP_E_ARG, "null engine");
+  if (block < 0 || block > 512 || block % 32) return fail(CP_E_ARG, "search block must be 0 or a multiple of 32 up to 512");
+  e->search_block = block;
   return CP_OK;
 }
 

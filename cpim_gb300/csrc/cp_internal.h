@@ -31,6 +31,11 @@ using u32 = unsigned int;
 // every scope position's domain and projection in registers; wider ones a few
 // positions at a time.
 constexpr int kMaxArity = 4;
+// Lanes that revise one binary arc together in the CTA fixpoints, by domain
+// words: each lane tests at most 8 values per pass, so a warp revises 4 arcs
+// at once for domains of up to 64 values and 2 for up to 128; wider domains
+// take the whole warp per arc.
+__host__ __device__ constexpr int arc_group_lanes(int W) { return W == 1 ? 8 : W == 2 ? 16 : 32; }
 // Weak-support lists of the tiled SAC sweep: per directional arc, kWeakStride
 // words (80 bytes, 16-byte aligned): the support count of the (kWeakK+1)-th
 // weakest value, then the kWeakK values of the revised variable with the

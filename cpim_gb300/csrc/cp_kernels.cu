@@ -296,6 +296,107 @@ __device__ __forceinline__ void revise_arc(const DevNet& N, const Fix& F, u32* q
   commit<WT>(N, F, qn, fbn, qlenn, slot, z, rm, cn);
 }
 
+// OR over the lanes of gmask (group-uniform result).
+__device__ __forceinline__ u64 group_or64(u64 x, u32 gmask) {
+  const u32 lo = __reduce_or_sync(gmask, static_cast<u32>(x));
+  const u32 hi = __reduce_or_sync(gmask, static_cast<u32>(x >> 32));
+  return (static_cast<u64>(hi) << 32) | lo;
+}
+
+// Revises na (2 .. 32 / G) arcs of y at once, arc g by the G lanes of group
+// g (G = arc_group_lanes(WT)), with the same choice per arc as revise_arc:
+// the union of the supports of D(y) when y has fewer live values than z, else
+// each live value of z tests its row against D(y); G values per pass, one per
+// lane. D(y) is warp-uniform, D(z) and everything that steers a group's
+// collective calls group-uniform; groups without an arc stay idle.
+template <int WT>
+__device__ __forceinline__ void revise_arcs_grouped(const DevNet& N, const Fix& F, u32* qn, u32* fbn, int* qlenn,
+                                                    int slot, int y, const Arc* arcs, int na, Cnt& cn) {
+  constexpr int G = arc_group_lanes(WT);
+  static_assert(G < 32, "grouped revision needs several arcs per warp");
+  constexpr u32 kLow = (1u << G) - 1u;
+  const int lane = threadIdx.x & 31, g = lane / G, li = lane % G;
+  const u32 gmask = kLow << (g * G);
+  const bool act = g < na;
+  const Arc A = arcs[act ? g : 0];
+  const int z = A.z;
+  u64 dy[WT];
+  load_dom_uniform<WT>(F.D + static_cast<size_t>(y) * WT, dy);
+  const u64 mine = li < WT ? vload(F.D + static_cast<size_t>(z) * WT + li) : 0ull;
+  u64 dz[WT];
+  int cy = 0, cz = 0;
+#pragma unroll
+  for (int w = 0; w < WT; ++w) {
+    dz[w] = __shfl_sync(kFull, mine, w, G);
+    cy += __popcll(dy[w]);
+    cz += __popcll(dz[w]);
+  }
+  if (act && li == 0) ++cn.rev;
+  const bool empty = cy == 0 || cz == 0;
+  if (act && empty && li == 0) set_failed(F, slot, cy == 0 ? y : z);
+  const bool live = act && !empty;
+  const bool by_union = cy < cz;
+  const u32 off = by_union ? A.yz : A.zy;
+  u64 acc[WT], rm[WT];
+#pragma unroll
+  for (int w = 0; w < WT; ++w) acc[w] = rm[w] = 0;
+  bool done = !live;
+#pragma unroll
+  for (int base = 0; base < 64 * WT; base += G) {
+    const u64 src = by_union ? dy[base >> 6] : dz[base >> 6];
+    const u32 bits = done ? 0u : static_cast<u32>(src >> (base & 63)) & kLow;
+    if (__ballot_sync(kFull, bits != 0) == 0) continue;
+    bool unsup = false;
+    if ((bits >> li) & 1u) {
+      u64 r[WT];
+      load_row<WT>(N.rel, off + static_cast<size_t>(base + li) * WT, r);
+      ++cn.rows;
+      u64 hit = 0;
+#pragma unroll
+      for (int w = 0; w < WT; ++w) {
+        acc[w] |= r[w];
+        hit |= r[w] & dy[w];
+      }
+      unsup = !by_union && hit == 0;
+    }
+    const u32 m = __ballot_sync(kFull, unsup);
+    rm[base >> 6] |= static_cast<u64>((m >> (g * G)) & kLow) << (base & 63);
+    if (by_union && !done) {
+      u64 gap = 0;
+#pragma unroll
+      for (int w = 0; w < WT; ++w) gap |= dz[w] & ~group_or64(acc[w], gmask);
+      done = gap == 0;
+    }
+  }
+  if (by_union) {
+#pragma unroll
+    for (int w = 0; w < WT; ++w) rm[w] = dz[w] & ~group_or64(acc[w], gmask);
+  }
+  // Commit: remove rm from D(z); a group whose removal changed D(z) checks
+  // for wipe-out and admits z to the next round.
+  u64 newly = 0;
+  if (live && li < WT) {
+    const u64 r = sel<WT>(rm, li);
+    if (r) {
+      const u64 old = atomicAnd(F.D + static_cast<size_t>(z) * WT + li, ~r);
+      newly = old & r;
+    }
+  }
+  const u32 nb = __ballot_sync(kFull, newly != 0);
+  if (nb == 0) return;
+  cn.dels += __popcll(newly);
+  __threadfence_block();
+  const bool changed = (nb & gmask) != 0;
+  const u64 cur = (changed && li < WT) ? vload(F.D + static_cast<size_t>(z) * WT + li) : 0ull;
+  const u32 ne = __ballot_sync(kFull, cur != 0);
+  if (changed && li == 0) {
+    if ((ne & gmask) == 0)
+      set_failed(F, slot, z);
+    else
+      append_var(qn, fbn, qlenn, z);
+  }
+}
+
 // Table revision (GAC on a positive table, the definition of
 // samples/verify_gac.cpp:121-164): a tuple is valid iff every coordinate is
 // in its variable's domain; each scope variable keeps exactly the values that
@@ -481,24 +582,41 @@ __device__ __forceinline__ void process_item(const DevNet& N, const Fix& F, int 
   const int t0 = N.tinc_start[y], dt = N.tinc_start[y + 1] - t0;
   const int lo = c * N.chunk;
   const int hi = min(lo + N.chunk, da + dt);
-  for (int i = lo; i < hi; ++i) {
+  for (int i = lo; i < hi;) {
     if (i < da) {
       if (any_failed(F)) return;
-      const Arc A = N.arcs[a0 + i];
-      u64 dy[WT];
-      load_dom_uniform<WT>(F.D + static_cast<size_t>(y) * WT, dy);
-      int cy = 0;
+      const int left = min(hi, da) - i;
+      bool grouped = false;
+      if constexpr (arc_group_lanes(WT) < 32) {
+        if (left >= 2) {
+          // Several arcs left in the item: one lane group per arc.
+          const int na = min(32 / arc_group_lanes(WT), left);
+          revise_arcs_grouped<WT>(N, F, qn, fbn, qlenn, slot, y, N.arcs + a0 + i, na, cn);
+          i += na;
+          grouped = true;
+        }
+      }
+      if (!grouped) {
+        const Arc A = N.arcs[a0 + i];
+        u64 dy[WT];
+        load_dom_uniform<WT>(F.D + static_cast<size_t>(y) * WT, dy);
+        int cy = 0;
 #pragma unroll
-      for (int w = 0; w < WT; ++w) cy += __popcll(dy[w]);
-      revise_arc<WT>(N, F, qn, fbn, qlenn, slot, y, dy, cy, A, cn);
+        for (int w = 0; w < WT; ++w) cy += __popcll(dy[w]);
+        revise_arc<WT>(N, F, qn, fbn, qlenn, slot, y, dy, cy, A, cn);
+        ++i;
+      }
     } else if constexpr (kTab) {
       if (any_failed(F)) return;
       const int t = N.vtab[t0 + i - da];
+      ++i;
       int prev = 0;
       if (lane == 0) prev = atomicMax(F.tstamp + t, stamp);
       prev = __shfl_sync(kFull, prev, 0);
       if (prev >= stamp) continue;
       revise_table<WT>(N, F, qn, fbn, qlenn, slot, t, cn);
+    } else {
+      break;
     }
   }
 }
@@ -510,6 +628,23 @@ __device__ __forceinline__ int cta_round_items(const DevNet& N, const u32* q, in
   __shared__ int s_w[32];
   __shared__ int s_carry;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (len <= 32) {
+    // One warp scans a short queue (the usual round of a search node): one
+    // barrier instead of the block scan's five.
+    if (warp == 0) {
+      const int v = lane < len ? var_chunks(N, static_cast<int>(q[lane])) : 0;
+      int x = v;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(kFull, x, o);
+        if (lane >= o) x += y;
+      }
+      if (lane < len) pre[lane] = x - v;
+      if (lane == 31) pre[len] = x;
+    }
+    __syncthreads();
+    return pre[len];
+  }
   if (threadIdx.x == 0) s_carry = 0;
   __syncthreads();
   for (int base = 0; base < len; base += blockDim.x) {

@@ -323,6 +323,10 @@ int cp_mac_solve(cp_net* net, int var_heuristic, int val_heuristic, int64_t time
  * in one CTA (node counts and solutions are those of the host-driven search);
  * 1 drives every node from the host. */
 int cp_engine_set_search_mode(cp_engine* e, int mode);
+/* Threads per CTA of the device searches (cp_mac_solve, cp_gsolver_solve,
+ * cp_mac_batch_*): a multiple of 32 in 32..512, or 0 (default) to choose from
+ * the number of searches and the network sizes. Results are identical. */
+int cp_engine_set_search_block(cp_engine* e, int block);
 /* Many MAC searches in one launch (one CTA per search, CTAs take searches
  * from a queue). Search i runs on nets[i] from its level 0 with the next
  * n_choice[i] (choice_var, choice_val) pairs reduced to single values (n_choice
