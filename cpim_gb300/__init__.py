@@ -95,6 +95,7 @@ def lib():
         "cp_net_destroy": ([vp], i),
         "cp_net_device_bytes": ([vp], i64),
         "cp_net_reload": ([vp, P64, P64], i),
+        "cp_net_reload_async": ([vp, P64, P64], i),
         "cp_level_copy": ([vp, i, i], i),
         "cp_dom_get": ([vp, i, P64], i),
         "cp_dom_set": ([vp, i, P64], i),
@@ -334,6 +335,11 @@ class Net:
 
     def reload(self, inst: Instance):
         _check(lib().cp_net_reload(self._h, _p(inst.init, C.c_uint64), _p(inst.bin_rows, C.c_uint64)))
+
+    def reload_async(self, inst: Instance):
+        """reload, queued on the engine's stream; inst's arrays must stay
+        alive and unchanged until this network's next call."""
+        _check(lib().cp_net_reload_async(self._h, _p(inst.init, C.c_uint64), _p(inst.bin_rows, C.c_uint64)))
 
     # -- level stack --
     def dom_get(self, level=0) -> np.ndarray:

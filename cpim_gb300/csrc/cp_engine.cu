@@ -64,6 +64,10 @@ void cpgpu::set_last_error(const std::string& msg) { g_last_error = msg; }
 struct cp_engine {
   int device = 0;
   cudaStream_t stream = nullptr;
+  // Asynchronous reloads: copies and the derivation of the other relation
+  // side run on a lowest-priority stream; the engine's stream waits on xfer_ev.
+  cudaStream_t xfer = nullptr;
+  cudaEvent_t xfer_ev = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
   int sm_count = 0;
   size_t smem_optin = 0;
@@ -221,6 +225,7 @@ struct cp_net {
   int* d_sizes = nullptr;     // n
   uint8_t* d_ok1 = nullptr;   // per-test results of the plain path
   u64* h_dom = nullptr;       // pinned n*W
+  bool h_dom_pending = false; // an asynchronous reload may still be reading h_dom
   int* h_sizes = nullptr;     // pinned n
   void* d_cta_scratch = nullptr;  // k_node state when shared memory is too small
   void* d_sac_scratch = nullptr;
@@ -432,6 +437,11 @@ static void engine_free(cp_engine* e) {
   if (e->ev1) cudaEventDestroy(e->ev1);
   if (e->evk0) cudaEventDestroy(e->evk0);
   if (e->evk1) cudaEventDestroy(e->evk1);
+  if (e->xfer) {
+    cudaStreamSynchronize(e->xfer);
+    cudaStreamDestroy(e->xfer);
+  }
+  if (e->xfer_ev) cudaEventDestroy(e->xfer_ev);
   if (e->stream) cudaStreamDestroy(e->stream);
   delete e;
 }
@@ -827,10 +837,32 @@ int cp_net_upload(cp_engine* e, int n, const int* dom, int W, const uint64_t* in
                          tab_tuples, max_levels, out, false);
 }
 
-int cp_net_reload(cp_net* net, const uint64_t* init, const uint64_t* bin_rows) {
+// Waits for an asynchronous reload's copy out of h_dom before the host
+// writes h_dom again.
+static int settle_h_dom(cp_net* net) {
+  if (net->h_dom_pending) {
+    CP_CUDA(cudaStreamSynchronize(net->e->xfer));
+    net->h_dom_pending = false;
+  }
+  return CP_OK;
+}
+
+static int net_reload_impl(cp_net* net, const uint64_t* init, const uint64_t* bin_rows, bool wait) {
   if (!net) return fail(CP_E_ARG, "null net");
   cp_engine* e = net->e;
-  cudaStream_t s = e->stream;
+  CP_TRY(settle_h_dom(net));
+  if (!wait && !e->xfer) {
+    int least = 0, greatest = 0;
+    CP_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    CP_CUDA(cudaStreamCreateWithPriority(&e->xfer, cudaStreamNonBlocking, least));
+    CP_CUDA(cudaEventCreateWithFlags(&e->xfer_ev, cudaEventDisableTiming));
+  }
+  // The asynchronous form queues behind the engine's earlier work.
+  if (!wait) {
+    CP_CUDA(cudaEventRecord(e->xfer_ev, e->stream));
+    CP_CUDA(cudaStreamWaitEvent(e->xfer, e->xfer_ev, 0));
+  }
+  cudaStream_t s = wait ? e->stream : e->xfer;
   const int W = net->W_user, Wi = net->W, n = net->n;
   if (net->nb > 0 && bin_rows) {
     if (W == Wi) {
@@ -847,7 +879,7 @@ int cp_net_reload(cp_net* net, const uint64_t* init, const uint64_t* bin_rows) {
       CP_CUDA(cudaMemcpyAsync(net->d_rel, pad.data(), pad.size() * 8, cudaMemcpyHostToDevice, s));
       CP_CUDA(cudaStreamSynchronize(s));
     }
-    CP_CUDA(cudaMemsetAsync(net->d_rel + net->relA_words, 0, static_cast<size_t>(net->relB_words) * 8, s));
+    // k_transpose writes every word of the B blocks (dom[y] rows each).
     CP_CUDA(launch_transpose(net->dn, net->d_rel, net->d_bx, net->d_by, net->d_offA, net->d_offB, s));
     ++e->launches;
   }
@@ -863,8 +895,22 @@ int cp_net_reload(cp_net* net, const uint64_t* init, const uint64_t* bin_rows) {
       }
     CP_CUDA(cudaMemcpyAsync(net->d_levels, net->h_dom, static_cast<size_t>(n) * Wi * 8, cudaMemcpyHostToDevice, s));
   }
-  CP_CUDA(cudaStreamSynchronize(s));
+  if (wait) {
+    CP_CUDA(cudaStreamSynchronize(s));
+  } else {
+    CP_CUDA(cudaEventRecord(e->xfer_ev, s));
+    CP_CUDA(cudaStreamWaitEvent(e->stream, e->xfer_ev, 0));
+    net->h_dom_pending = init != nullptr;
+  }
   return CP_OK;
+}
+
+int cp_net_reload(cp_net* net, const uint64_t* init, const uint64_t* bin_rows) {
+  return net_reload_impl(net, init, bin_rows, true);
+}
+
+int cp_net_reload_async(cp_net* net, const uint64_t* init, const uint64_t* bin_rows) {
+  return net_reload_impl(net, init, bin_rows, false);
 }
 
 int cp_net_destroy(cp_net* net) {
@@ -899,6 +945,7 @@ int cp_dom_get(cp_net* net, int level, uint64_t* out) {
 int cp_dom_set(cp_net* net, int level, const uint64_t* in) {
   if (!net || !in) return fail(CP_E_ARG, "null argument");
   CP_TRY(check_level(net, level));
+  CP_TRY(settle_h_dom(net));
   const int W = net->W_user, Wi = net->W;
   for (int x = 0; x < net->n; ++x)
     for (int w = 0; w < Wi; ++w) {
@@ -2133,11 +2180,8 @@ static int upload_generated(cp_engine* e, const cpgen::Instance& I, int max_leve
       err = cudaMemcpyAsync(d_thr, I.bthr.data(), I.bthr.size() * sizeof(u32), cudaMemcpyHostToDevice, e->stream);
     if (err == cudaSuccess)
       err = launch_gen_rows(net->dn, net->d_rel, net->d_bx, net->d_by, net->d_offA, d_seed, d_thr, e->stream);
-    if (err == cudaSuccess) {
-      err = cudaMemsetAsync(net->d_rel + net->relA_words, 0, static_cast<size_t>(net->relB_words) * 8, e->stream);
-      if (err == cudaSuccess)
-        err = launch_transpose(net->dn, net->d_rel, net->d_bx, net->d_by, net->d_offA, net->d_offB, e->stream);
-    }
+    if (err == cudaSuccess)  // k_transpose writes every word of the B blocks
+      err = launch_transpose(net->dn, net->d_rel, net->d_bx, net->d_by, net->d_offA, net->d_offB, e->stream);
     if (err == cudaSuccess) err = cudaStreamSynchronize(e->stream);
     e->launches += 2;
     e->dev_free(d_seed);

@@ -120,6 +120,14 @@ int64_t cp_net_device_bytes(const cp_net* net);
 /* Replaces the relation rows of an uploaded network with new host rows of the
  * same shape (a fresh upload of the same instance without reallocation). */
 int cp_net_reload(cp_net* net, const uint64_t* init, const uint64_t* bin_rows);
+/* The same, returning once the copies (and the device-side derivation of the
+ * other relation side) are queued on a lowest-priority transfer stream of
+ * the engine that its own stream then waits on: work of other engines
+ * proceeds meanwhile (with a higher stream priority, cp_engine_set_priority,
+ * it keeps the SMs first), and this network's next call runs after the
+ * reload. bin_rows must stay unchanged until that call (pinned memory
+ * overlaps the copy with other work). No counterpart in the reference. */
+int cp_net_reload_async(cp_net* net, const uint64_t* init, const uint64_t* bin_rows);
 
 /* ---- level stack (Network::NewLevel/BackTo/CopyLevel, src/Network.cpp:438-455;
  *      IntVar::RemoveValue/ReduceTo, :106-118; GModel level API,

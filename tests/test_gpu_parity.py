@@ -285,3 +285,55 @@ def test_sac_graph_rounds_equal_direct(args):
                         assert np.array_equal(net.dom_get(level), d_o), (graphs, level)
                         assert st.deletions == dels_o, (graphs, level)
             net.close()
+
+
+def test_reload_sync_and_async_match_oracle():
+    # cp_net_reload / cp_net_reload_async replace the relations and domains of
+    # an uploaded network with those of another instance of the same shape;
+    # two engines alternate with the next reload queued while the current
+    # closure runs, and every closure equals the oracle's SAC1 of the
+    # instance it was given.
+    base = cp.gen_binary(60, 24, 300, 0.45, 0.45, 0.1, 3)
+    rng = np.random.default_rng(11)
+    insts = []
+    for k in range(4):  # same scopes, other rows and initial domains
+        keep = rng.integers(0, 2 ** 63, size=base.bin_rows.shape, dtype=np.int64).astype(np.uint64)
+        keep |= rng.integers(0, 2 ** 63, size=base.bin_rows.shape, dtype=np.int64).astype(np.uint64)
+        init = base.init & ~(np.uint64(1) << rng.integers(0, 24, size=base.init.shape).astype(np.uint64))
+        insts.append(cp.Instance(n=base.n, W=base.W, dom=base.dom, init=init, bin_scope=base.bin_scope,
+                                 bin_rows=base.bin_rows & keep, tab_arity=base.tab_arity, tab_scope=base.tab_scope,
+                                 tab_ntup=base.tab_ntup, tab_tuples=base.tab_tuples))
+    want = [O.sac1(oracle_view_of(i)) for i in insts]
+    with cp.Engine(0) as e1, cp.Engine(0) as e2:
+        nets = (e1.upload(base, max_levels=2), e2.upload(base, max_levels=2))
+        for k, inst in enumerate(insts):
+            nets[0].reload(inst)
+            st = nets[0].enforce_sac1(0)
+            ok, d, dels = want[k]
+            assert bool(st.inconsistent) == (not ok)
+            if ok:
+                assert np.array_equal(nets[0].dom_get(0), d)
+        order = [2, 0, 3, 1, 1, 2]
+        nets[0].reload_async(insts[order[0]])
+        for i, k in enumerate(order):
+            cur = nets[i % 2]
+            if i + 1 < len(order):
+                nets[(i + 1) % 2].reload_async(insts[order[i + 1]])
+            st = cur.enforce_sac1(0)
+            ok, d, dels = want[k]
+            assert bool(st.inconsistent) == (not ok), (i, k)
+            if ok:
+                assert np.array_equal(cur.dom_get(0), d), (i, k)
+                assert st.deletions == dels
+        # A host write of the domains right after an asynchronous reload waits
+        # for the reload's copy out of the shared staging buffer.
+        nets[0].reload_async(insts[0])
+        nets[0].dom_set(0, insts[1].init)
+        nets[0].reload(insts[1])
+        st = nets[0].enforce_sac1(0)
+        ok, d, _ = want[1]
+        assert bool(st.inconsistent) == (not ok)
+        if ok:
+            assert np.array_equal(nets[0].dom_get(0), d)
+        for n in nets:
+            n.close()
