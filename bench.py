@@ -421,10 +421,19 @@ def run_ours(args):
                            tab_ntup=inst.tab_ntup, tab_tuples=inst.tab_tuples)
     out = np.zeros(inst.n * inst.W, np.uint64)
 
+    parts = {"reload": [], "enforce": [], "dom_get": []}
+
     def e2e_closure():
+        t0 = time.perf_counter()
         net.reload(e2e_inst)
+        t1 = time.perf_counter()
         st = net.enforce_sac1(0)
+        t2 = time.perf_counter()
         r = net.dom_get(0)
+        t3 = time.perf_counter()
+        parts["reload"].append(t1 - t0)
+        parts["enforce"].append(t2 - t1)
+        parts["dom_get"].append(t3 - t2)
         return st, r
 
     # Pipelined: two engines, one copy of the network each; while one engine
@@ -469,6 +478,20 @@ def run_ours(args):
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     _, _, e2e_value = job_rate(e2e_br, e2e_s, device="cuda")
+    # What bounds it: the host-to-device bandwidth of the relation rows
+    # (torch copy of the same pinned buffer) and the per-call wall times of
+    # the sequential leg.
+    dev_rows = torch.empty(rows_pin.numel(), dtype=torch.int64, device="cuda")
+    h2d = []
+    for _ in range(10):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dev_rows.copy_(rows_pin, non_blocking=True)
+        torch.cuda.synchronize()
+        h2d.append(time.perf_counter() - t0)
+    e2e_parts = {k + "_us": 1e6 * float(np.median(v)) for k, v in parts.items()}
+    e2e_parts["h2d_rows_gb_per_s"] = rows_pin.numel() * 8 / float(np.median(h2d)) / 1e9
+    del dev_rows
 
     # Plain single-instance path: one launch per singleton test (sample).
     rng = np.random.default_rng(1)
@@ -507,7 +530,7 @@ def run_ours(args):
                 "d2h_bytes_per_step": int(R * out.nbytes), "steps": e2e_steps,
                 "mode": "each closure's upload overlapped with the previous closure on a second engine "
                         "(cp_net_reload_async)",
-                "sequential_value": e2e_seq_value},
+                "sequential_value": e2e_seq_value, "sequential_median_per_call": e2e_parts},
         "gpu_launches": int(gpu_launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
