@@ -96,6 +96,10 @@ def lib():
         "cp_net_device_bytes": ([vp], i64),
         "cp_net_reload": ([vp, P64, P64], i),
         "cp_net_reload_async": ([vp, P64, P64], i),
+        "cp_level_push": ([vp, i, PI], i),
+        "cp_level_pop_to": ([vp, i], i),
+        "cp_level_top": ([vp], i),
+        "cp_dom_set_var": ([vp, i, i, P64], i),
         "cp_level_copy": ([vp, i, i], i),
         "cp_dom_get": ([vp, i, P64], i),
         "cp_dom_set": ([vp, i, P64], i),
@@ -148,6 +152,7 @@ def lib():
         "cp_engine_set_cta_quota": ([vp, i], i),
         "cp_submit_instance": ([vp, i, vp, C.POINTER(C.c_int64)], i),
         "cp_wait": ([vp, i64, i64, vp], i),
+        "cp_poll": ([vp, i64, vp], i),
         "cp_result_domains": ([vp, i64, P64], i),
         "cp_result_solution": ([vp, i64, PI], i),
         "cp_release": ([vp, i64], i),
@@ -346,6 +351,25 @@ class Net:
         out = np.zeros(self.n * self.W, np.uint64)
         _check(lib().cp_dom_get(self._h, level, _p(out, C.c_uint64)))
         return out
+
+    def level_push(self, src: int) -> int:
+        """Network::NewLevel: level src + 1 := level src; returns src + 1."""
+        out = C.c_int()
+        _check(lib().cp_level_push(self._h, int(src), C.byref(out)))
+        return out.value
+
+    def level_pop_to(self, level: int):
+        """Network::BackTo: level becomes the top."""
+        _check(lib().cp_level_pop_to(self._h, int(level)))
+
+    def level_top(self) -> int:
+        return int(lib().cp_level_top(self._h))
+
+    def dom_set_var(self, level, var, words):
+        w = np.ascontiguousarray(words, dtype=np.uint64)
+        if w.size < self.W:
+            raise ValueError("need W words")
+        _check(lib().cp_dom_set_var(self._h, int(level), int(var), _p(w, C.c_uint64)))
 
     def dom_set(self, level, words):
         w = np.ascontiguousarray(words, dtype=np.uint64)
@@ -751,6 +775,15 @@ class Server:
     def wait(self, ticket: int, timeout_ms: int = 600000) -> Result:
         r = Result()
         _check(lib().cp_wait(self._h, ticket, timeout_ms, C.byref(r)))
+        return r
+
+    def poll(self, ticket: int):
+        """The request's Result once done, else None (still queued or running)."""
+        r = Result()
+        rc = lib().cp_poll(self._h, ticket, C.byref(r))
+        if rc == 1:
+            return None
+        _check(rc)
         return r
 
     def domains(self, ticket: int, n: int, W: int) -> np.ndarray:

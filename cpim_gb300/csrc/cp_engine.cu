@@ -217,6 +217,7 @@ struct cp_net {
   int64_t* d_offB = nullptr;
   std::vector<int64_t> offA, offB;  // host copies: word offsets of each constraint's A / B rows
   int64_t relA_words = 0, relB_words = 0;
+  int top = 0;                 // level stack top (cp_level_push / cp_level_pop_to)
   GridScratch G{};
   SacScratch S{};
   KStats* d_stats = nullptr;
@@ -976,6 +977,43 @@ int cp_reduce_to(cp_net* net, int level, int var, int value) {
   CP_TRY(check_var_val(net, var, value));
   CP_CUDA(launch_level_edit(net->dn, net->level_ptr(level), var, value, kOpAssign, net->e->stream));
   ++net->e->launches;
+  CP_CUDA(cudaStreamSynchronize(net->e->stream));
+  return CP_OK;
+}
+
+int cp_level_push(cp_net* net, int src, int* new_level) {
+  if (!net || !new_level) return fail(CP_E_ARG, "null argument");
+  CP_TRY(check_level(net, src));
+  CP_TRY(check_level(net, src + 1));
+  CP_TRY(cp_level_copy(net, src, src + 1));
+  net->top = src + 1;
+  *new_level = src + 1;
+  return CP_OK;
+}
+
+int cp_level_pop_to(cp_net* net, int level) {
+  if (!net) return fail(CP_E_ARG, "null net");
+  CP_TRY(check_level(net, level));
+  net->top = level;
+  return CP_OK;
+}
+
+int cp_level_top(const cp_net* net) { return net ? net->top : CP_E_ARG; }
+
+int cp_dom_set_var(cp_net* net, int level, int var, const uint64_t* words) {
+  if (!net || !words) return fail(CP_E_ARG, "null argument");
+  CP_TRY(check_level(net, level));
+  if (var < 0 || var >= net->n) return fail(CP_E_ARG, "variable out of range");
+  const int W = net->W_user, Wi = net->W, d = net->dom[var];
+  u64 v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int w = 0; w < Wi; ++w) {
+    u64 x = w < W ? words[w] : 0ull;
+    const int lo = w * 64;
+    if (d - lo < 64) x &= (d - lo <= 0) ? 0ull : ((1ull << (d - lo)) - 1ull);
+    v[w] = x;
+  }
+  CP_CUDA(cudaMemcpyAsync(net->level_ptr(level) + static_cast<size_t>(var) * Wi, v, static_cast<size_t>(Wi) * 8,
+                          cudaMemcpyHostToDevice, net->e->stream));
   CP_CUDA(cudaStreamSynchronize(net->e->stream));
   return CP_OK;
 }

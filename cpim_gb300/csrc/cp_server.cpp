@@ -676,6 +676,17 @@ int cp_wait(cp_server* s, int64_t ticket, int64_t timeout_ms, cp_result* res) {
   return CP_OK;
 }
 
+int cp_poll(cp_server* s, int64_t ticket, cp_result* res) {
+  if (!s || !res) return CP_E_ARG;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(ticket);
+    if (it == s->reqs.end()) return CP_E_ARG;
+    if (it->second->status == 0 || it->second->status == 1) return 1;
+  }
+  return cp_wait(s, ticket, 0, res);
+}
+
 int cp_result_domains(cp_server* s, int64_t ticket, uint64_t* out) {
   if (!s || !out) return CP_E_ARG;
   std::lock_guard<std::mutex> lk(s->mu);

@@ -138,6 +138,17 @@ int cp_dom_set(cp_net* net, int level, const uint64_t* in); /* n*W words */
 int cp_dom_sizes(cp_net* net, int level, int* out);         /* n popcounts */
 int cp_reduce_to(cp_net* net, int level, int var, int value);
 int cp_remove(cp_net* net, int level, int var, int value);
+/* Network::NewLevel(src) (src/Network.cpp:438-442): level src + 1 := level
+ * src, which becomes the top; *new_level = src + 1. */
+int cp_level_push(cp_net* net, int src, int* new_level);
+/* Network::BackTo(p) (src/Network.cpp:444-446, IntVar::BackTo :235-239):
+ * level p becomes the top; the data of every level is left as it is. */
+int cp_level_pop_to(cp_net* net, int level);
+/* The top level set by the last cp_level_push / cp_level_pop_to (0 at upload). */
+int cp_level_top(const cp_net* net);
+/* The domain of one variable at a level: W words, bits past its size cleared
+ * (the per-variable form of cp_dom_set). */
+int cp_dom_set_var(cp_net* net, int level, int var, const uint64_t* words);
 
 /* ---- propagation --------------------------------------------------------- */
 /* AC fixpoint at `level` (AC_3bit for binary networks, GAC when tables are
@@ -290,6 +301,9 @@ int cp_submit_instance(cp_server* s, int type, const cp_instance* inst, int64_t*
 int cp_cancel(cp_server* s, int64_t ticket);
 /* Waits up to timeout_ms for a request; CP_E_TIMEOUT if still running. */
 int cp_wait(cp_server* s, int64_t ticket, int64_t timeout_ms, cp_result* res);
+/* cp_wait without waiting: 0 with *res filled once the request is done,
+ * 1 while it is queued or running. */
+int cp_poll(cp_server* s, int64_t ticket, cp_result* res);
 /* n*W words of a done propagate / SAC request (unspecified if inconsistent);
  * CP_E_STATE if there are none. */
 int cp_result_domains(cp_server* s, int64_t ticket, uint64_t* out);

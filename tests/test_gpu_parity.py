@@ -337,3 +337,42 @@ def test_reload_sync_and_async_match_oracle():
             assert np.array_equal(nets[0].dom_get(0), d)
         for n in nets:
             n.close()
+
+
+def test_level_push_pop_and_set_var():
+    # Network::NewLevel / BackTo over the C ABI (cp_level_push / cp_level_pop_to)
+    # and the per-variable domain write (cp_dom_set_var).
+    inst = cp.gen_binary(40, 20, 150, 0.35, 0.35, 0.1, 9)
+    with cp.Engine(0) as eng:
+        net = eng.upload(inst, max_levels=4)
+        assert net.level_top() == 0
+        d0 = net.dom_get(0)
+        assert net.level_push(0) == 1 and net.level_top() == 1
+        assert np.array_equal(net.dom_get(1), d0)
+        net.reduce_to(1, 3, int(np.flatnonzero([(int(d0[3]) >> a) & 1 for a in range(20)])[0]))
+        net.enforce_ac(1)
+        assert np.array_equal(net.dom_get(0), d0)  # the pushed level leaves level 0 alone
+        assert net.level_push(1) == 2 and net.level_push(2) == 3
+        with pytest.raises(cp.CPError):
+            net.level_push(3)  # no level 4
+        net.level_pop_to(1)
+        assert net.level_top() == 1
+        # Per-variable write, bits past the domain size cleared.
+        net.dom_set_var(2, 5, np.array([np.uint64(0xFFFFFFFFFFFFFFFF)], np.uint64))
+        d2 = net.dom_get(2)
+        assert int(d2[5]) == (1 << 20) - 1
+        words = net.dom_get(1)
+        words[5] = np.uint64(0b1011)
+        net.dom_set_var(1, 5, words[5:6])
+        assert np.array_equal(net.dom_get(1), words)
+        ok, d, dels = O.ac3bit(oracle_view_of(cp.Instance(n=inst.n, W=inst.W, dom=inst.dom, init=words,
+                                                          bin_scope=inst.bin_scope, bin_rows=inst.bin_rows,
+                                                          tab_arity=inst.tab_arity, tab_scope=inst.tab_scope,
+                                                          tab_ntup=inst.tab_ntup, tab_tuples=inst.tab_tuples)))
+        st = net.enforce_ac(1)
+        assert bool(st.inconsistent) == (not ok)
+        if ok:
+            assert np.array_equal(net.dom_get(1), d)
+        with pytest.raises(cp.CPError):
+            net.dom_set_var(1, inst.n, words[:1])
+        net.close()

@@ -208,3 +208,28 @@ def test_server_register_over_budget():
     with cp.Server(budget_bytes=1 << 20) as srv:
         with pytest.raises(cp.CPError):
             srv.register(h, slots=4)
+
+
+def test_server_poll_matches_wait():
+    # cp_poll answers 1 (pending) until a request is done, then fills the same
+    # result as cp_wait; an unknown ticket is an argument error.
+    import time
+    reqs = _requests(count=12, seed=5)
+    with cp.Server(budget_bytes=8 * 10**9) as srv, cp.Engine(0) as eng:
+        tickets = [srv.submit(t, h) for t, h in reqs]
+        polled = {}
+        deadline = time.time() + 120
+        while len(polled) < len(tickets) and time.time() < deadline:
+            for tk in tickets:
+                if tk not in polled:
+                    r = srv.poll(tk)
+                    if r is not None:
+                        polled[tk] = (r.status, r.inconsistent, r.num_positive, r.num_negative, r.mac_status)
+            time.sleep(0.001)
+        assert len(polled) == len(tickets)
+        for tk in tickets:
+            r = srv.wait(tk, 1000)
+            assert polled[tk] == (r.status, r.inconsistent, r.num_positive, r.num_negative, r.mac_status)
+        _check(srv, eng, reqs, tickets)
+        with pytest.raises(cp.CPError):
+            srv.poll(10**9)
