@@ -333,13 +333,16 @@ double alg_bytes(const cp_net* net, const Acc& a, int64_t branches) {
 // ---- one AC fixpoint at a level ----------------------------------------
 // evt_dev: device list of seeds (nullptr = all variables); nevt: its length.
 // nevt_dev (optional, grid path only): the event count read on the device.
+// ctl_cleared: the grid fixpoint's control block was already cleared (by
+// k_round_prep) in stream order before this call.
 int run_ac(cp_net* net, int level, const int* evt_dev, int nevt, int& launches, KStats* st = nullptr,
-           const int* nevt_dev = nullptr) {
+           const int* nevt_dev = nullptr, bool ctl_cleared = false) {
   cp_engine* e = net->e;
   if (!st) st = net->d_stats;
   if (net->prefer_grid) {
     cudaStream_t s = e->stream;
-    CP_CUDA(cudaMemsetAsync(net->G.flags, 0, net->G.ctl_words * sizeof(int), s));  // flags .. bitmaps
+    if (!ctl_cleared)
+      CP_CUDA(cudaMemsetAsync(net->G.flags, 0, net->G.ctl_words * sizeof(int), s));  // flags .. bitmaps
     net->G.wait_ns = e->wait_ns;
     CP_CUDA(launch_ac_front(net->dn, net->level_ptr(level), evt_dev, nevt_dev, evt_dev ? nevt : 0, net->G, st,
                             net->front_blocks, s));
@@ -767,17 +770,13 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   CP_TRY(net->alloc(&net->d_sizes, n));
   CP_TRY(net->alloc(&net->d_ok1, total_values));
   {
-    static_assert(4 * sizeof(KStats) <= 512, "four stats slots in the pinned block");
-    const size_t st_bytes = 512;  // two fetched slots, then two reset values
+    static_assert(2 * sizeof(KStats) <= 512, "two stats slots in the pinned block");
+    const size_t st_bytes = 512;  // the two stats slots fetched after each call
     const size_t dom_bytes = (static_cast<size_t>(n) * Wi * 8 + 255) & ~size_t(255);
     net->h_block_bytes = st_bytes + dom_bytes + static_cast<size_t>(n) * sizeof(int);
     CP_TRY(e->pinned_get(net->h_block_bytes, &net->h_block));
     char* hb = static_cast<char*>(net->h_block);
     net->h_stats = reinterpret_cast<KStats*>(hb);
-    KStats z{};
-    z.fail_var = -1;
-    net->h_stats[2] = z;  // constant: the source of every captured stats reset
-    net->h_stats[3] = z;
     net->h_dom = reinterpret_cast<u64*>(hb + st_bytes);
     net->h_sizes = reinterpret_cast<int*>(hb + st_bytes + dom_bytes);
   }
@@ -1077,23 +1076,27 @@ int sac_round_launches(cp_net* net, int level, bool root, int& launches, bool ca
   cudaStream_t s = e->stream;
   // Kernel-time events: external records become event nodes of a captured round.
   const unsigned evf = captured ? cudaEventRecordExternal : cudaEventRecordDefault;
-  CP_CUDA(cudaMemcpyAsync(net->d_stats, net->h_stats + 2, 2 * sizeof(KStats), cudaMemcpyHostToDevice, s));
+  // Stats slots and (grid fixpoint) control block in one kernel.
+  CP_CUDA(launch_round_prep(net->d_stats, net->prefer_grid ? net->G.flags : nullptr,
+                            net->prefer_grid ? net->G.ctl_words : 0, s));
   if (root) {
-    CP_TRY(run_ac(net, level, nullptr, 0, launches, net->d_stats + 1));
+    CP_TRY(run_ac(net, level, nullptr, 0, launches, net->d_stats + 1, nullptr, true));
   } else if (net->prefer_grid) {
-    CP_TRY(run_ac(net, level, net->S.evt, 0, launches, net->d_stats + 1, net->S.nevt));
+    CP_TRY(run_ac(net, level, net->S.evt, 0, launches, net->d_stats + 1, net->S.nevt, true));
   } else {
     CP_CUDA(cudaMemcpyAsync(&net->h_sizes[0], net->S.nevt, sizeof(int), cudaMemcpyDeviceToHost, s));
     CP_CUDA(cudaStreamSynchronize(s));
     CP_TRY(run_ac(net, level, net->S.evt, net->h_sizes[0], launches, net->d_stats + 1));
   }
   const size_t nw = (static_cast<size_t>(net->n) + 31) / 32;
-  CP_CUDA(cudaMemsetAsync(net->S.nwork, 0, 6 * sizeof(int), s));  // nwork .. ndeep
-  CP_CUDA(cudaMemsetAsync(net->S.evt_fb, 0, nw * 4, s));
+  CP_CUDA(launch_round_clear(net->S.nwork, 6, net->S.evt_fb, static_cast<int>(nw), s));  // nwork .. ndeep
   const bool tiled = net->tile_grid > 0 && e->sac_mode == 0;
   SacScratch S = net->S;
   if (!tiled) S.tiles = nullptr;
-  CP_CUDA(launch_build_work(net->dn, net->level_ptr(level), S, s));
+  // The tiled sweep's start domains are copied by the same launch.
+  CP_CUDA(launch_build_work(net->dn, net->level_ptr(level), S, tiled ? S.snap : nullptr, s));
+  launches += 2;
+  e->launches += 2;
   CP_CUDA(cudaEventRecordWithFlags(e->evk0, s, evf));
   // Mode 0: failed branches remove their value from the level at once
   // (later branches of the sweep start without it; the closure is the
@@ -1104,8 +1107,6 @@ int sac_round_launches(cp_net* net, int level, bool root, int& launches, bool ca
     // Two-round branches resolved by the tiled kernel, the rest (the deep
     // list) by the general kernel; the sweep-start domains and the
     // weak-support lists counted against them come first.
-    CP_CUDA(cudaMemcpyAsync(S.snap, net->level_ptr(level), static_cast<size_t>(net->n) * net->W * 8,
-                            cudaMemcpyDeviceToDevice, s));
     if (S.weak) {
       CP_CUDA(launch_weak(net->dn, S.snap, S.weak, s));
       launches += 1;
@@ -1208,6 +1209,9 @@ int cp_enforce_sac1(cp_net* net, int level, cp_stats* st) {
   for (bool root = true;; root = false) {
     ++sweeps;
     CP_TRY(sac_round(net, level, root, launches));
+    // The end of this round on the device; the last record (the round after
+    // which the host stops) closes device_ms without the host's reaction time.
+    CP_CUDA(cudaEventRecord(e->ev1, s));
     CP_TRY(sac_round_wait(net));
     acc.add(net->h_stats[1], 0);  // the level AC before this sweep
     if (net->h_stats[1].inconsistent) {
@@ -1235,7 +1239,6 @@ int cp_enforce_sac1(cp_net* net, int level, cp_stats* st) {
     }
     if (k.removed == 0) break;
   }
-  CP_CUDA(cudaEventRecord(e->ev1, s));
   CP_CUDA(cudaEventSynchronize(e->ev1));
   if (st) {
     acc.s.inconsistent = inconsistent ? 1 : 0;

@@ -276,7 +276,9 @@ size_t sac_tile_smem(const DevNet& N, int slot_cap);
 int sac_tile_blocks_per_sm(const DevNet& N, int slot_cap, int block);
 // Builds the list of live (x, a) pairs of a level (warp ballot + prefix);
 // when S.tiles is set, also one tile per 32-value slice with live values.
-cudaError_t launch_build_work(const DevNet& N, const u64* dom, SacScratch S, cudaStream_t s);
+cudaError_t launch_build_work(const DevNet& N, const u64* dom, SacScratch S, u64* snap, cudaStream_t s);
+cudaError_t launch_round_prep(KStats* st, int* ctl, int ctl_words, cudaStream_t s);
+cudaError_t launch_round_clear(int* ctr, int nctr, u32* fb, int nw, cudaStream_t s);
 // Removes failed pairs from the level, collecting changed variables.
 cudaError_t launch_commit(const DevNet& N, u64* dom, SacScratch S, KStats* st, cudaStream_t s);
 // Builds the B blocks (transposes) of the binary relations.

@@ -1864,10 +1864,14 @@ __global__ void k_ac3_replay(DevNet N, const int* arc_con, const int* bx, const 
 // Live (x, a) pairs of a level, one warp per variable: ballot of the live
 // flags, lane offsets by prefix popcount, one atomic per 32 values.
 template <int WT>
-__global__ void k_build_work(DevNet N, const u64* dom, int2* work, int* nwork, int4* tiles, int* ntiles) {
+__global__ void k_build_work(DevNet N, const u64* dom, int2* work, int* nwork, int4* tiles, int* ntiles, u64* snap) {
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nw = (gridDim.x * blockDim.x) >> 5;
+  if (snap)  // the sweep-start domains, for the tiled sweep
+    for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < static_cast<size_t>(N.n) * WT;
+         i += static_cast<size_t>(gridDim.x) * blockDim.x)
+      snap[i] = dom[i];
   for (int x = gw; x < N.n; x += nw) {
     const int ds = N.dsize[x];
     for (int base = 0; base < ds; base += 32) {
@@ -2972,13 +2976,42 @@ cudaError_t launch_weak(const DevNet& N, const u64* root, u32* weak, cudaStream_
   });
 }
 
-cudaError_t launch_build_work(const DevNet& N, const u64* dom, SacScratch S, cudaStream_t s) {
+cudaError_t launch_build_work(const DevNet& N, const u64* dom, SacScratch S, u64* snap, cudaStream_t s) {
   return dispatch_w(N.W, [&](auto wt) -> cudaError_t {
     constexpr int WT = decltype(wt)::value;
     const int blocks = std::max(1, std::min(4096, (N.n * 32 + 255) / 256));
-    k_build_work<WT><<<blocks, 256, 0, s>>>(N, dom, S.work, S.nwork, S.tiles, S.ntiles);
+    k_build_work<WT><<<blocks, 256, 0, s>>>(N, dom, S.work, S.nwork, S.tiles, S.ntiles, snap);
     return cudaGetLastError();
   });
+}
+
+// Start of a SAC round: the round's two stats slots (fail_var -1, the rest
+// zero) and, for the grid fixpoint, its control block (flags .. bitmaps).
+__global__ void k_round_prep(KStats* st, int* ctl, int ctl_words) {
+  constexpr int kw = static_cast<int>(sizeof(KStats) / sizeof(int));
+  int* p = reinterpret_cast<int*>(st);
+  for (int i = threadIdx.x; i < 2 * kw; i += blockDim.x) p[i] = 0;
+  for (int i = threadIdx.x; i < ctl_words; i += blockDim.x) ctl[i] = 0;
+  __syncthreads();
+  if (threadIdx.x == 0) st[0].fail_var = st[1].fail_var = -1;
+}
+
+// After the round's level AC has read the previous commit's events: the sweep
+// counters (nwork .. ndeep) and the changed-variable bitmap.
+__global__ void k_round_clear(int* ctr, int nctr, u32* fb, int nw) {
+  for (int i = threadIdx.x; i < nctr; i += blockDim.x) ctr[i] = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nw; i += gridDim.x * blockDim.x) fb[i] = 0u;
+}
+
+cudaError_t launch_round_prep(KStats* st, int* ctl, int ctl_words, cudaStream_t s) {
+  k_round_prep<<<1, 256, 0, s>>>(st, ctl, ctl_words);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_round_clear(int* ctr, int nctr, u32* fb, int nw, cudaStream_t s) {
+  const int blocks = std::max(1, std::min(64, (nw + 255) / 256));
+  k_round_clear<<<blocks, 256, 0, s>>>(ctr, nctr, fb, nw);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_commit(const DevNet& N, u64* dom, SacScratch S, KStats* st, cudaStream_t s) {
