@@ -536,7 +536,7 @@ def run_ours(args):
                      "frac": achieved / peak, "traffic": traffic,
                      "frac_without_branch_copy": achieved_nc / peak,
                      "dram_frac": (dram_gbs / peak) if dram_gbs else None,
-                     "kernel": "SAC sweep kernels (k_weak + k_sac_tile + k_sac on the deep list), per sweep",
+                     "kernel": "SAC sweep kernels (k_work_and_weak + k_sac_tile + k_sac on the deep list), per sweep",
                      "kernel_ms_per_launch": kms_launch,
                      "alg_bytes_per_launch": kern_bytes / max(1, launches_k),
                      "branch_copy_bytes_per_launch": copy_bytes / max(1, launches_k),

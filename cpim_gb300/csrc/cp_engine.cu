@@ -1093,11 +1093,14 @@ int sac_round_launches(cp_net* net, int level, bool root, int& launches, bool ca
   const bool tiled = net->tile_grid > 0 && e->sac_mode == 0;
   SacScratch S = net->S;
   if (!tiled) S.tiles = nullptr;
-  // The tiled sweep's start domains are copied by the same launch.
-  CP_CUDA(launch_build_work(net->dn, net->level_ptr(level), S, tiled ? S.snap : nullptr, s));
   launches += 2;
   e->launches += 2;
+  const bool with_weak = tiled && S.weak;
+  if (!with_weak) CP_CUDA(launch_build_work(net->dn, net->level_ptr(level), S, tiled ? S.snap : nullptr, s));
   CP_CUDA(cudaEventRecordWithFlags(e->evk0, s, evf));
+  // With weak-support lists, the work list, the sweep-start snapshot and the
+  // lists are built by one launch (inside the sweep's kernel time).
+  if (with_weak) CP_CUDA(launch_work_and_weak(net->dn, net->level_ptr(level), S, S.snap, S.weak, s));
   // Mode 0: failed branches remove their value from the level at once
   // (later branches of the sweep start without it; the closure is the
   // same, since a wipe-out on a larger domain implies one on a smaller);
@@ -1107,11 +1110,6 @@ int sac_round_launches(cp_net* net, int level, bool root, int& launches, bool ca
     // Two-round branches resolved by the tiled kernel, the rest (the deep
     // list) by the general kernel; the sweep-start domains and the
     // weak-support lists counted against them come first.
-    if (S.weak) {
-      CP_CUDA(launch_weak(net->dn, S.snap, S.weak, s));
-      launches += 1;
-      e->launches += 1;
-    }
     // Without the snapshot the tiled kernel reads the level itself and removes
     // nothing at it (a pure Jacobi sweep: the level does not change).
     SacScratch St = S;
@@ -1134,7 +1132,7 @@ int sac_round_launches(cp_net* net, int level, bool root, int& launches, bool ca
     launches += 1;
     e->launches += 1;
   }
-  launches += 2;
+  launches += 2;  // the work list (with the weak lists where there are any) and the general branch kernel
   e->launches += 2;
   CP_CUDA(cudaMemcpyAsync(net->h_stats, net->d_stats, 2 * sizeof(KStats), cudaMemcpyDeviceToHost, s));
   return CP_OK;

@@ -271,12 +271,13 @@ cudaError_t launch_sac_tile(const DevNet& N, u64* root, SacScratch S, uint8_t* o
                             int block, int grid, cudaStream_t s);
 cudaError_t launch_batch_snap(int W, const BatchDev& B, cudaStream_t s);
 // Weak-support lists of every arc for the domains at root (into S.weak).
-cudaError_t launch_weak(const DevNet& N, const u64* root, u32* weak, cudaStream_t s);
 size_t sac_tile_smem(const DevNet& N, int slot_cap);
 int sac_tile_blocks_per_sm(const DevNet& N, int slot_cap, int block);
 // Builds the list of live (x, a) pairs of a level (warp ballot + prefix);
 // when S.tiles is set, also one tile per 32-value slice with live values.
 cudaError_t launch_build_work(const DevNet& N, const u64* dom, SacScratch S, u64* snap, cudaStream_t s);
+cudaError_t launch_work_and_weak(const DevNet& N, const u64* dom, SacScratch S, u64* snap, u32* weak,
+                                 cudaStream_t s);
 cudaError_t launch_round_prep(KStats* st, int* ctl, int ctl_words, cudaStream_t s);
 cudaError_t launch_round_clear(int* ctr, int nctr, u32* fb, int nw, cudaStream_t s);
 // Removes failed pairs from the level, collecting changed variables.

@@ -1863,14 +1863,18 @@ __global__ void k_ac3_replay(DevNet N, const int* arc_con, const int* bx, const 
 // ---------------------------------------------------------------------------
 // Live (x, a) pairs of a level, one warp per variable: ballot of the live
 // flags, lane offsets by prefix popcount, one atomic per 32 values.
+// The work list of a sweep (block vb of vg blocks of the body): one warp per
+// variable appends its live values; with snap, the sweep-start domains are
+// copied too.
 template <int WT>
-__global__ void k_build_work(DevNet N, const u64* dom, int2* work, int* nwork, int4* tiles, int* ntiles, u64* snap) {
+__device__ __forceinline__ void build_work_body(const DevNet& N, const u64* dom, int2* work, int* nwork, int4* tiles,
+                                                int* ntiles, u64* snap, int vb, int vg) {
   const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nw = (gridDim.x * blockDim.x) >> 5;
+  const int gw = (vb * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (vg * blockDim.x) >> 5;
   if (snap)  // the sweep-start domains, for the tiled sweep
-    for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < static_cast<size_t>(N.n) * WT;
-         i += static_cast<size_t>(gridDim.x) * blockDim.x)
+    for (size_t i = vb * static_cast<size_t>(blockDim.x) + threadIdx.x; i < static_cast<size_t>(N.n) * WT;
+         i += static_cast<size_t>(vg) * blockDim.x)
       snap[i] = dom[i];
   for (int x = gw; x < N.n; x += nw) {
     const int ds = N.dsize[x];
@@ -1887,6 +1891,11 @@ __global__ void k_build_work(DevNet N, const u64* dom, int2* work, int* nwork, i
       if ((bits >> lane) & 1u) work[b0 + __popc(bits & ((1u << lane) - 1u))] = make_int2(x, base + lane);
     }
   }
+}
+
+template <int WT>
+__global__ void k_build_work(DevNet N, const u64* dom, int2* work, int* nwork, int4* tiles, int* ntiles, u64* snap) {
+  build_work_body<WT>(N, dom, work, nwork, tiles, ntiles, snap, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -2302,10 +2311,12 @@ __device__ void weak_lists_of(const DevNet& N, const u64* root, int y, u32* weak
   for (int j = N.arc_start[y]; j < N.arc_start[y + 1]; ++j) weak_list_arc<WT>(N, root, dy, j, weak);
 }
 
+// Weak-support lists of every arc, one warp per arc (block vb of vg blocks of
+// the body).
 template <int WT>
-__global__ void k_weak(DevNet N, const u64* root, u32* weak) {
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nw = (gridDim.x * blockDim.x) >> 5;
+__device__ __forceinline__ void weak_body(const DevNet& N, const u64* root, u32* weak, int vb, int vg) {
+  const int gw = (vb * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (vg * blockDim.x) >> 5;
   const int narcs = N.arc_start[N.n];
   for (int j = gw; j < narcs; j += nw) {
     // Source variable of arc j: the last y with arc_start[y] <= j.
@@ -2318,6 +2329,18 @@ __global__ void k_weak(DevNet N, const u64* root, u32* weak) {
     load_dom_uniform<WT>(root + static_cast<size_t>(lo) * WT, dy);
     weak_list_arc<WT>(N, root, dy, j, weak);
   }
+}
+
+// The sweep's work list and its weak-support lists in one launch: the first
+// work_blocks blocks build the list (and the snapshot), the others the lists.
+// Both read the level's domains, which nothing changes before the sweep.
+template <int WT>
+__global__ void k_work_and_weak(DevNet N, const u64* dom, int2* work, int* nwork, int4* tiles, int* ntiles, u64* snap,
+                                u32* weak, int work_blocks) {
+  if (static_cast<int>(blockIdx.x) < work_blocks)
+    build_work_body<WT>(N, dom, work, nwork, tiles, ntiles, snap, blockIdx.x, work_blocks);
+  else
+    weak_body<WT>(N, dom, weak, blockIdx.x - work_blocks, gridDim.x - work_blocks);
 }
 
 __device__ __forceinline__ void flush_tile_counts(KStats* st, u64 c_rev, u64 c_rows, u64 c_done) {
@@ -2967,11 +2990,13 @@ cudaError_t launch_sac_tile(const DevNet& N, u64* root, SacScratch S, uint8_t* o
   });
 }
 
-cudaError_t launch_weak(const DevNet& N, const u64* root, u32* weak, cudaStream_t s) {
+cudaError_t launch_work_and_weak(const DevNet& N, const u64* dom, SacScratch S, u64* snap, u32* weak,
+                                 cudaStream_t s) {
   return dispatch_w(N.W, [&](auto wt) -> cudaError_t {
     constexpr int WT = decltype(wt)::value;
-    const int blocks = std::max(1, std::min(8192, (2 * N.nb * 32 + 255) / 256));
-    k_weak<WT><<<blocks, 256, 0, s>>>(N, root, weak);
+    const int wb = std::max(1, std::min(4096, (N.n * 32 + 255) / 256));
+    const int kb = std::max(1, std::min(8192, (2 * N.nb * 32 + 255) / 256));
+    k_work_and_weak<WT><<<wb + kb, 256, 0, s>>>(N, dom, S.work, S.nwork, S.tiles, S.ntiles, snap, weak, wb);
     return cudaGetLastError();
   });
 }
