@@ -240,8 +240,9 @@ struct cp_net {
   int64_t device_bytes = 0;
   int max_deg = 0;     // largest number of binary arcs at one variable
 
-  void* h_block = nullptr;  // pinned block holding h_stats, h_dom, h_sizes
+  void* h_block = nullptr;  // host-mapped pinned block holding h_stats, h_dom, h_sizes
   size_t h_block_bytes = 0;
+  KStats* dh_stats = nullptr;  // device address of h_stats (written by k_stats_out)
   // SAC1 rounds captured as CUDA graphs: [0] root AC + sweep, [1] events AC +
   // sweep; valid for the level and knobs in sac_key.
   cudaGraphExec_t sac_exec[2] = {nullptr, nullptr};
@@ -260,7 +261,7 @@ struct cp_net {
     drop_sac_graphs();
     if (e) {
       for (void* p : allocs) e->dev_free(p);
-      e->pinned_put(h_block, h_block_bytes);
+      e->mapped_put(h_block, h_block_bytes);
       --e->live_nets;
     }
   }
@@ -774,9 +775,14 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
     const size_t st_bytes = 512;  // the two stats slots fetched after each call
     const size_t dom_bytes = (static_cast<size_t>(n) * Wi * 8 + 255) & ~size_t(255);
     net->h_block_bytes = st_bytes + dom_bytes + static_cast<size_t>(n) * sizeof(int);
-    CP_TRY(e->pinned_get(net->h_block_bytes, &net->h_block));
+    CP_TRY(e->mapped_get(net->h_block_bytes, &net->h_block));
     char* hb = static_cast<char*>(net->h_block);
     net->h_stats = reinterpret_cast<KStats*>(hb);
+    {
+      void* dh = nullptr;
+      CP_CUDA(cudaHostGetDevicePointer(&dh, net->h_block, 0));
+      net->dh_stats = static_cast<KStats*>(dh);
+    }
     net->h_dom = reinterpret_cast<u64*>(hb + st_bytes);
     net->h_sizes = reinterpret_cast<int*>(hb + st_bytes + dom_bytes);
   }
@@ -1134,7 +1140,11 @@ int sac_round_launches(cp_net* net, int level, bool root, int& launches, bool ca
   }
   launches += 2;  // the work list (with the weak lists where there are any) and the general branch kernel
   e->launches += 2;
-  CP_CUDA(cudaMemcpyAsync(net->h_stats, net->d_stats, 2 * sizeof(KStats), cudaMemcpyDeviceToHost, s));
+  // The round's stats straight into host-mapped memory (a kernel, not a copy
+  // node that would queue behind other engines' transfers).
+  CP_CUDA(launch_stats_out(net->d_stats, net->dh_stats, 2, s));
+  ++launches;
+  ++e->launches;
   return CP_OK;
 }
 

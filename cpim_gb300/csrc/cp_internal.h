@@ -279,6 +279,7 @@ cudaError_t launch_build_work(const DevNet& N, const u64* dom, SacScratch S, u64
 cudaError_t launch_work_and_weak(const DevNet& N, const u64* dom, SacScratch S, u64* snap, u32* weak,
                                  cudaStream_t s);
 cudaError_t launch_round_prep(KStats* st, int* ctl, int ctl_words, cudaStream_t s);
+cudaError_t launch_stats_out(const KStats* src, KStats* dst, int k, cudaStream_t s);
 cudaError_t launch_round_clear(int* ctr, int nctr, u32* fb, int nw, cudaStream_t s);
 // Removes failed pairs from the level, collecting changed variables.
 cudaError_t launch_commit(const DevNet& N, u64* dom, SacScratch S, KStats* st, cudaStream_t s);

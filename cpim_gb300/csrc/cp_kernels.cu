@@ -3028,6 +3028,21 @@ __global__ void k_round_clear(int* ctr, int nctr, u32* fb, int nw) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nw; i += gridDim.x * blockDim.x) fb[i] = 0u;
 }
 
+// Copies k stats slots to host-mapped memory, visible to the host once the
+// stream has been synchronised.
+__global__ void k_stats_out(const KStats* src, KStats* dst, int k) {
+  constexpr int kw = static_cast<int>(sizeof(KStats) / sizeof(int));
+  const int* a = reinterpret_cast<const int*>(src);
+  int* b = reinterpret_cast<int*>(dst);
+  for (int i = threadIdx.x; i < k * kw; i += blockDim.x) b[i] = a[i];
+  __threadfence_system();
+}
+
+cudaError_t launch_stats_out(const KStats* src, KStats* dst, int k, cudaStream_t s) {
+  k_stats_out<<<1, 64, 0, s>>>(src, dst, k);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_round_prep(KStats* st, int* ctl, int ctl_words, cudaStream_t s) {
   k_round_prep<<<1, 256, 0, s>>>(st, ctl, ctl_words);
   return cudaGetLastError();
