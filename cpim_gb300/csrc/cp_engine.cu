@@ -597,6 +597,7 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   }
   // Tables.
   std::vector<int> t_arity(n_tab), t_soff(n_tab), t_scope, t_ntup(n_tab);
+  std::vector<int> t_scope4(static_cast<size_t>(n_tab) * kMaxArity, 0);
   std::vector<int64_t> t_off(n_tab);
   int64_t total_tup = 0;
   {
@@ -614,6 +615,7 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
         if (seen[v] == t) return fail(CP_E_ARG, "repeated variable in table");
         seen[v] = t;
         t_scope.push_back(v);
+        if (i < kMaxArity) t_scope4[static_cast<size_t>(t) * kMaxArity + i] = v;
         ++tab_deg[v];
       }
       so += r;
@@ -685,7 +687,7 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   Arc* d_arcs;
   int* d_tinc;
   int* d_vtab;
-  int *d_tar, *d_tsc, *d_tso, *d_tnt;
+  int *d_tar, *d_tsc, *d_tso, *d_ts4, *d_tnt;
   int64_t* d_toff;
   uint16_t* d_ttup;
   // Metadata arrays: one device block, filled by one copy from pinned staging.
@@ -698,6 +700,7 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   mp.add(&d_tar, t_arity.data(), n_tab);
   mp.add(&d_tsc, t_scope.data(), t_scope.size());
   mp.add(&d_tso, t_soff.data(), n_tab);
+  mp.add(&d_ts4, t_scope4.data(), t_scope4.size());
   mp.add(&d_tnt, t_ntup.data(), n_tab);
   mp.add(&d_toff, t_off.data(), n_tab);
   mp.add(&d_ttup, t_tup.data(), t_tup.size());
@@ -729,6 +732,7 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   D.t_arity = d_tar;
   D.t_scope = d_tsc;
   D.t_soff = d_tso;
+  D.t_scope4 = d_ts4;
   D.t_ntup = d_tnt;
   D.t_off = d_toff;
   D.t_tup = d_ttup;

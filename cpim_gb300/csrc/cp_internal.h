@@ -64,6 +64,7 @@ struct DevNet {
   const int* t_arity = nullptr;
   const int* t_scope = nullptr;     // scopes of all tables, concatenated
   const int* t_soff = nullptr;      // [nt] start of table t's scope in t_scope
+  const int* t_scope4 = nullptr;    // [nt * kMaxArity] the first kMaxArity scope positions at a fixed stride
   const int* t_ntup = nullptr;
   const int64_t* t_off = nullptr;   // offset of table t's tuples in t_tup
   const uint16_t* t_tup = nullptr;

@@ -414,7 +414,7 @@ __device__ __forceinline__ int table_removals(const DevNet& N, const u64* D, int
   int empty_var = -1;
 #pragma unroll
   for (int i = 0; i < kMaxArity; ++i) {
-    s[i] = i < r ? N.t_scope[N.t_soff[t] + i] : 0;
+    s[i] = i < r ? N.t_scope4[t * kMaxArity + i] : 0;
     u64 any = 0;
     if (i < r) {
       load_dom_uniform<WT>(D + static_cast<size_t>(s[i]) * WT, snap[i]);
@@ -1571,9 +1571,13 @@ __device__ __forceinline__ void front_table(const DevNet& N, const Fix& F, int t
                                             int* fn, int slot, Cnt& cn) {
   const int lane = threadIdx.x & 31;
   const int ar = N.t_arity[t];
-  const int* sc = N.t_scope + N.t_soff[t];
   bool act = false;
-  for (int p = lane; p < ar && !act; p += 32) act = all || front_bit(bc, sc[p]);
+  if (ar <= kMaxArity) {
+    act = lane < ar && (all || front_bit(bc, N.t_scope4[t * kMaxArity + lane]));
+  } else {
+    const int* sc = N.t_scope + N.t_soff[t];
+    for (int p = lane; p < ar && !act; p += 32) act = all || front_bit(bc, sc[p]);
+  }
   if (!__any_sync(kFull, act) || any_failed(F)) return;
   if constexpr (WT <= 4) {
     if (ar <= kMaxArity) {
