@@ -572,8 +572,11 @@ __device__ __forceinline__ void revise_table(const DevNet& N, const Fix& F, u32*
   if (empty_var >= 0 && lane == 0) set_failed(F, slot, empty_var);
 }
 
-// Work item c (chunk of incidences) of variable y.
-template <int WT, bool kTab>
+// Work item c (chunk of incidences) of variable y. kGroup: items with several
+// arcs left are revised by lane groups (revise_arcs_grouped) -- for the
+// latency-bound single-CTA fixpoints of searches; the throughput-bound SAC
+// branch and batch kernels keep one arc per warp, and their registers.
+template <int WT, bool kTab, bool kGroup = true>
 __device__ __forceinline__ void process_item(const DevNet& N, const Fix& F, int y, int c, u32* fbc, u32* qn, u32* fbn,
                                              int* qlenn, int slot, int stamp, Cnt& cn) {
   const int lane = threadIdx.x & 31;
@@ -587,7 +590,7 @@ __device__ __forceinline__ void process_item(const DevNet& N, const Fix& F, int 
       if (any_failed(F)) return;
       const int left = min(hi, da) - i;
       bool grouped = false;
-      if constexpr (arc_group_lanes(WT) < 32) {
+      if constexpr (kGroup && arc_group_lanes(WT) < 32) {
         if (left >= 2) {
           // Several arcs left in the item: one lane group per arc.
           const int na = min(32 / arc_group_lanes(WT), left);
@@ -682,7 +685,7 @@ __device__ __forceinline__ int cta_round_items(const DevNet& N, const u32* q, in
 
 // CTA-local fixpoint; the caller has seeded queue 0 and synchronised.
 // Returns the number of rounds; sets *err on a round-count overrun.
-template <int WT, bool kTab>
+template <int WT, bool kTab, bool kGroup = true>
 __device__ int cta_fixpoint(const DevNet& N, const Fix& F, Cnt& cn, int* err) {
   const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const long long max_rounds = N.total_values + 2;
@@ -708,7 +711,7 @@ __device__ int cta_fixpoint(const DevNet& N, const Fix& F, Cnt& cn, int* err) {
     int i = 0;
     for (int j = warp; j < items; j += nwarps) {
       while (F.pre[i + 1] <= j) ++i;
-      process_item<WT, kTab>(N, F, static_cast<int>(qc[i]), j - F.pre[i], fbc, qn, fbn, qlenn, cur ^ 1,
+      process_item<WT, kTab, kGroup>(N, F, static_cast<int>(qc[i]), j - F.pre[i], fbc, qn, fbn, qlenn, cur ^ 1,
                              F.stamp_base + r + 1, cn);
     }
     __syncthreads();
@@ -1317,7 +1320,7 @@ __global__ void __launch_bounds__(256) k_sac(DevNet N, const u64* root, const in
       append_var(F.q0, F.fb0, F.qlen, xa.x);
     }
     __syncthreads();
-    const int rounds = cta_fixpoint<WT, kTab>(N, F, cn, &s_err);
+    const int rounds = cta_fixpoint<WT, kTab, false>(N, F, cn, &s_err);
     rounds_max = max(rounds_max, rounds);
     if (threadIdx.x == 0) {
       const bool failed = (s_failed[0] | s_failed[1]) != 0;
@@ -2542,7 +2545,7 @@ __global__ void __launch_bounds__(512) k_batch_node(BatchDev B, int op, KStats* 
       for (int j = threadIdx.x; j < ne; j += blockDim.x) seed_var<WT>(N, F, ev[j]);
     }
     __syncthreads();
-    const int rounds = cta_fixpoint<WT, kTab>(N, F, cn, &s_err);
+    const int rounds = cta_fixpoint<WT, kTab, false>(N, F, cn, &s_err);
     rounds_max = max(rounds_max, rounds);
     block_copy(dom, F.D, words);
     if (threadIdx.x == 0 && (s_failed[0] | s_failed[1])) B.inc[inst] = 1;
@@ -2679,7 +2682,7 @@ __global__ void __launch_bounds__(256) k_batch_sac(BatchDev B, int deep_only, KS
       append_var(F.q0, F.fb0, F.qlen, x);
     }
     __syncthreads();
-    const int rounds = cta_fixpoint<WT, kTab>(N, F, cn, &s_err);
+    const int rounds = cta_fixpoint<WT, kTab, false>(N, F, cn, &s_err);
     rounds_max = max(rounds_max, rounds);
     if (threadIdx.x == 0) {
       const bool failed = (s_failed[0] | s_failed[1]) != 0;
