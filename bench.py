@@ -437,8 +437,9 @@ def run_ours(args):
         return st, r
 
     # Pipelined: two engines, one copy of the network each; while one engine
-    # runs closure i, closure i+1's relations and domains go to the other
-    # (cp_net_reload_async, on that engine's lowest-priority transfer stream).
+    # runs closure i (cp_enforce_sac1_begin / _end), closure i+1's relations
+    # and domains go to the other (cp_net_reload_async, on that engine's
+    # lowest-priority transfer stream).
     # Every closure still uploads its inputs from pinned host memory and
     # reads its domains back.
     eng_b = cp.Engine(local)
@@ -451,9 +452,10 @@ def run_ours(args):
         br, r = 0, None
         for i in range(count):
             cur = pair[i % 2]
+            cur.enforce_sac1_begin(0)  # queued behind its own reload
             if i + 1 < count:
                 pair[(i + 1) % 2].reload_async(e2e_inst)
-            st = cur.enforce_sac1(0)
+            st = cur.enforce_sac1_end()
             r = cur.dom_get(0)
             assert np.array_equal(r, final)
             br += st.branches

@@ -108,6 +108,8 @@ def lib():
         "cp_remove": ([vp, i, i, i], i),
         "cp_enforce_ac": ([vp, i, i, PI, C.POINTER(Stats)], i),
         "cp_enforce_sac1": ([vp, i, C.POINTER(Stats)], i),
+        "cp_enforce_sac1_begin": ([vp, i], i),
+        "cp_enforce_sac1_end": ([vp, C.POINTER(Stats)], i),
         "cp_singletons": ([vp, i, i, PI, PI, PU8, i, C.POINTER(Stats)], i),
         "cp_sac_sweep": ([vp, i, P64, C.POINTER(C.c_int64), C.POINTER(Stats)], i),
         "cp_sac_tiles": ([vp, i, i, PI, PI, PI, i, P64, C.POINTER(C.c_double)], i),
@@ -402,6 +404,16 @@ class Net:
     def enforce_sac1(self, level=0) -> Stats:
         st = Stats()
         _check(lib().cp_enforce_sac1(self._h, level, C.byref(st)))
+        return st
+
+    def enforce_sac1_begin(self, level=0):
+        """First half of enforce_sac1: queues the first round and returns."""
+        _check(lib().cp_enforce_sac1_begin(self._h, level))
+
+    def enforce_sac1_end(self) -> Stats:
+        """Second half: waits, runs the further sweeps, returns the stats."""
+        st = Stats()
+        _check(lib().cp_enforce_sac1_end(self._h, C.byref(st)))
         return st
 
     def singletons(self, vars_, vals, level=0, mode=0):

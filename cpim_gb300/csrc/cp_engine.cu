@@ -243,6 +243,8 @@ struct cp_net {
   void* h_block = nullptr;  // host-mapped pinned block holding h_stats, h_dom, h_sizes
   size_t h_block_bytes = 0;
   KStats* dh_stats = nullptr;  // device address of h_stats (written by k_stats_out)
+  int sac_pending_level = -1;  // level of a SAC1 call begun and not yet ended
+  int sac_pending_launches = 0;
   // SAC1 rounds captured as CUDA graphs: [0] root AC + sweep, [1] events AC +
   // sweep; valid for the level and knobs in sac_key.
   cudaGraphExec_t sac_exec[2] = {nullptr, nullptr};
@@ -1207,23 +1209,37 @@ int sac_round_wait(cp_net* net) {
 
 extern "C" {
 
-int cp_enforce_sac1(cp_net* net, int level, cp_stats* st) {
+// SAC1 in two halves: begin queues the first round (level AC + sweep) and
+// returns; end waits for it and runs the further sweeps the host decides on.
+static int sac1_begin(cp_net* net, int level) {
   if (!net) return fail(CP_E_ARG, "null net");
   CP_TRY(check_level(net, level));
+  if (net->sac_pending_level >= 0) return fail(CP_E_STATE, "a SAC1 call on this network is still open");
+  cp_engine* e = net->e;
+  cudaStream_t s = e->stream;
+  net->sac_pending_launches = 0;
+  CP_CUDA(cudaEventRecord(e->ev0, s));
+  CP_TRY(sac_round(net, level, true, net->sac_pending_launches));
+  // The end of this round on the device; the last record (the round after
+  // which the host stops) closes device_ms without the host's reaction time.
+  CP_CUDA(cudaEventRecord(e->ev1, s));
+  net->sac_pending_level = level;
+  return CP_OK;
+}
+
+static int sac1_end(cp_net* net, cp_stats* st) {
+  if (!net) return fail(CP_E_ARG, "null net");
+  if (net->sac_pending_level < 0) return fail(CP_E_STATE, "no SAC1 call open on this network");
+  const int level = net->sac_pending_level;
+  net->sac_pending_level = -1;
   cp_engine* e = net->e;
   cudaStream_t s = e->stream;
   Acc acc;
-  int launches = 0;
-  CP_CUDA(cudaEventRecord(e->ev0, s));
+  int launches = net->sac_pending_launches;
   bool inconsistent = false;
-  int sweeps = 0;
+  int sweeps = 1;
   double kernel_ms = 0, kernel_bytes = 0;
-  for (bool root = true;; root = false) {
-    ++sweeps;
-    CP_TRY(sac_round(net, level, root, launches));
-    // The end of this round on the device; the last record (the round after
-    // which the host stops) closes device_ms without the host's reaction time.
-    CP_CUDA(cudaEventRecord(e->ev1, s));
+  for (;;) {
     CP_TRY(sac_round_wait(net));
     acc.add(net->h_stats[1], 0);  // the level AC before this sweep
     if (net->h_stats[1].inconsistent) {
@@ -1250,6 +1266,9 @@ int cp_enforce_sac1(cp_net* net, int level, cp_stats* st) {
       kernel_bytes += alg_bytes(net, ka, static_cast<int64_t>(k.branches));
     }
     if (k.removed == 0) break;
+    ++sweeps;
+    CP_TRY(sac_round(net, level, false, launches));
+    CP_CUDA(cudaEventRecord(e->ev1, s));
   }
   CP_CUDA(cudaEventSynchronize(e->ev1));
   if (st) {
@@ -1265,6 +1284,15 @@ int cp_enforce_sac1(cp_net* net, int level, cp_stats* st) {
   }
   return CP_OK;
 }
+
+int cp_enforce_sac1(cp_net* net, int level, cp_stats* st) {
+  CP_TRY(sac1_begin(net, level));
+  return sac1_end(net, st);
+}
+
+int cp_enforce_sac1_begin(cp_net* net, int level) { return sac1_begin(net, level); }
+
+int cp_enforce_sac1_end(cp_net* net, cp_stats* st) { return sac1_end(net, st); }
 
 int cp_sac_sweep(cp_net* net, int level, uint64_t* verdict, int64_t* deep, cp_stats* st) {
   if (!net || !verdict) return fail(CP_E_ARG, "null argument");

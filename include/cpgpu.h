@@ -166,6 +166,13 @@ int cp_enforce_ac(cp_net* net, int level, int n_evt, const int* evt, cp_stats* s
  * closure is the same (unique), while the number of tests run depends on
  * scheduling. */
 int cp_enforce_sac1(cp_net* net, int level, cp_stats* st);
+/* cp_enforce_sac1 in two halves: _begin queues the first round (level AC and
+ * sweep) and returns; _end waits for it, runs the further sweeps and fills
+ * st. Between the two the host is free (e.g. to queue another network's
+ * upload), but the engine takes no other call. No counterpart in the
+ * reference. */
+int cp_enforce_sac1_begin(cp_net* net, int level);
+int cp_enforce_sac1_end(cp_net* net, cp_stats* st);
 /* Singleton tests of `count` pairs (vars[i], vals[i]) against the domains of
  * `level` without changing them: ok[i] = 1 if the AC fixpoint of the level
  * with vars[i] reduced to vals[i] is consistent. mode 0 = batched persistent

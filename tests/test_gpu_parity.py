@@ -376,3 +376,29 @@ def test_level_push_pop_and_set_var():
         with pytest.raises(cp.CPError):
             net.dom_set_var(1, inst.n, words[:1])
         net.close()
+
+
+def test_sac1_begin_end_equals_enforce():
+    # cp_enforce_sac1_begin / _end give the closure and stats of
+    # cp_enforce_sac1 (including closures of several sweeps and wipe-outs),
+    # and refuse a second begin or an end without a begin.
+    cases = [(60, 16, 300, 0.35, 0.35, 0.1, 3), (30, 8, 120, 0.45, 0.45, 0.1, 3), (40, 100, 160, 0.8, 0.8, 0.2, 3)]
+    with cp.Engine(0) as eng:
+        for args in cases:
+            inst = cp.gen_binary(*args)
+            ok, d, dels = O.sac1(oracle_view_of(inst))
+            net = eng.upload(inst, max_levels=2)
+            net.enforce_sac1_begin(0)
+            with pytest.raises(cp.CPError):
+                net.enforce_sac1_begin(0)
+            st = net.enforce_sac1_end()
+            assert bool(st.inconsistent) == (not ok)
+            if ok:
+                assert st.deletions == dels
+                assert np.array_equal(net.dom_get(0), d)
+            with pytest.raises(cp.CPError):
+                net.enforce_sac1_end()
+            net.dom_set(0, inst.init)
+            st2 = net.enforce_sac1(0)
+            assert (st2.inconsistent, st2.deletions, st2.sweeps) == (st.inconsistent, st.deletions, st.sweeps)
+            net.close()
