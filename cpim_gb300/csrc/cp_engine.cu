@@ -762,7 +762,8 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
   CP_TRY(net->alloc(&S.deep, total_values));
   // The sweep counters sit together so that one memset clears them.
   int* ctr = nullptr;
-  CP_TRY(net->alloc(&ctr, 8));
+  CP_TRY(net->alloc(&ctr, 8));  // [7]: k_commit's completion counter, zero between launches
+  CP_CUDA(cudaMemsetAsync(ctr, 0, 8 * sizeof(int), e->stream));
   S.nwork = ctr;
   S.cursor = ctr + 1;
   S.nevt = ctr + 2;
@@ -1139,18 +1140,16 @@ int sac_round_launches(cp_net* net, int level, bool root, int& launches, bool ca
                                 nullptr, gs_root));
   }
   CP_CUDA(cudaEventRecordWithFlags(e->evk1, s, evf));
+  // The round's stats go straight into host-mapped memory (from the commit
+  // kernel's last block, or a one-block kernel), not by a copy node that
+  // would queue behind other engines' transfers.
   if (!sweep_only) {
-    CP_CUDA(launch_commit(net->dn, net->level_ptr(level), S, net->d_stats, s));
-    launches += 1;
-    e->launches += 1;
+    CP_CUDA(launch_commit(net->dn, net->level_ptr(level), S, net->d_stats, net->dh_stats, 2, s));
+  } else {
+    CP_CUDA(launch_stats_out(net->d_stats, net->dh_stats, 2, s));
   }
-  launches += 2;  // the work list (with the weak lists where there are any) and the general branch kernel
-  e->launches += 2;
-  // The round's stats straight into host-mapped memory (a kernel, not a copy
-  // node that would queue behind other engines' transfers).
-  CP_CUDA(launch_stats_out(net->d_stats, net->dh_stats, 2, s));
-  ++launches;
-  ++e->launches;
+  launches += 3;  // the work list (with the weak lists where there are any), the general branch kernel,
+  e->launches += 3;  // and the commit or stats kernel
   return CP_OK;
 }
 

@@ -283,7 +283,10 @@ cudaError_t launch_round_prep(KStats* st, int* ctl, int ctl_words, cudaStream_t 
 cudaError_t launch_stats_out(const KStats* src, KStats* dst, int k, cudaStream_t s);
 cudaError_t launch_round_clear(int* ctr, int nctr, u32* fb, int nw, cudaStream_t s);
 // Removes failed pairs from the level, collecting changed variables.
-cudaError_t launch_commit(const DevNet& N, u64* dom, SacScratch S, KStats* st, cudaStream_t s);
+// out (host-mapped, may be null): the last block copies nst stats slots there;
+// S.nwork + 7 is its completion counter (zero between launches).
+cudaError_t launch_commit(const DevNet& N, u64* dom, SacScratch S, KStats* st, KStats* out, int nst,
+                          cudaStream_t s);
 // Builds the B blocks (transposes) of the binary relations.
 cudaError_t launch_transpose(const DevNet& N, u64* rel, const int* bx, const int* by, const int64_t* offA,
                              const int64_t* offB, cudaStream_t s);

@@ -1295,6 +1295,7 @@ __global__ void __launch_bounds__(256) k_sac(DevNet N, const u64* root, const in
   const CtaLayout L = cta_layout(N);
   const size_t words = static_cast<size_t>(N.n) * WT;
   const int total = *nwork;
+  if (total == 0) return;  // an empty list (e.g. no deep branches): nothing to count either
   if (threadIdx.x == 0) s_err = 0;
   Cnt cn;
   int rounds_max = 0;
@@ -2395,8 +2396,10 @@ __global__ void __launch_bounds__(256, WT <= 2 ? 5 : 1) k_sac_tile(DevNet N, u64
   flush_tile_counts(st, c_rev, c_rows, c_done);
 }
 
+// With out: the last block to finish (counted on done, which it resets)
+// copies the round's nst stats slots into host-mapped memory.
 __global__ void k_commit(int W, const int2* work, const int* nwork, const uint8_t* ok, u64* dom, int* evt, int* nevt,
-                         u32* evt_fb, KStats* st) {
+                         u32* evt_fb, KStats* st, unsigned* done, KStats* out, int nst) {
   const int total = *nwork;
   u64 removed = 0;
   for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < total; b += gridDim.x * blockDim.x) {
@@ -2411,6 +2414,19 @@ __global__ void k_commit(int W, const int2* work, const int* nwork, const uint8_
     atomicAdd(&st->removed, removed);
     atomicAdd(&st->deletions, removed);
   }
+  if (!out) return;
+  __shared__ bool s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last) return;
+  constexpr int kw = static_cast<int>(sizeof(KStats) / sizeof(int));
+  const int* a = reinterpret_cast<const int*>(st);
+  int* b = reinterpret_cast<int*>(out);
+  for (int i = threadIdx.x; i < nst * kw; i += blockDim.x) b[i] = __ldcg(a + i);
+  __threadfence_system();
+  if (threadIdx.x == 0) *done = 0u;
 }
 
 // 32x32 bit-matrix transpose across a warp: lane r holds row r (bit c =
@@ -2646,6 +2662,7 @@ __global__ void __launch_bounds__(256) k_batch_sac(BatchDev B, int deep_only, KS
   __shared__ DevNet sN;
   char* base = gscratch ? gscratch + blockIdx.x * gstride : reinterpret_cast<char*>(smem_raw);
   const int total = deep_only ? *B.ndeep : *B.nwork;
+  if (total == 0) return;  // an empty list: nothing to count either
   if (threadIdx.x == 0) s_err = 0;
   Cnt cn;
   int rounds_max = 0;
@@ -3061,9 +3078,11 @@ cudaError_t launch_round_clear(int* ctr, int nctr, u32* fb, int nw, cudaStream_t
   return cudaGetLastError();
 }
 
-cudaError_t launch_commit(const DevNet& N, u64* dom, SacScratch S, KStats* st, cudaStream_t s) {
+cudaError_t launch_commit(const DevNet& N, u64* dom, SacScratch S, KStats* st, KStats* out, int nst,
+                          cudaStream_t s) {
   const int blocks = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(4096, (N.total_values + 255) / 256)));
-  k_commit<<<blocks, 256, 0, s>>>(N.W, S.work, S.nwork, S.ok, dom, S.evt, S.nevt, S.evt_fb, st);
+  k_commit<<<blocks, 256, 0, s>>>(N.W, S.work, S.nwork, S.ok, dom, S.evt, S.nevt, S.evt_fb, st,
+                                  reinterpret_cast<unsigned*>(S.nwork + 7), out, nst);
   return cudaGetLastError();
 }
 
