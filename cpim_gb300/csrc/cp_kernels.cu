@@ -97,6 +97,12 @@ __device__ __forceinline__ void load_row(const u64* rel, size_t off, u64 (&r)[WT
   }
 }
 
+// Programmatic dependent launch: a kernel started by launch_pdl may be
+// scheduled while the previous kernel of its stream is still finishing; it
+// waits here, before its first memory access, for that kernel to complete
+// and its writes to be visible. Without the launch attribute this is a no-op.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 __device__ __forceinline__ long long globaltimer_ns() {
   long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -1288,6 +1294,7 @@ template <int WT, bool kTab>
 __global__ void __launch_bounds__(256) k_sac(DevNet N, const u64* root, const int2* work, const int* nwork,
                                              int* cursor, uint8_t* ok, KStats* st, char* gscratch, size_t gstride,
                                              const int* idx, u64* gs_root) {
+  pdl_wait();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_qlen[3], s_failed[2], s_failvar, s_err, s_b;
   char* base = gscratch ? gscratch + blockIdx.x * gstride : reinterpret_cast<char*>(smem_raw);
@@ -1641,6 +1648,7 @@ __device__ __forceinline__ Fix make_front_fix(u64* D, const GridScratch& G, KSta
 template <int WT, bool kTab>
 __global__ void __launch_bounds__(kFrontBlock, WT <= 2 ? 2 : 1) k_front_first(DevNet N, u64* D, GridScratch G,
                                                                               KStats* st) {
+  pdl_wait();
   const Fix F = make_front_fix(D, G, st);
   const int nw = (N.n + 31) >> 5;
   const int lane = threadIdx.x & 31;
@@ -2345,6 +2353,7 @@ __device__ __forceinline__ void weak_body(const DevNet& N, const u64* root, u32*
 template <int WT>
 __global__ void k_work_and_weak(DevNet N, const u64* dom, int2* work, int* nwork, int4* tiles, int* ntiles, u64* snap,
                                 u32* weak, int work_blocks) {
+  pdl_wait();
   if (static_cast<int>(blockIdx.x) < work_blocks)
     build_work_body<WT>(N, dom, work, nwork, tiles, ntiles, snap, blockIdx.x, work_blocks);
   else
@@ -2368,6 +2377,7 @@ __global__ void __launch_bounds__(256, WT <= 2 ? 5 : 1) k_sac_tile(DevNet N, u64
                                                                    const int4* tiles, const int* ntiles, int* tcursor,
                                                                    uint8_t* ok, int* deep, int* ndeep, int slot_cap,
                                                                    KStats* st, const u32* weak) {
+  pdl_wait();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   u64* T = reinterpret_cast<u64*>(smem_raw);  // [slot_cap][32][WT]
   int4* nbr = reinterpret_cast<int4*>(smem_raw + static_cast<size_t>(slot_cap) * 32 * WT * 8);  // [slot_cap]
@@ -2400,6 +2410,7 @@ __global__ void __launch_bounds__(256, WT <= 2 ? 5 : 1) k_sac_tile(DevNet N, u64
 // copies the round's nst stats slots into host-mapped memory.
 __global__ void k_commit(int W, const int2* work, const int* nwork, const uint8_t* ok, u64* dom, int* evt, int* nevt,
                          u32* evt_fb, KStats* st, unsigned* done, KStats* out, int nst) {
+  pdl_wait();
   const int total = *nwork;
   u64 removed = 0;
   for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < total; b += gridDim.x * blockDim.x) {
@@ -2847,6 +2858,24 @@ cudaError_t dispatch_wt(const DevNet& N, F&& f) {
   return dispatch_w(N.W, [&](auto wt) { return f(wt, std::false_type{}); });
 }
 
+// Launches a kernel with programmatic stream serialisation (the kernel starts
+// with pdl_wait()), so that its launch overlaps the end of the previous
+// kernel on the stream, in direct launches and in captured graphs alike.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 template <typename K>
 cudaError_t allow_smem(K kernel, size_t bytes) {
   if (bytes <= 48 * 1024) return cudaSuccess;
@@ -2943,8 +2972,7 @@ cudaError_t launch_ac_front(const DevNet& N, u64* level_dom, const int* evt, con
       // Round 0 as a plain launch, one warp per task.
       const int warps = kFrontBlock / 32;
       const int blocks = std::max(1, (front_tasks(N, 2 * N.nb) + warps - 1) / warps);
-      k_front_first<WT, TB><<<blocks, kFrontBlock, 0, s>>>(N, level_dom, G, st);
-      cudaError_t e = cudaGetLastError();
+      cudaError_t e = launch_pdl(k_front_first<WT, TB>, dim3(blocks), dim3(kFrontBlock), 0, s, N, level_dom, G, st);
       if (e != cudaSuccess) return e;
       first = 1;
     }
@@ -2978,9 +3006,8 @@ cudaError_t launch_sac_branches(const DevNet& N, const u64* root, const int2* wo
     constexpr bool TB = decltype(tab)::value;
     cudaError_t e = allow_smem(k_sac<WT, TB>, smem);
     if (e != cudaSuccess) return e;
-    k_sac<WT, TB><<<grid, block, smem, s>>>(N, root, work, count, cursor, ok, st, static_cast<char*>(gscratch),
-                                            gstride, idx, gs_root);
-    return cudaGetLastError();
+    return launch_pdl(k_sac<WT, TB>, dim3(grid), dim3(block), smem, s, N, root, work, count, cursor, ok, st,
+                      static_cast<char*>(gscratch), gstride, idx, gs_root);
   });
 }
 
@@ -3008,9 +3035,8 @@ cudaError_t launch_sac_tile(const DevNet& N, u64* root, SacScratch S, uint8_t* o
     constexpr int WT = decltype(wt)::value;
     cudaError_t e = allow_smem(k_sac_tile<WT>, smem);
     if (e != cudaSuccess) return e;
-    k_sac_tile<WT><<<grid, block, smem, s>>>(N, root, S.snap, S.tiles, S.ntiles, S.tcursor, ok, S.deep, S.ndeep,
-                                             slot_cap, st, S.weak);
-    return cudaGetLastError();
+    return launch_pdl(k_sac_tile<WT>, dim3(grid), dim3(block), smem, s, N, root, S.snap, S.tiles, S.ntiles,
+                      S.tcursor, ok, S.deep, S.ndeep, slot_cap, st, S.weak);
   });
 }
 
@@ -3020,8 +3046,8 @@ cudaError_t launch_work_and_weak(const DevNet& N, const u64* dom, SacScratch S, 
     constexpr int WT = decltype(wt)::value;
     const int wb = std::max(1, std::min(4096, (N.n * 32 + 255) / 256));
     const int kb = std::max(1, std::min(8192, (2 * N.nb * 32 + 255) / 256));
-    k_work_and_weak<WT><<<wb + kb, 256, 0, s>>>(N, dom, S.work, S.nwork, S.tiles, S.ntiles, snap, weak, wb);
-    return cudaGetLastError();
+    return launch_pdl(k_work_and_weak<WT>, dim3(wb + kb), dim3(256), 0, s, N, dom, S.work, S.nwork, S.tiles,
+                      S.ntiles, snap, weak, wb);
   });
 }
 
@@ -3048,6 +3074,7 @@ __global__ void k_round_prep(KStats* st, int* ctl, int ctl_words) {
 // After the round's level AC has read the previous commit's events: the sweep
 // counters (nwork .. ndeep) and the changed-variable bitmap.
 __global__ void k_round_clear(int* ctr, int nctr, u32* fb, int nw) {
+  pdl_wait();
   for (int i = threadIdx.x; i < nctr; i += blockDim.x) ctr[i] = 0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nw; i += gridDim.x * blockDim.x) fb[i] = 0u;
 }
@@ -3074,16 +3101,14 @@ cudaError_t launch_round_prep(KStats* st, int* ctl, int ctl_words, cudaStream_t 
 
 cudaError_t launch_round_clear(int* ctr, int nctr, u32* fb, int nw, cudaStream_t s) {
   const int blocks = std::max(1, std::min(64, (nw + 255) / 256));
-  k_round_clear<<<blocks, 256, 0, s>>>(ctr, nctr, fb, nw);
-  return cudaGetLastError();
+  return launch_pdl(k_round_clear, dim3(blocks), dim3(256), 0, s, ctr, nctr, fb, nw);
 }
 
 cudaError_t launch_commit(const DevNet& N, u64* dom, SacScratch S, KStats* st, KStats* out, int nst,
                           cudaStream_t s) {
   const int blocks = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(4096, (N.total_values + 255) / 256)));
-  k_commit<<<blocks, 256, 0, s>>>(N.W, S.work, S.nwork, S.ok, dom, S.evt, S.nevt, S.evt_fb, st,
-                                  reinterpret_cast<unsigned*>(S.nwork + 7), out, nst);
-  return cudaGetLastError();
+  return launch_pdl(k_commit, dim3(blocks), dim3(256), 0, s, N.W, S.work, S.nwork, S.ok, dom, S.evt, S.nevt,
+                    S.evt_fb, st, reinterpret_cast<unsigned*>(S.nwork + 7), out, nst);
 }
 
 cudaError_t launch_transpose(const DevNet& N, u64* rel, const int* bx, const int* by, const int64_t* offA,
