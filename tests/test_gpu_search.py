@@ -251,3 +251,22 @@ def test_mac_domwdeg_matches_reference(golden, mode):
             if m["status"] == 1:
                 assert m["solution"] == r["solution"], c["args"]
             net.close()
+
+
+def test_search_block_sizes_give_the_same_search():
+    # cp_engine_set_search_block: any CTA size (a multiple of 32 up to 512)
+    # runs the same search; other sizes are refused.
+    inst = cp.gen_binary(50, 16, 250, 0.3, 0.3, 0.0, 4)
+    with cp.Engine(0) as eng:
+        for bad in (-32, 16, 33, 544):
+            with pytest.raises(cp.CPError):
+                eng.set_search_block(bad)
+        want = None
+        for block in (0, 32, 64, 128, 256, 512):
+            eng.set_search_block(block)
+            net = eng.upload(inst)
+            r = net.mac_solve()
+            net.close()
+            got = (r["status"], r["num_positive"], r["num_negative"], r["solution"])
+            want = want or got
+            assert got == want, block
