@@ -2273,12 +2273,19 @@ __device__ __forceinline__ void tile_one(const DevNet& N, u64* root, const u64* 
 // as count << 16 | v (0xffffffff past the end), then padding. One warp per
 // arc; the smallest keys are taken by repeated warp minima.
 template <int WT>
-__device__ void weak_list_arc(const DevNet& N, const u64* root, const u64 (&dy)[WT], int j, u32* weak) {
+__device__ void weak_list_arc(const DevNet& N, const u64* root, const Arc A, int j, u32* weak) {
   const int lane = threadIdx.x & 31;
-  const Arc A = N.arcs[j];
   const int z = A.z, dz = N.dsize[z];
-  u64 d0z[WT];
-  load_dom_uniform<WT>(root + static_cast<size_t>(z) * WT, d0z);
+  // D(y) (y = the arc's source) and D(z), both loaded before either is
+  // broadcast (one word per lane), so the two loads overlap.
+  const u64 wy = lane < WT ? vload(root + static_cast<size_t>(A.src) * WT + lane) : 0ull;
+  const u64 wz = lane < WT ? vload(root + static_cast<size_t>(z) * WT + lane) : 0ull;
+  u64 dy[WT], d0z[WT];
+#pragma unroll
+  for (int w = 0; w < WT; ++w) {
+    dy[w] = __shfl_sync(kFull, wy, w);
+    d0z[w] = __shfl_sync(kFull, wz, w);
+  }
   u32 key[2 * WT];
 #pragma unroll
   for (int t = 0; t < 2 * WT; ++t) {
@@ -2322,9 +2329,7 @@ __device__ void weak_list_arc(const DevNet& N, const u64* root, const u64 (&dy)[
 // Lists of all arcs of source variable y (one warp).
 template <int WT>
 __device__ void weak_lists_of(const DevNet& N, const u64* root, int y, u32* weak) {
-  u64 dy[WT];
-  load_dom_uniform<WT>(root + static_cast<size_t>(y) * WT, dy);
-  for (int j = N.arc_start[y]; j < N.arc_start[y + 1]; ++j) weak_list_arc<WT>(N, root, dy, j, weak);
+  for (int j = N.arc_start[y]; j < N.arc_start[y + 1]; ++j) weak_list_arc<WT>(N, root, N.arcs[j], j, weak);
 }
 
 // Weak-support lists of every arc, one warp per arc (block vb of vg blocks of
@@ -2334,17 +2339,7 @@ __device__ __forceinline__ void weak_body(const DevNet& N, const u64* root, u32*
   const int gw = (vb * blockDim.x + threadIdx.x) >> 5;
   const int nw = (vg * blockDim.x) >> 5;
   const int narcs = N.arc_start[N.n];
-  for (int j = gw; j < narcs; j += nw) {
-    // Source variable of arc j: the last y with arc_start[y] <= j.
-    int lo = 0, hi = N.n - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (N.arc_start[mid] <= j) lo = mid; else hi = mid - 1;
-    }
-    u64 dy[WT];
-    load_dom_uniform<WT>(root + static_cast<size_t>(lo) * WT, dy);
-    weak_list_arc<WT>(N, root, dy, j, weak);
-  }
+  for (int j = gw; j < narcs; j += nw) weak_list_arc<WT>(N, root, N.arcs[j], j, weak);
 }
 
 // The sweep's work list and its weak-support lists in one launch: the first
