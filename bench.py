@@ -15,8 +15,9 @@ L2 is flushed (a 256 MiB write) before every closure. e2e: the same metric
 through the C ABI with host buffers: every closure re-uploads the relations
 and domains from pinned host memory, runs cp_enforce_sac1 and reads the final
 domains back; two engines alternate, so that closure i+1's upload
-(cp_net_reload_async) overlaps closure i (e2e.sequential_value: the same
-without the overlap, cp_net_reload).
+(cp_net_reload_async) overlaps closure i, whose domains come back with
+cp_enforce_sac1_end_domains (e2e.sequential_value: the same without the
+overlap, cp_net_reload, cp_enforce_sac1 and cp_dom_get).
 
 Outside the timed region the line also carries: parity (every first-sweep
 singleton verdict and the SAC closure against the oracle on the host cores),
@@ -455,8 +456,7 @@ def run_ours(args):
             cur.enforce_sac1_begin(0)  # queued behind its own reload
             if i + 1 < count:
                 pair[(i + 1) % 2].reload_async(e2e_inst)
-            st = cur.enforce_sac1_end()
-            r = cur.dom_get(0)
+            st, r = cur.enforce_sac1_end_domains()  # the closure comes back with the call
             assert np.array_equal(r, final)
             br += st.branches
         return br, r
@@ -531,7 +531,7 @@ def run_ours(args):
                 "h2d_bytes_per_step": int(R * (inst.bin_rows.nbytes + inst.init.nbytes)),
                 "d2h_bytes_per_step": int(R * out.nbytes), "steps": e2e_steps,
                 "mode": "each closure's upload overlapped with the previous closure on a second engine "
-                        "(cp_net_reload_async)",
+                        "(cp_net_reload_async); the closure's domains returned by cp_enforce_sac1_end_domains",
                 "sequential_value": e2e_seq_value, "sequential_median_per_call": e2e_parts},
         "gpu_launches": int(gpu_launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

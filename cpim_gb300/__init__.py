@@ -110,6 +110,7 @@ def lib():
         "cp_enforce_sac1": ([vp, i, C.POINTER(Stats)], i),
         "cp_enforce_sac1_begin": ([vp, i], i),
         "cp_enforce_sac1_end": ([vp, C.POINTER(Stats)], i),
+        "cp_enforce_sac1_end_domains": ([vp, C.POINTER(Stats), P64], i),
         "cp_singletons": ([vp, i, i, PI, PI, PU8, i, C.POINTER(Stats)], i),
         "cp_sac_sweep": ([vp, i, P64, C.POINTER(C.c_int64), C.POINTER(Stats)], i),
         "cp_sac_tiles": ([vp, i, i, PI, PI, PI, i, P64, C.POINTER(C.c_double)], i),
@@ -415,6 +416,13 @@ class Net:
         st = Stats()
         _check(lib().cp_enforce_sac1_end(self._h, C.byref(st)))
         return st
+
+    def enforce_sac1_end_domains(self):
+        """Second half returning (stats, final domains of the level)."""
+        st = Stats()
+        out = np.zeros(self.n * self.W, np.uint64)
+        _check(lib().cp_enforce_sac1_end_domains(self._h, C.byref(st), _p(out, C.c_uint64)))
+        return st, out
 
     def singletons(self, vars_, vals, level=0, mode=0):
         v = np.ascontiguousarray(vars_, dtype=np.int32)

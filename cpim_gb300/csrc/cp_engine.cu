@@ -243,6 +243,7 @@ struct cp_net {
   void* h_block = nullptr;  // host-mapped pinned block holding h_stats, h_dom, h_sizes
   size_t h_block_bytes = 0;
   KStats* dh_stats = nullptr;  // device address of h_stats (written by k_stats_out)
+  u64* dh_dom = nullptr;       // device address of h_dom (the last SAC commit writes the closure there)
   int sac_pending_level = -1;  // level of a SAC1 call begun and not yet ended
   int sac_pending_launches = 0;
   // SAC1 rounds captured as CUDA graphs: [0] root AC + sweep, [1] events AC +
@@ -789,6 +790,7 @@ static int net_upload_impl(cp_engine* e, int n, const int* dom, int W, const uin
       void* dh = nullptr;
       CP_CUDA(cudaHostGetDevicePointer(&dh, net->h_block, 0));
       net->dh_stats = static_cast<KStats*>(dh);
+      net->dh_dom = reinterpret_cast<u64*>(static_cast<char*>(dh) + st_bytes);
     }
     net->h_dom = reinterpret_cast<u64*>(hb + st_bytes);
     net->h_sizes = reinterpret_cast<int*>(hb + st_bytes + dom_bytes);
@@ -1144,7 +1146,7 @@ int sac_round_launches(cp_net* net, int level, bool root, int& launches, bool ca
   // kernel's last block, or a one-block kernel), not by a copy node that
   // would queue behind other engines' transfers.
   if (!sweep_only) {
-    CP_CUDA(launch_commit(net->dn, net->level_ptr(level), S, net->d_stats, net->dh_stats, 2, s));
+    CP_CUDA(launch_commit(net->dn, net->level_ptr(level), S, net->d_stats, net->dh_stats, 2, net->dh_dom, s));
   } else {
     CP_CUDA(launch_stats_out(net->d_stats, net->dh_stats, 2, s));
   }
@@ -1226,7 +1228,7 @@ static int sac1_begin(cp_net* net, int level) {
   return CP_OK;
 }
 
-static int sac1_end(cp_net* net, cp_stats* st) {
+static int sac1_end(cp_net* net, cp_stats* st, uint64_t* domains = nullptr) {
   if (!net) return fail(CP_E_ARG, "null net");
   if (net->sac_pending_level < 0) return fail(CP_E_STATE, "no SAC1 call open on this network");
   const int level = net->sac_pending_level;
@@ -1270,6 +1272,17 @@ static int sac1_end(cp_net* net, cp_stats* st) {
     CP_CUDA(cudaEventRecord(e->ev1, s));
   }
   CP_CUDA(cudaEventSynchronize(e->ev1));
+  if (domains) {
+    // The last sweep removed nothing, so its commit kernel left the level in
+    // h_dom; otherwise (a wipe-out) the level is read back.
+    if (!inconsistent && net->h_stats[0].removed == 0) {
+      for (int x = 0; x < net->n; ++x)
+        for (int w = 0; w < net->W_user; ++w)
+          domains[static_cast<size_t>(x) * net->W_user + w] = net->h_dom[static_cast<size_t>(x) * net->W + w];
+    } else {
+      CP_TRY(fetch_level(net, level, domains));
+    }
+  }
   if (st) {
     acc.s.inconsistent = inconsistent ? 1 : 0;
     acc.s.deletions = acc.dels;
@@ -1292,6 +1305,11 @@ int cp_enforce_sac1(cp_net* net, int level, cp_stats* st) {
 int cp_enforce_sac1_begin(cp_net* net, int level) { return sac1_begin(net, level); }
 
 int cp_enforce_sac1_end(cp_net* net, cp_stats* st) { return sac1_end(net, st); }
+
+int cp_enforce_sac1_end_domains(cp_net* net, cp_stats* st, uint64_t* domains) {
+  if (!domains) return fail(CP_E_ARG, "null domains");
+  return sac1_end(net, st, domains);
+}
 
 int cp_sac_sweep(cp_net* net, int level, uint64_t* verdict, int64_t* deep, cp_stats* st) {
   if (!net || !verdict) return fail(CP_E_ARG, "null argument");

@@ -283,9 +283,11 @@ cudaError_t launch_round_prep(KStats* st, int* ctl, int ctl_words, cudaStream_t 
 cudaError_t launch_stats_out(const KStats* src, KStats* dst, int k, cudaStream_t s);
 cudaError_t launch_round_clear(int* ctr, int nctr, u32* fb, int nw, cudaStream_t s);
 // Removes failed pairs from the level, collecting changed variables.
-// out (host-mapped, may be null): the last block copies nst stats slots there;
-// S.nwork + 7 is its completion counter (zero between launches).
-cudaError_t launch_commit(const DevNet& N, u64* dom, SacScratch S, KStats* st, KStats* out, int nst,
+// out (host-mapped, may be null): the last block copies nst stats slots there
+// and, with dom_out (host-mapped, may be null) and no removal in the sweep,
+// the level's n * W words; S.nwork + 7 is its completion counter (zero
+// between launches).
+cudaError_t launch_commit(const DevNet& N, u64* dom, SacScratch S, KStats* st, KStats* out, int nst, u64* dom_out,
                           cudaStream_t s);
 // Builds the B blocks (transposes) of the binary relations.
 cudaError_t launch_transpose(const DevNet& N, u64* rel, const int* bx, const int* by, const int64_t* offA,

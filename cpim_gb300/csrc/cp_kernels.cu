@@ -2402,9 +2402,12 @@ __global__ void __launch_bounds__(256, WT <= 2 ? 5 : 1) k_sac_tile(DevNet N, u64
 }
 
 // With out: the last block to finish (counted on done, which it resets)
-// copies the round's nst stats slots into host-mapped memory.
+// copies the round's nst stats slots into host-mapped memory and, with
+// dom_out, when the sweep removed nothing (the level is the closure), the
+// level's dom_words words too.
 __global__ void k_commit(int W, const int2* work, const int* nwork, const uint8_t* ok, u64* dom, int* evt, int* nevt,
-                         u32* evt_fb, KStats* st, unsigned* done, KStats* out, int nst) {
+                         u32* evt_fb, KStats* st, unsigned* done, KStats* out, int nst, u64* dom_out,
+                         size_t dom_words) {
   pdl_wait();
   const int total = *nwork;
   u64 removed = 0;
@@ -2431,6 +2434,8 @@ __global__ void k_commit(int W, const int2* work, const int* nwork, const uint8_
   const int* a = reinterpret_cast<const int*>(st);
   int* b = reinterpret_cast<int*>(out);
   for (int i = threadIdx.x; i < nst * kw; i += blockDim.x) b[i] = __ldcg(a + i);
+  if (dom_out && __ldcg(&st->removed) == 0)
+    for (size_t i = threadIdx.x; i < dom_words; i += blockDim.x) dom_out[i] = __ldcg(dom + i);
   __threadfence_system();
   if (threadIdx.x == 0) *done = 0u;
 }
@@ -3099,11 +3104,12 @@ cudaError_t launch_round_clear(int* ctr, int nctr, u32* fb, int nw, cudaStream_t
   return launch_pdl(k_round_clear, dim3(blocks), dim3(256), 0, s, ctr, nctr, fb, nw);
 }
 
-cudaError_t launch_commit(const DevNet& N, u64* dom, SacScratch S, KStats* st, KStats* out, int nst,
+cudaError_t launch_commit(const DevNet& N, u64* dom, SacScratch S, KStats* st, KStats* out, int nst, u64* dom_out,
                           cudaStream_t s) {
   const int blocks = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(4096, (N.total_values + 255) / 256)));
   return launch_pdl(k_commit, dim3(blocks), dim3(256), 0, s, N.W, S.work, S.nwork, S.ok, dom, S.evt, S.nevt,
-                    S.evt_fb, st, reinterpret_cast<unsigned*>(S.nwork + 7), out, nst);
+                    S.evt_fb, st, reinterpret_cast<unsigned*>(S.nwork + 7), out, nst, dom_out,
+                    static_cast<size_t>(N.n) * N.W);
 }
 
 cudaError_t launch_transpose(const DevNet& N, u64* rel, const int* bx, const int* by, const int64_t* offA,

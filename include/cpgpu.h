@@ -173,6 +173,10 @@ int cp_enforce_sac1(cp_net* net, int level, cp_stats* st);
  * reference. */
 int cp_enforce_sac1_begin(cp_net* net, int level);
 int cp_enforce_sac1_end(cp_net* net, cp_stats* st);
+/* _end that also returns the level's final domains (n*W words, as
+ * cp_dom_get): the last sweep's commit kernel writes them to host memory, so
+ * no separate read-back follows. */
+int cp_enforce_sac1_end_domains(cp_net* net, cp_stats* st, uint64_t* domains);
 /* Singleton tests of `count` pairs (vars[i], vals[i]) against the domains of
  * `level` without changing them: ok[i] = 1 if the AC fixpoint of the level
  * with vars[i] reduced to vals[i] is consistent. mode 0 = batched persistent

@@ -401,4 +401,12 @@ def test_sac1_begin_end_equals_enforce():
             net.dom_set(0, inst.init)
             st2 = net.enforce_sac1(0)
             assert (st2.inconsistent, st2.deletions, st2.sweeps) == (st.inconsistent, st.deletions, st.sweeps)
+            # _end_domains returns the closure with the call.
+            net.dom_set(0, inst.init)
+            net.enforce_sac1_begin(0)
+            st3, d3 = net.enforce_sac1_end_domains()
+            assert (st3.inconsistent, st3.deletions, st3.sweeps) == (st.inconsistent, st.deletions, st.sweeps)
+            if ok:
+                assert np.array_equal(d3, d)
+                assert np.array_equal(net.dom_get(0), d)
             net.close()
