@@ -2302,27 +2302,54 @@ __device__ void weak_list_arc(const DevNet& N, const u64* root, const Arc A, int
   }
   u32* out = weak + static_cast<size_t>(j) * kWeakStride;
   if (lane > kWeakK && lane < kWeakStride) out[lane] = 0xffffffffu;  // padding
-  for (int k = 0; k <= kWeakK; ++k) {
-    u32 m = key[0];
-#pragma unroll
-    for (int t = 1; t < 2 * WT; ++t) m = min(m, key[t]);
-    m = __reduce_min_sync(kFull, m);
+  // Writes the k-th smallest key m; true once the keys are exhausted.
+  auto emit = [&](int k, u32 m) -> bool {
     if (lane == 0) {
       if (k < kWeakK)
         out[1 + k] = m;
       else
         out[0] = m | 0xffffu;
     }
-    if (m == 0xffffffffu) {
-      if (lane == 0) {
-        for (int r = k + 1; r < kWeakK; ++r) out[1 + r] = 0xffffffffu;
-        out[0] = 0xffffffffu;
-      }
-      break;
+    if (m != 0xffffffffu) return false;
+    if (lane == 0) {
+      for (int r = k + 1; r < kWeakK; ++r) out[1 + r] = 0xffffffffu;
+      out[0] = 0xffffffffu;
     }
+    return true;
+  };
+  if constexpr (WT <= 4) {
+    // Each lane's keys in increasing order (odd-even transposition); a step
+    // then takes the warp minimum of the lanes' first keys, and the lane that
+    // owns it (keys are distinct) moves on to its next key.
 #pragma unroll
-    for (int t = 0; t < 2 * WT; ++t)
-      if (key[t] == m) key[t] = 0xffffffffu;
+    for (int i = 0; i < 2 * WT; ++i) {
+#pragma unroll
+      for (int t = i & 1; t + 1 < 2 * WT; t += 2) {
+        const u32 a = key[t], b = key[t + 1];
+        key[t] = min(a, b);
+        key[t + 1] = max(a, b);
+      }
+    }
+    for (int k = 0; k <= kWeakK; ++k) {
+      const u32 m = __reduce_min_sync(kFull, key[0]);
+      if (emit(k, m)) break;
+      if (key[0] == m) {
+#pragma unroll
+        for (int t = 0; t + 1 < 2 * WT; ++t) key[t] = key[t + 1];
+        key[2 * WT - 1] = 0xffffffffu;
+      }
+    }
+  } else {
+    for (int k = 0; k <= kWeakK; ++k) {
+      u32 m = key[0];
+#pragma unroll
+      for (int t = 1; t < 2 * WT; ++t) m = min(m, key[t]);
+      m = __reduce_min_sync(kFull, m);
+      if (emit(k, m)) break;
+#pragma unroll
+      for (int t = 0; t < 2 * WT; ++t)
+        if (key[t] == m) key[t] = 0xffffffffu;
+    }
   }
 }
 
