@@ -144,10 +144,9 @@ def read_benchmark_list(path):
 
 
 def dump_network(inst, path):
-    """A binary network as the text format of the reference driver's `file`
-    mode: "n W", domain sizes, initial words, "nb", scope pairs, rows."""
-    if inst.n_tab:
-        raise ValueError("binary networks only")
+    """A network as the text format of the reference driver's `file` mode:
+    "n W", domain sizes, initial words, "nb", scope pairs, rows, then (with
+    tables) "nt" and per table its arity, scope, tuple count and tuples."""
     with open(path, "w") as f:
         f.write("%d %d\n" % (inst.n, inst.W))
         f.write(" ".join(str(int(d)) for d in inst.dom) + "\n")
@@ -155,3 +154,12 @@ def dump_network(inst, path):
         f.write("%d\n" % inst.n_bin)
         f.write(" ".join(str(int(v)) for v in inst.bin_scope) + "\n")
         f.write(" ".join(str(int(w)) for w in inst.bin_rows) + "\n")
+        if inst.n_tab:
+            f.write("%d\n" % inst.n_tab)
+            so = to = 0
+            for t in range(inst.n_tab):
+                r, k = int(inst.tab_arity[t]), int(inst.tab_ntup[t])
+                f.write("%d %s %d\n" % (r, " ".join(str(int(v)) for v in inst.tab_scope[so:so + r]), k))
+                f.write(" ".join(str(int(v)) for v in inst.tab_tuples[to:to + k * r]) + "\n")
+                so += r
+                to += k * r

@@ -123,6 +123,34 @@ int main(int argc, char** argv) {
       std::cerr << "truncated network file" << std::endl;
       return 2;
     }
+    // Optional positive tables: "nt", then per table its arity, scope,
+    // tuple count and tuples.
+    int nt = 0;
+    if (in >> nt) {
+      for (int t = 0; t < nt; ++t) {
+        int r = 0, k = 0;
+        in >> r;
+        I.tarity.push_back(r);
+        I.tscope_off.push_back(int64_t(I.tscope.size()));
+        for (int q = 0; q < r; ++q) {
+          int v = 0;
+          in >> v;
+          I.tscope.push_back(v);
+        }
+        in >> k;
+        I.tntup.push_back(k);
+        I.ttup_off.push_back(int64_t(I.ttup.size()));
+        for (int64_t q = 0; q < int64_t(k) * r; ++q) {
+          int v = 0;
+          in >> v;
+          I.ttup.push_back(v);
+        }
+      }
+      if (!in) {
+        std::cerr << "truncated table section" << std::endl;
+        return 2;
+      }
+    }
     i = 3;
   } else if (kind == "uneven" && argc >= 7) {
     I = cpgen::uneven_instance(std::strtoull(argv[2], nullptr, 10), std::atoi(argv[3]), std::atoi(argv[4]),

@@ -104,3 +104,24 @@ def test_nary_batch_matches_oracle(engine):
     b.close()
     for n in nets:
         n.close()
+
+
+def test_nary_gac_matches_reference_runs(engine):
+    # The device's GAC against the reference's own generic AC3 on networks
+    # whose tables all have one arity (tests/golden/nary_reference_cases.json).
+    import json
+    import os
+    from tests.golden_cases import dom_hex
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "nary_reference_cases.json")
+    with open(path) as f:
+        cases = json.load(f)["cases"]
+    for c in cases:
+        kw = {k: tuple(v) if isinstance(v, list) else v for k, v in c["kwargs"].items()}
+        net = engine.upload(to_engine(nary_arrays(c["seed"], **kw)))
+        st = net.enforce_ac(0)
+        ref = c["result"]
+        assert bool(st.inconsistent) == (not ref["consistent"]), (c["name"], c["seed"])
+        if ref["consistent"]:
+            assert st.deletions == ref["deletions"], (c["name"], c["seed"])
+            assert dom_hex(net.dom_get(0)) == ref["domains"], (c["name"], c["seed"])
+        net.close()

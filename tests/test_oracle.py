@@ -302,3 +302,30 @@ def test_nary_cases_pinned_by_definition():
                 if inst.n <= 48:
                     oks, ds, _ = O.sac1(inst)
                     assert not oks or np.all((ds & ~d1) == 0), (name, seed)
+
+
+def _nary_reference_cases():
+    import json
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "nary_reference_cases.json")
+    with open(path) as f:
+        cases = json.load(f)["cases"]
+    for c in cases:
+        c["kwargs"] = {k: tuple(v) if isinstance(v, list) else v for k, v in c["kwargs"].items()}
+    return cases
+
+
+def test_nary_gac_pinned_by_reference_ac3():
+    # Networks whose tables all have one arity (2 .. 12, domains up to 300
+    # values): the reference's own generic AC3 (run by
+    # tests/golden/make_nary_golden.py) and the oracle's GAC agree on the
+    # verdict, the deletions and every domain word.
+    from tests.nary_cases import nary_arrays, to_oracle
+    for c in _nary_reference_cases():
+        inst = to_oracle(nary_arrays(c["seed"], **c["kwargs"]))
+        ok, d, dels = O.gac(inst)
+        ref = c["result"]
+        assert ok == ref["consistent"], (c["name"], c["seed"])
+        if ok:
+            assert dels == ref["deletions"], (c["name"], c["seed"])
+            assert O.dom_hex(d) == ref["domains"], (c["name"], c["seed"])
