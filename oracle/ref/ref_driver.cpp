@@ -182,8 +182,9 @@ int main(int argc, char** argv) {
     out << ", \"consistent\": " << (cs.state ? "true" : "false") << ", \"deletions\": " << cs.num_delete;
     if (cs.state) out << ", \"domains\": \"" << domains_hex(net, I, 0) << "\"";
     delete ac;
-  } else if (op == "sac1") {
-    SAC1 sac(&net, AC_3bit);
+  } else if (op == "sac1" || op == "sac1_ac3") {
+    // sac1_ac3: SAC1 over the generic AC3 (tables of any arity).
+    SAC1 sac(&net, op == "sac1" ? AC_3bit : AC_3);
     bool ok;
     {
       Silence s;

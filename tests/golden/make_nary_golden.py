@@ -4,7 +4,8 @@ sources by oracle/ref/Makefile into oracle/_ref/ref_driver: each network
 (tests/nary_cases.py's seeded generator) is written in the driver's `file`
 format and propagated by AC3 there. On networks whose tables all have the
 same arity the reference's generic revise is exact (its defect needs mixed
-arities), so these pin the oracle's GAC and, through it, the device's.
+arities), so these pin the oracle's GAC and, through it, the device's; on the
+small-domain ones the reference's SAC1 over that AC3 pins the oracle's SAC1.
 
     python tests/golden/make_nary_golden.py   # writes nary_reference_cases.json
 """
@@ -37,13 +38,13 @@ SHAPES = [
 SEEDS = (1, 2, 3, 4, 5)
 
 
-def run(kw, seed):
+def run(kw, seed, op="ac3"):
     inst = to_engine(nary_arrays(seed, **kw))
     with tempfile.NamedTemporaryFile("w", suffix=".net", delete=False) as f:
         path = f.name
     try:
         dump_network(inst, path)
-        r = subprocess.run([DRIVER, "file", path, "ac3"], capture_output=True, text=True, check=True, timeout=600)
+        r = subprocess.run([DRIVER, "file", path, op], capture_output=True, text=True, check=True, timeout=600)
     finally:
         os.unlink(path)
     res = json.loads(r.stdout)
@@ -57,10 +58,16 @@ def main():
     cases = []
     for name, kw in SHAPES:
         for seed in SEEDS:
-            cases.append({"name": name, "kwargs": {k: list(v) if isinstance(v, tuple) else v for k, v in kw.items()},
-                          "seed": seed, "result": run(kw, seed)})
+            case = {"name": name, "kwargs": {k: list(v) if isinstance(v, tuple) else v for k, v in kw.items()},
+                    "seed": seed, "result": run(kw, seed)}
+            # SAC1 over the generic AC3 (the driver's op sac1_ac3) where its
+            # tuple enumeration is affordable (domains of at most 16 values).
+            if kw["d"] <= 16:
+                case["sac1"] = run(kw, seed, "sac1_ac3")
+            cases.append(case)
     with open(OUT, "w") as f:
-        json.dump({"generator": "tests/nary_cases.py", "driver": "oracle/ref/ref_driver.cpp (op ac3, file mode)",
+        json.dump({"generator": "tests/nary_cases.py",
+                   "driver": "oracle/ref/ref_driver.cpp (ops ac3 and sac1_ac3, file mode)",
                    "cases": cases}, f, indent=1)
     print("%d cases -> %s" % (len(cases), OUT))
 

@@ -329,3 +329,22 @@ def test_nary_gac_pinned_by_reference_ac3():
         if ok:
             assert dels == ref["deletions"], (c["name"], c["seed"])
             assert O.dom_hex(d) == ref["domains"], (c["name"], c["seed"])
+
+
+def test_nary_sac1_pinned_by_reference():
+    # The same one-arity networks (domains of at most 16 values): the
+    # reference's SAC1 over its generic AC3 and the oracle's SAC1 agree on the
+    # verdict and, when consistent, on the deletions and every domain word.
+    from tests.nary_cases import nary_arrays, to_oracle
+    n = 0
+    for c in _nary_reference_cases():
+        if "sac1" not in c:
+            continue
+        ok, d, dels = O.sac1(to_oracle(nary_arrays(c["seed"], **c["kwargs"])))
+        ref = c["sac1"]
+        assert ok == ref["consistent"], (c["name"], c["seed"])
+        if ok:
+            assert dels == ref["deletions"], (c["name"], c["seed"])
+            assert O.dom_hex(d) == ref["domains"], (c["name"], c["seed"])
+        n += 1
+    assert n >= 30
