@@ -192,11 +192,13 @@ int main(int argc, char** argv) {
     }
     out << ", \"consistent\": " << (ok ? "true" : "false") << ", \"deletions\": " << sac.del();
     if (ok) out << ", \"domains\": \"" << domains_hex(net, I, 0) << "\"";
-  } else if (op == "mac" || op == "mac_domdeg" || op == "mac_domwdeg") {
-    const Heuristic::Var vh = op == "mac" ? Heuristic::VRH_DOM_MIN
-                              : op == "mac_domdeg" ? Heuristic::VRH_DOM_DEG_MIN
-                                                   : Heuristic::VRH_DOM_WDEG_MIN;
-    MAC mac(&net, AC_3bit, vh, Heuristic::VLH_MIN);
+  } else if (op == "mac" || op == "mac_domdeg" || op == "mac_domwdeg" || op == "mac_ac3" || op == "mac_ac3_domdeg") {
+    // mac_ac3*: MAC over the generic AC3 (tables of any arity).
+    const Heuristic::Var vh = (op == "mac" || op == "mac_ac3") ? Heuristic::VRH_DOM_MIN
+                              : (op == "mac_domdeg" || op == "mac_ac3_domdeg") ? Heuristic::VRH_DOM_DEG_MIN
+                                                                               : Heuristic::VRH_DOM_WDEG_MIN;
+    const bool generic = op == "mac_ac3" || op == "mac_ac3_domdeg";
+    MAC mac(&net, generic ? AC_3 : AC_3bit, vh, Heuristic::VLH_MIN);
     SearchStatistics st;
     const double t0 = now_s();
     {

@@ -5,7 +5,8 @@ sources by oracle/ref/Makefile into oracle/_ref/ref_driver: each network
 format and propagated by AC3 there. On networks whose tables all have the
 same arity the reference's generic revise is exact (its defect needs mixed
 arities), so these pin the oracle's GAC and, through it, the device's; on the
-small-domain ones the reference's SAC1 over that AC3 pins the oracle's SAC1.
+small-domain ones the reference's SAC1 and MAC (dom/min, dom/deg) over that
+AC3 pin the oracle's SAC1 and MAC.
 
     python tests/golden/make_nary_golden.py   # writes nary_reference_cases.json
 """
@@ -38,17 +39,19 @@ SHAPES = [
 SEEDS = (1, 2, 3, 4, 5)
 
 
-def run(kw, seed, op="ac3"):
+def run(kw, seed, op="ac3", arg=None):
     inst = to_engine(nary_arrays(seed, **kw))
     with tempfile.NamedTemporaryFile("w", suffix=".net", delete=False) as f:
         path = f.name
     try:
         dump_network(inst, path)
-        r = subprocess.run([DRIVER, "file", path, op], capture_output=True, text=True, check=True, timeout=600)
+        cmd = [DRIVER, "file", path, op] + ([str(arg)] if arg is not None else [])
+        r = subprocess.run(cmd, capture_output=True, text=True, check=True, timeout=600)
     finally:
         os.unlink(path)
     res = json.loads(r.stdout)
     res.pop("fingerprint", None)
+    res.pop("solve_ms", None)  # a timing, not a result
     return res
 
 
@@ -64,10 +67,14 @@ def main():
             # tuple enumeration is affordable (domains of at most 16 values).
             if kw["d"] <= 16:
                 case["sac1"] = run(kw, seed, "sac1_ac3")
+                # MAC over the generic AC3 to the first solution, dom/min and
+                # dom/deg (ops mac_ac3, mac_ac3_domdeg; 20 s limit).
+                case["mac"] = run(kw, seed, "mac_ac3", 20000)
+                case["mac_domdeg"] = run(kw, seed, "mac_ac3_domdeg", 20000)
             cases.append(case)
     with open(OUT, "w") as f:
         json.dump({"generator": "tests/nary_cases.py",
-                   "driver": "oracle/ref/ref_driver.cpp (ops ac3 and sac1_ac3, file mode)",
+                   "driver": "oracle/ref/ref_driver.cpp (ops ac3, sac1_ac3, mac_ac3, mac_ac3_domdeg; file mode)",
                    "cases": cases}, f, indent=1)
     print("%d cases -> %s" % (len(cases), OUT))
 

@@ -348,3 +348,22 @@ def test_nary_sac1_pinned_by_reference():
             assert O.dom_hex(d) == ref["domains"], (c["name"], c["seed"])
         n += 1
     assert n >= 30
+
+
+def test_nary_mac_pinned_by_reference():
+    # The same one-arity networks: the reference's MAC over its generic AC3
+    # (dom/min and dom/deg, min value) and the oracle's MAC agree on the node
+    # counts and the first solution.
+    from tests.nary_cases import nary_arrays, to_oracle
+    n = 0
+    for c in _nary_reference_cases():
+        for key, varh in (("mac", 1), ("mac_domdeg", 4)):
+            if key not in c:
+                continue
+            ref = c[key]
+            assert not ref["time_out"]
+            m = O.mac(to_oracle(nary_arrays(c["seed"], **c["kwargs"])), varh=varh)
+            assert (m["num_positive"], m["num_negative"]) == (ref["num_positive"], ref["num_negative"]), (c["name"], key)
+            assert m["solution"] == (ref["solution"] if ref["num_sol"] else []), (c["name"], key)
+            n += 1
+    assert n >= 60
