@@ -125,3 +125,34 @@ def test_nary_gac_matches_reference_runs(engine):
             assert st.deletions == ref["deletions"], (c["name"], c["seed"])
             assert dom_hex(net.dom_get(0)) == ref["domains"], (c["name"], c["seed"])
         net.close()
+
+
+def test_nary_sac1_and_mac_match_reference_runs(engine):
+    # The device's SAC1 and MAC (dom/min, dom/deg) against the reference's own
+    # SAC1 and MAC over its generic AC3 on the one-arity networks of at most
+    # 16 values (tests/golden/nary_reference_cases.json).
+    import json
+    import os
+    from tests.golden_cases import dom_hex
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "nary_reference_cases.json")
+    with open(path) as f:
+        cases = [c for c in json.load(f)["cases"] if "sac1" in c]
+    assert len(cases) >= 30
+    for c in cases:
+        kw = {k: tuple(v) if isinstance(v, list) else v for k, v in c["kwargs"].items()}
+        arrays = nary_arrays(c["seed"], **kw)
+        net = engine.upload(to_engine(arrays))
+        st = net.enforce_sac1(0)
+        ref = c["sac1"]
+        assert bool(st.inconsistent) == (not ref["consistent"]), (c["name"], c["seed"])
+        if ref["consistent"]:
+            assert st.deletions == ref["deletions"], (c["name"], c["seed"])
+            assert dom_hex(net.dom_get(0)) == ref["domains"], (c["name"], c["seed"])
+        net.close()
+        for key, varh in (("mac", cp.VarHeuristic.VRH_DOM_MIN), ("mac_domdeg", cp.VarHeuristic.VRH_DOM_DEG_MIN)):
+            ref = c[key]
+            net = engine.upload(to_engine(arrays))
+            r = net.mac_solve(var_h=varh)
+            net.close()
+            assert (r["num_positive"], r["num_negative"]) == (ref["num_positive"], ref["num_negative"]), (c["name"], key)
+            assert r["solution"] == (ref["solution"] if ref["num_sol"] else []), (c["name"], key)
